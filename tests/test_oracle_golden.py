@@ -1,0 +1,102 @@
+"""Pin the CPU oracle to golden vectors produced by the reference's own code
+(tests/golden/make_golden.py runs trot's modules unmodified)."""
+import numpy as np
+import pytest
+
+from oracle import afqmc_oracle as orc
+from tests.golden_model import model_from_golden, rel_err, state_from_golden, walkers_from_golden
+
+TOL = 1e-11
+
+
+def test_prop_ctx(golden):
+    m = model_from_golden(golden)
+    assert rel_err(m.prop.mf_shifts, golden["mf_shifts"]) < TOL
+    h0p = complex(golden["h0_prop"])
+    assert h0p.imag == 0.0
+    assert abs(m.prop.h0_prop - h0p.real) < TOL * max(1, abs(h0p.real))
+    assert rel_err(m.prop.exp_h1_half, golden["exp_h1_half"]) < TOL
+
+
+def test_overlap_force_bias_energy(golden):
+    m = model_from_golden(golden)
+    w = walkers_from_golden(golden)
+    assert rel_err(m.overlap(w), golden["overlap"]) < TOL
+    assert rel_err(m.force_bias(w), golden["force_bias"]) < TOL
+    assert rel_err(m.energy(w), golden["energy"]) < TOL
+
+
+def test_trotter(golden):
+    m = model_from_golden(golden)
+    w = walkers_from_golden(golden)
+    out = m.trotter(w, golden["trotter_fields"], 6)
+    if m.kind == "rhf_r":
+        assert rel_err(out, golden["trotter_out"]) < TOL
+    else:
+        assert rel_err(out[0], golden["trotter_out_u"]) < TOL
+        assert rel_err(out[1], golden["trotter_out_d"]) < TOL
+
+
+def _check_state(st, golden, prefix, kind):
+    w = walkers_from_golden(golden, prefix)
+    if kind == "rhf_r":
+        assert rel_err(st.walkers, w) < TOL
+    else:
+        assert rel_err(st.walkers[0], w[0]) < TOL
+        assert rel_err(st.walkers[1], w[1]) < TOL
+    assert rel_err(st.weights, golden[prefix + "weights"]) < TOL
+    assert rel_err(st.overlaps, golden[prefix + "overlaps"]) < TOL
+    assert abs(st.pop_control_ene_shift - float(golden[prefix + "shift"])) < 1e-9
+    assert abs(st.e_estimate - float(golden[prefix + "e_estimate"])) < 1e-9
+    assert st.node_encounters == int(golden[prefix + "nodes"])
+
+
+def test_step(golden):
+    m = model_from_golden(golden)
+    params = orc.Params(dt=float(golden["dt"]))
+    st = orc.afqmc_step(state_from_golden(golden), m, params, golden["step_fields"][0])
+    _check_state(st, golden, "step1_", m.kind)
+
+
+def test_block(golden):
+    m = model_from_golden(golden)
+    params = orc.Params(dt=float(golden["dt"]))
+    st, e_block, w_sum = orc.block(state_from_golden(golden), m, params, golden["step_fields"],
+                                   float(golden["zeta"]))
+    _check_state(st, golden, "block_", m.kind)
+    assert abs(e_block - float(golden["block_energy"])) < 1e-9 * max(1, abs(e_block))
+    assert abs(w_sum - float(golden["block_weight"])) < 1e-12 * max(1, w_sum)
+
+
+def test_qr_and_sr(golden):
+    m = model_from_golden(golden)
+    w = walkers_from_golden(golden)
+    q, norm = orc.orthogonalize(w, m.walker_kind)
+    if m.kind == "rhf_r":
+        assert rel_err(q, golden["qr_out"]) < 1e-12
+    else:
+        assert rel_err(q[0], golden["qr_out_u"]) < 1e-12
+        assert rel_err(q[1], golden["qr_out_d"]) < 1e-12
+    assert rel_err(norm, golden["qr_norm"]) < 1e-12
+    sr_w = golden["sr_weights_in"]
+    idx = orc.sr_indices(sr_w, float(golden["sr_zeta"]), sr_w.shape[0])
+    np.testing.assert_array_equal(idx, golden["sr_idx"])
+    _, wn, _ = orc.stochastic_reconfiguration(w, sr_w, float(golden["sr_zeta"]), m.walker_kind)
+    np.testing.assert_array_equal(wn, golden["sr_weights_out"])
+
+
+def test_init_walkers(golden):
+    m = model_from_golden(golden)
+    mo_a, mo_b = golden["mo_a"], golden["mo_b"]
+    rdm1 = np.stack([mo_a @ mo_a.T, mo_b @ mo_b.T])
+    na, nb = mo_a.shape[1], mo_b.shape[1]
+    iw = orc.init_walkers(m.walker_kind, rdm1, na, nb, 2)
+    # eigenvectors are unique up to sign: compare the projectors w w^H
+    if m.kind == "rhf_r":
+        pairs = [(iw, golden["init_walkers"])]
+    else:
+        pairs = [(iw[0], golden["init_walkers_u"]), (iw[1], golden["init_walkers_d"])]
+    for a, b in pairs:
+        pa = a @ np.conj(np.swapaxes(a, -1, -2))
+        pb = b @ np.conj(np.swapaxes(b, -1, -2))
+        assert rel_err(pa, pb) < 1e-10
