@@ -1,0 +1,369 @@
+"""Walker-steps/s of the phaseless-AFQMC hot path (prop + E_L every step).
+
+Default workload: UHF trial, N=120 orbitals, (12, 10) electrons, G=600
+Cholesky vectors (decay length 150), 1024 walkers, dt=0.005, QR + block tail
+(overlaps, block energy, SR) every 10 steps; seeded synthetic Hamiltonian.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
+                    [--impl ours|reference] [--config NAME]
+
+Prints one JSON line (rank 0).  Under torchrun with N > 1 every rank runs an
+independent replica of the workload (the path does not shard), the timed
+region is bracketed by barriers, and the max time over ranks is used.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "walker-steps/s (prop+E_L), mixed vs FP64 on 1 GB300 at |ΔE_L|≤1e-5 Ha"
+UNIT = "walker-steps/s"
+
+
+def flops_per_walker_step(N, na, nb, G, nterms=6):
+    """Algorithmic flops of one walker-step (reference contraction order;
+    complex x real = 4 flop per MAC, complex x complex = 8)."""
+    ns, sq = na + nb, na * na + nb * nb
+    d = {
+        "green": 4 * N * sq + 8 * sq * N,
+        "force_bias": 4 * G * ns * N,
+        "vhs": 4 * G * N * N,
+        "taylor": nterms * 8 * N * N * ns,
+        "onebody": 2 * 4 * N * N * ns,
+        "overlap": 4 * N * sq + 6 * (na ** 3 + nb ** 3),
+        "exchange": 4 * G * sq * N,
+        "energy_rest": 8 * G * sq + 8 * ns * N,
+    }
+    return d
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------
+def build_workload(cfg, precision):
+    import torch
+
+    import trot_gb300 as tg
+    from trot_gb300 import synthetic
+
+    N, (na, nb), G, W = cfg["norb"], cfg["nelec"], cfg["nchol"], cfg["n_walkers"]
+    ss = synthetic.make_system(N, (na, nb), G, decay=cfg["decay"], seed=0, h0=0.0)
+    kind = cfg["kind"]
+    wk = "restricted" if kind == "rhf_r" else "unrestricted"
+    sysm = tg.System(norb=N, nelec=(na, nb), walker_kind=wk)
+    ham = tg.HamChol(h0=ss.h0, h1=ss.h1, chol=ss.chol)
+    params = tg.QmcParams(dt=cfg["dt"], n_walkers=W, n_prop_steps=cfg["qr_every"], seed=1234)
+    if kind == "uhf_u":
+        trial = tg.UhfTrial(ss.mo_a, ss.mo_b)
+        trial_ops, meas_ops = tg.make_uhf_trial_ops(sysm), tg.make_uhf_meas_ops(sysm)
+    else:
+        trial = tg.RhfTrial(ss.mo_a)
+        trial_ops, meas_ops = tg.make_rhf_trial_ops(sysm), tg.make_rhf_meas_ops(sysm)
+    meas_ctx = meas_ops.build_meas_ctx(ham, trial)
+    prop_ops = tg.make_prop_ops("restricted", wk, mixed_precision=(precision == "mixed"))
+    prop_ctx = prop_ops.build_prop_ctx(ham, trial_ops.get_rdm1(trial), params)
+    state = prop_ops.init_prop_state(sys=sysm, ham_data=ham, trial_ops=trial_ops, trial_data=trial,
+                                     meas_ops=meas_ops, params=params)
+    e = torch.empty(W, dtype=torch.complex128, device="cuda")
+    return dict(tg=tg, ss=ss, sys=sysm, ham=ham, params=params, trial=trial, trial_ops=trial_ops,
+                meas_ops=meas_ops, meas_ctx=meas_ctx, prop_ops=prop_ops, prop_ctx=prop_ctx, state=state, e=e,
+                W=W, N=N, na=na, nb=nb, G=G, qr_every=cfg["qr_every"], kind=kind)
+
+
+def run_steps(wl, nsteps, k0=0, fields_host=None, pinned_e=None):
+    """nsteps walker-steps (prop + E_L each step) plus the block tail every
+    qr_every steps.  With fields_host/pinned_e the fields come from pinned host
+    memory and each step's energies are copied back (end-to-end mode)."""
+    import torch
+
+    tg = wl["tg"]
+    st = wl["state"]
+    for k in range(k0, k0 + nsteps):
+        fields = None
+        if fields_host is not None:
+            fields = fields_host[k % fields_host.shape[0]].to("cuda", non_blocking=True)
+        st = wl["prop_ops"].step(st, params=wl["params"], ham_data=wl["ham"], trial_data=wl["trial"],
+                                 trial_ops=wl["trial_ops"], meas_ops=wl["meas_ops"], meas_ctx=wl["meas_ctx"],
+                                 prop_ctx=wl["prop_ctx"], fields=fields, energy_out=wl["e"])
+        if pinned_e is not None:
+            pinned_e.copy_(wl["e"], non_blocking=True)
+        if (k + 1) % wl["qr_every"] == 0:
+            st = block_tail(wl, st)
+    wl["state"] = st
+
+
+def block_tail(wl, st):
+    """QR, overlaps, block energy + EMA, SR (trot/prop/blocks.py:230-281)."""
+    import torch
+
+    tg = wl["tg"]
+    from trot_gb300 import _lib, native, rng
+
+    walkers = tg.walkers.orthonormalize_(st.walkers, wl["sys"].walker_kind)
+    ov = wl["meas_ops"].overlap(walkers, wl["trial"])
+    e = wl["meas_ops"].kernels["energy"](walkers, wl["ham"], wl["meas_ctx"], wl["trial"])
+    obs = wl.setdefault("obs", torch.empty(2, dtype=torch.float64, device="cuda"))
+    _lib.call("trot_block_energy", wl["W"], e.data_ptr(), st.weights.data_ptr(), st.scalars.data_ptr(),
+              float(wl["params"].dt), float(wl["params"].shift_ema), obs.data_ptr(), native.stream_ptr())
+    zeta = rng.uniform(st.rng_key, 1)
+    w_sr, weights_sr = tg.walkers.stochastic_reconfiguration(walkers, st.weights, zeta, wl["sys"].walker_kind)
+    ov_sr = wl["meas_ops"].overlap(w_sr, wl["trial"])
+    return st._replace(walkers=w_sr, weights=weights_sr, overlaps=ov_sr)
+
+
+def flush_l2(buf):
+    buf.add_(1.0)
+
+
+def cpu_port_rate(cfg, W_sample, steps, threads=None):
+    """Oracle (numpy complex128) walker-steps/s on a bounded sample of the workload."""
+    from oracle import afqmc_oracle as orc
+    from trot_gb300 import synthetic
+
+    N, (na, nb), G = cfg["norb"], cfg["nelec"], cfg["nchol"]
+    ss = synthetic.make_system(N, (na, nb), G, decay=cfg["decay"], seed=0, h0=0.0)
+    kind = cfg["kind"]
+    prop = orc.build_prop_ctx(ss.h0, ss.h1, ss.chol, ss.rdm1(), cfg["dt"])
+    if kind == "uhf_u":
+        m = orc.Model(kind, ss.h0, (ss.mo_a, ss.mo_b), orc.build_uhf_meas_ctx(ss.h1, ss.chol, ss.mo_a, ss.mo_b), prop)
+        w = (synthetic.perturbed_walkers(ss.mo_a, W_sample, 0.0), synthetic.perturbed_walkers(ss.mo_b, W_sample, 0.0))
+    else:
+        m = orc.Model(kind, ss.h0, ss.mo_a, orc.build_rhf_meas_ctx(ss.h1, ss.chol, ss.mo_a), prop)
+        w = synthetic.perturbed_walkers(ss.mo_a, W_sample, 0.0)
+    fields = synthetic.fields(W_sample, G, steps + 1, seed=9)
+    params = orc.Params(dt=cfg["dt"])
+    st = orc.State(w, np.ones(W_sample), m.overlap(w), 0.0, 0.0, 0)
+    m.energy(w)  # warm-up
+    st = orc.afqmc_step(st, m, params, fields[0])
+    t0 = time.perf_counter()
+    for k in range(steps):
+        m.energy(st.walkers)
+        st = orc.afqmc_step(st, m, params, fields[k + 1])
+    dt = time.perf_counter() - t0
+    return W_sample * steps / dt, dt
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["mixed", "fp64"])
+    ap.add_argument("--config", default="cfg2_uhf_n120")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="walkers in the CPU baseline sample (0 = auto)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    from trot_gb300 import synthetic
+
+    cfg = dict(synthetic.CONFIGS[args.config])
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    N, (na, nb), G, W = cfg["norb"], cfg["nelec"], cfg["nchol"], cfg["n_walkers"]
+    fl = flops_per_walker_step(N, na, nb, G)
+    config = {"workload": f"{cfg['kind']} N={N} nelec=({na},{nb}) G={G} W={W} dt={cfg['dt']} "
+                          f"qr/sr every {cfg['qr_every']}", "walkers": W, "norb": N, "nelec": [na, nb],
+              "nchol": G, "trial": cfg["kind"], "seed": 0}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cores = cpu_cores()
+        sample = args.cpu_sample or 16
+        rates = []
+        for _ in range(max(1, args.steps // 10)):
+            r, _ = cpu_port_rate(cfg, sample, 2)
+            rates.append(r)
+        v = statistics.median(rates)
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+                "warmup": args.warmup, "higher_is_better": True, "dtype": "c128", "data": "synthetic",
+                "config": config, "vs_baseline": None,
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                 "sample": f"{sample} walkers x 2 steps (prop + E_L), numpy complex128 oracle, "
+                                           f"{len(rates)} repeats, median"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from trot_gb300 import _lib
+
+    wl = build_workload(cfg, args.precision)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    # warm-up
+    run_steps(wl, args.warmup)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # timed region: K steps, device-timed with CUDA events on torch's stream
+    _lib.profile_enable(64 * (args.steps + 8))
+    flush_l2(flush)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        run_steps(wl, args.steps, k0=args.warmup)
+        ev1.record()
+        torch.cuda.synchronize()
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    prof = _lib.profile_collect()
+    _lib.profile_enable(0)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = W * args.steps * world / (ms / 1e3)
+
+    # end to end through the public API: host fields in, energies out, every step
+    k_e2e = max(4, args.steps // 2)
+    fields_host = torch.from_numpy(synthetic.fields(W, G, 4, seed=77)).pin_memory()
+    pinned_e = torch.empty(W, dtype=torch.complex128).pin_memory()
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run_steps(wl, k_e2e, k0=args.warmup + args.steps, fields_host=fields_host, pinned_e=pinned_e)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": W * k_e2e * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": W * G * 8,
+           "d2h_bytes_per_step": W * 16, "steps": k_e2e}
+    if rank != 0:
+        return
+
+    peaks, peak_src = load_peaks()
+    launches = sum(c for _, c in prof.values())
+    # roofline of the dominant kernel
+    top = max(prof.items(), key=lambda kv: kv[1][0]) if prof else ("none", (0.0, 1))
+    tname, (tms, tcnt) = top
+    fl_map = {"vhs": fl["vhs"], "exchange": fl["exchange"], "trotter": fl["taylor"] + fl["onebody"] + fl["overlap"],
+              "force_bias": fl["force_bias"], "green": fl["green"]}
+    kfl = next((v for k, v in fl_map.items() if tname.startswith(k)), sum(fl.values()))
+    per_launch_s = tms / max(tcnt, 1) / 1e3
+    achieved_tflops = kfl * W / per_launch_s / 1e12 if per_launch_s > 0 else 0.0
+    peak = peaks["bf16_tflops"]
+    roofline = {"bound": "tensor", "kernel": tname, "achieved": achieved_tflops, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved_tflops / peak, "peak_source": f"{peak_src} bf16 dense (MEASURED_PEAKS.json)",
+                "traffic": None, "algorithmic_flops_per_launch": kfl * W,
+                "note": "fp64 kernels run on the FP64 pipe; the bf16 tensor peak is the denominator the contract names"}
+    step_flops = sum(fl.values()) * W
+    kernels = {k: {"ms_total": round(v[0], 4), "launches": v[1], "ms_per_launch": round(v[0] / max(v[1], 1), 5)}
+               for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "mixed(bf16/fp32 tc, f64)",
+            "precision": args.precision, "data": "synthetic (seeded recipe)",
+            "config": dict(config, l2="per-step working set > L2 (129 MB); L2 flushed before the timed region",
+                           parallelism="replicas" if world > 1 else "1 GPU"),
+            "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+            "step_tflops": step_flops / (ms / args.steps / 1e3) / 1e12, "kernels": kernels}
+    if not args.no_cpu_baseline:
+        sample = args.cpu_sample or 16
+        r, secs = cpu_port_rate(cfg, sample, 2)
+        line["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
+                                "sample": f"{sample} walkers x 2 steps (prop + E_L) of the same workload, numpy "
+                                          f"complex128 oracle, {secs:.1f} s"}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,204 @@
+/*
+ * trot_gb300 — C ABI of the GB300 (sm_103a) phaseless-AFQMC hot path.
+ *
+ * Every entry point takes caller-owned device buffers (plain pointers),
+ * sizes, and a cudaStream_t passed as void*.  Nothing here allocates device
+ * memory: scratch comes from a caller-provided workspace whose size is given
+ * by trot_workspace_size().  Calls launch asynchronously on the given stream
+ * and never synchronise with the host, so they can be issued inside a CUDA
+ * graph capture.  Errors come back as a trot_status code; the message of the
+ * last error on the calling thread is in trot_last_error().
+ *
+ * Array conventions (all row-major, C order, as numpy/jax/torch lay them out):
+ *   complex128 arrays are interleaved (re, im) doubles;
+ *   walkers            (W, N, n)   complex128   W walkers, N orbitals, n columns
+ *   trial coefficients (N, n)      float64
+ *   Cholesky vectors   (G, N, N)   float64      (chol_flat = (G, N*N))
+ *   rot_chol           (G, n, N)   float64      half-rotated C^T L_g
+ *   rot_h1             (n, N)      float64      C^T h1
+ *
+ * Walker/trial kinds (the reference's make_*_meas_ops(sys) dispatch):
+ *   TROT_RHF_R  RHF trial, restricted walkers     trot/meas/rhf.py:119-138
+ *   TROT_RHF_U  RHF trial, unrestricted walkers   trot/meas/rhf.py:141-172
+ *   TROT_UHF_U  UHF trial, unrestricted walkers   trot/meas/uhf.py:43-57,205-231
+ */
+#ifndef TROT_GB300_H
+#define TROT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TROT_ABI_VERSION 1
+
+typedef enum {
+  TROT_OK = 0,
+  TROT_ERR_BAD_SHAPE = 1,
+  TROT_ERR_BAD_DTYPE = 2,
+  TROT_ERR_NULL_PTR = 3,
+  TROT_ERR_WORKSPACE_TOO_SMALL = 4,
+  TROT_ERR_CUDA = 5,
+  TROT_ERR_DEVICE_TIMEOUT = 6,
+  TROT_ERR_NUMERIC_GUARD = 7,
+  TROT_ERR_UNSUPPORTED = 8
+} trot_status;
+
+typedef enum { TROT_RHF_R = 0, TROT_RHF_U = 1, TROT_UHF_U = 2 } trot_kind;
+
+/* Arithmetic of the dense contractions.  TROT_FP64 computes everything in
+ * float64.  TROT_MIXED runs the force-bias / VHS / Taylor / exchange
+ * contractions on tensor cores and keeps LU, log-det, QR, weights and energy
+ * accumulation in float64. */
+typedef enum { TROT_FP64 = 0, TROT_MIXED = 1 } trot_precision;
+
+typedef enum {
+  TROT_OP_FORCE_BIAS = 0,
+  TROT_OP_LOCAL_ENERGY = 1,
+  TROT_OP_APPLY_TROTTER = 2,
+  TROT_OP_PROP_STEP = 3,
+  TROT_OP_QR = 4,
+  TROT_OP_SR = 5
+} trot_op;
+
+/* Static description of one Hamiltonian + trial + propagation context.
+ * Mirrors HamChol (trot/ham/chol.py:14-58), RhfMeasCtx / UhfMeasCtx
+ * (trot/meas/rhf.py:282-319, trot/meas/uhf.py:277-336), CholAfqmcCtx
+ * (trot/prop/chol_afqmc_ops.py:16-50) and the QmcParams fields the step reads
+ * (trot/prop/types.py:30-47).  All pointers are device pointers.  For TROT_RHF_*
+ * the *_b trial/rot pointers may be NULL (the alpha ones are used for both
+ * spins). */
+typedef struct {
+  int kind;          /* trot_kind */
+  int precision;     /* trot_precision */
+  int n_walkers;     /* W */
+  int norb;          /* N */
+  int nchol;         /* G */
+  int nocc_a;        /* columns of alpha (or restricted) walkers */
+  int nocc_b;        /* columns of beta walkers (ignored for TROT_RHF_R) */
+  int n_exp_terms;   /* Taylor terms, reference default 6 */
+  double h0;
+  double h0_prop;    /* -h0 - 1/2 sum_g mf_g^2 (real) */
+  double dt;
+  double sqrt_dt;
+  double weight_floor;         /* 1e-3 */
+  double weight_cap;           /* 100 */
+  double pop_control_damping;  /* 0.1 */
+  const double* mo_a;          /* (N, na) */
+  const double* mo_b;          /* (N, nb) */
+  const double* rot_h1_a;      /* (na, N) */
+  const double* rot_h1_b;      /* (nb, N) */
+  const double* rot_chol_a;    /* (G, na, N) */
+  const double* rot_chol_b;    /* (G, nb, N) */
+  const double* exp_h1_half;   /* (N, N) */
+  const double* chol_flat;     /* (G, N*N) */
+  const double* mf_shifts_im;  /* (G) imaginary parts of mf_shifts (real parts are 0) */
+  const void* mixed;           /* device context from trot_mixed_prepare, or NULL */
+} trot_system;
+
+/* Walker population.  Walkers are updated in place by the step. */
+typedef struct {
+  double* walkers_a;           /* complex128 (W, N, na) */
+  double* walkers_b;           /* complex128 (W, N, nb); NULL for TROT_RHF_R */
+  double* weights;             /* float64 (W) */
+  double* overlaps;            /* complex128 (W) */
+  double* scalars;             /* float64 [pop_control_ene_shift, e_estimate] */
+  int64_t* node_encounters;    /* int64 [1] */
+} trot_state;
+
+const char* trot_last_error(void);
+int trot_abi_version(void);
+
+/* Bytes of workspace the given op needs for this system. */
+size_t trot_workspace_size(const trot_system* sys, int op);
+
+/* Trial overlaps of all walkers (complex128 out (W)).
+ * Replaces overlap_r / overlap_u: trot/trial/rhf.py:45-54, trot/trial/uhf.py:48-58. */
+int trot_overlap(const trot_system* sys, const double* walkers_a, const double* walkers_b,
+                 double* overlaps_out, void* stream);
+
+/* Force bias of all walkers (complex128 out (W, G)).
+ * Replaces force_bias_kernel_rw_rh / _uw_rh: trot/meas/rhf.py:119-125,141-153;
+ * trot/meas/uhf.py:43-57. */
+int trot_force_bias(const trot_system* sys, const double* walkers_a, const double* walkers_b,
+                    double* force_bias_out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Local energy of all walkers (complex128 out (W)).
+ * Replaces energy_kernel_rw_rh / _uw_rh: trot/meas/rhf.py:128-138,156-172;
+ * trot/meas/uhf.py:205-231. */
+int trot_local_energy(const trot_system* sys, const double* walkers_a, const double* walkers_b,
+                      double* energy_out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* exp(-dt/2 h1) exp(sqrt(dt) i VHS(x)) exp(-dt/2 h1) applied to every walker,
+ * with complex128 shifted fields x (W, G); the Taylor series has
+ * sys->n_exp_terms terms.  In-place allowed (out == in).
+ * Replaces apply_trotter (trot/prop/chol_afqmc_ops.py:198-222,
+ * trot/prop/utils.py:20-30). */
+int trot_apply_trotter(const trot_system* sys, const double* walkers_a, const double* walkers_b,
+                       const double* shifted_fields, double* out_a, double* out_b,
+                       void* workspace, size_t workspace_bytes, void* stream);
+
+/* One phaseless step with injected float64 fields (W, G): force bias, field
+ * shifts, Trotter propagation, overlaps, importance weights, population
+ * control shift.  Updates *state in place.  If energy_out is not NULL it also
+ * writes the local energy of the walkers at the START of the step
+ * (complex128 (W)), reusing the step's Green's functions.
+ * Replaces afqmc_step (trot/prop/afqmc.py:79-144). */
+int trot_prop_step(const trot_system* sys, const trot_state* state, const double* fields,
+                   double* energy_out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Reduced QR of every walker with diag(R) real non-negative; Q replaces the
+ * walkers in place; norm_out (complex128 (W), may be NULL) receives
+ * det(R)^2 (restricted) or det(R_a) det(R_b).
+ * Replaces orthogonalize / orthonormalize (trot/walkers.py:137-179). */
+int trot_orthonormalize(const trot_system* sys, double* walkers_a, double* walkers_b,
+                        double* norm_out, void* stream);
+
+/* Stochastic reconfiguration (comb resampling) with zeta in [0, 1) read from
+ * the device (zeta_dev, float64 [1]) or, when zeta_dev is NULL, the value zeta:
+ * idx_out (int64 (W)) = searchsorted(cumsum|w|, tot (k + zeta) / W, 'left');
+ * walkers_out[k] = walkers_in[idx_out[k]]; weights_out[:] = tot / W.
+ * Input and output walker buffers must not overlap.
+ * Replaces stochastic_reconfiguration / _sr_indices (trot/walkers.py:249-293). */
+int trot_sr_resample(const trot_system* sys, const double* weights_in, const double* zeta_dev, double zeta,
+                     const double* walkers_a_in, const double* walkers_b_in,
+                     double* walkers_a_out, double* walkers_b_out, double* weights_out,
+                     int64_t* idx_out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Block energy on the device (trot/prop/blocks.py:236-257): clamps Re(E_L)
+ * to e_estimate when non-finite or further than sqrt(2/dt) from it, zeroes the
+ * weights of non-finite walkers (in place), forms the weighted block energy
+ * and updates e_estimate (scalars[1]) with the shift_ema moving average.
+ * obs_out (float64 [2], device) receives [e_block, sum of weights]. */
+int trot_block_energy(int n_walkers, const double* energy, double* weights, double* scalars, double dt,
+                      double shift_ema, double* obs_out, void* stream);
+
+/* Auxiliary fields N(0, 1), float64 (W, G), drawn on the device from the
+ * sub-key of `key` (int64 [2] device array holding two uint32 words,
+ * Philox-4x32-10).  Replaces jax.random.normal in afqmc_step
+ * (trot/prop/afqmc.py:91-93); call trot_split_key afterwards to advance. */
+int trot_sample_normal_fields(const int64_t* key, int n_walkers, int nchol, double* fields, void* stream);
+
+/* n uniforms in [0, 1) from the sub-key of `key` (the SR zeta,
+ * trot/prop/blocks.py:270-271). */
+int trot_sample_uniform(const int64_t* key, int n, double* out, void* stream);
+
+/* key <- split(key)[0] in place on the device (jax.random.split pattern). */
+int trot_split_key(int64_t* key, void* stream);
+
+/* Per-kernel timers for measurement: trot_profile_enable(n) creates a pool
+ * for n launches (0 disables); while enabled every kernel launch of the C ABI
+ * is bracketed by CUDA events on its stream.  trot_profile_collect
+ * synchronises, writes up to max_names kernel names (48-byte slots), total
+ * milliseconds and launch counts, clears the records and returns the number
+ * of names.  Keep disabled during CUDA graph capture.  No counterpart in the
+ * reference (it has no profiling hooks). */
+int trot_profile_enable(int max_launches);
+int trot_profile_collect(int max_names, char* names, double* total_ms, int* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TROT_GB300_H */

@@ -1,0 +1,98 @@
+"""C ABI checks that need no GPU: the library builds and loads, exports every
+entry point include/trot_gb300.h declares, and rejects bad arguments with a
+status code before launching anything."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from trot_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    txt = open(os.path.join(ROOT, "include", "trot_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(trot_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_header_symbols_exported():
+    lib = _lib.load()
+    decl = _declared()
+    assert len(decl) >= 14
+    for name in decl:
+        assert hasattr(lib, name), name
+    assert set(decl) == set(_lib.exported_symbols())
+
+
+def test_abi_version():
+    assert _lib.load().trot_abi_version() == 1
+
+
+def _sys(**kw):
+    s = _lib.TrotSystem()
+    s.kind, s.precision, s.n_walkers, s.norb, s.nchol, s.nocc_a, s.nocc_b = 0, 0, 4, 8, 5, 2, 2
+    s.n_exp_terms = 6
+    s.mo_a = s.mo_b = 0x1000
+    s.rot_h1_a = s.rot_chol_a = s.exp_h1_half = s.chol_flat = s.mf_shifts_im = 0x1000
+    for k, v in kw.items():
+        setattr(s, k, v)
+    return s
+
+
+def _status(fn, *args):
+    return getattr(_lib.load(), fn)(*args)
+
+
+def test_error_null_pointers():
+    s = _sys()
+    assert _status("trot_overlap", ctypes.byref(s), None, None, 0x1000, None) == 3
+    assert _status("trot_overlap", ctypes.byref(s), 0x1000, None, None, None) == 3
+    assert b"null" in _lib.load().trot_last_error()
+    assert _status("trot_overlap", None, 0x1000, None, 0x1000, None) == 3
+    s2 = _sys(kind=2)
+    s2.mo_b = 0
+    assert _status("trot_overlap", ctypes.byref(s2), 0x1000, 0x1000, 0x1000, None) == 3
+
+
+def test_error_bad_shapes():
+    for kw in (dict(n_walkers=0), dict(norb=0), dict(nocc_a=9), dict(kind=7), dict(kind=1, nocc_b=3)):
+        s = _sys(**kw)
+        assert _status("trot_overlap", ctypes.byref(s), 0x1000, 0x1000, 0x1000, None) == 1, kw
+    s = _sys(precision=5)
+    assert _status("trot_overlap", ctypes.byref(s), 0x1000, 0x1000, 0x1000, None) == 2
+
+
+def test_error_workspace_too_small():
+    s = _sys()
+    need = _lib.load().trot_workspace_size(ctypes.byref(s), _lib.OP_FORCE_BIAS)
+    assert need > 0
+    assert _status("trot_force_bias", ctypes.byref(s), 0x1000, None, 0x1000, 0x1000, need // 2, None) == 4
+    assert _status("trot_local_energy", ctypes.byref(s), 0x1000, None, 0x1000, None, 0, None) == 4
+    st = _lib.TrotState()
+    st.walkers_a = st.weights = st.overlaps = st.scalars = st.node_encounters = 0x1000
+    assert _status("trot_prop_step", ctypes.byref(s), ctypes.byref(st), 0x1000, None, 0x1000, 16, None) == 4
+
+
+def test_error_sr_arguments():
+    s = _sys()
+    assert _status("trot_sr_resample", ctypes.byref(s), 0x1000, None, 1.5, 0x1000, None, 0x2000, None,
+                   0x1000, 0x1000, 0x1000, 1 << 20, None) == 1
+    assert _status("trot_sr_resample", ctypes.byref(s), 0x1000, None, 0.5, 0x1000, None, 0x1000, None,
+                   0x1000, 0x1000, 0x1000, 1 << 20, None) == 1
+
+
+def test_mixed_requires_context():
+    s = _sys(precision=1)
+    st = _lib.TrotState()
+    st.walkers_a = st.weights = st.overlaps = st.scalars = st.node_encounters = 0x1000
+    assert _status("trot_prop_step", ctypes.byref(s), ctypes.byref(st), 0x1000, None, 0x1000, 1 << 30, None) == 3
+
+
+def test_workspace_size_monotone():
+    small = _lib.load().trot_workspace_size(ctypes.byref(_sys(n_walkers=4)), _lib.OP_PROP_STEP)
+    big = _lib.load().trot_workspace_size(ctypes.byref(_sys(n_walkers=400)), _lib.OP_PROP_STEP)
+    assert big > small > 0
+    assert _lib.load().trot_workspace_size(ctypes.byref(_sys(n_walkers=0)), _lib.OP_PROP_STEP) == 0

@@ -1,0 +1,100 @@
+// FP64 complex x real GEMM on the CUDA cores.
+//
+//   C[m][n] (+)= alpha * sum_k A[m][k] * B(k, n)
+//
+// A complex row-major (lda), B real either (N, K) row-major ("nk", the force
+// bias: rot_chol_flat is (G, n*N)) or (K, N) row-major ("kn", the VHS build:
+// chol_flat is (G, N*N)).  Used by the FP64 force bias
+// (trot/meas/rhf.py:125) and the FP64 VHS build
+// (trot/prop/chol_afqmc_ops.py:83-87: Re(x) @ chol_flat + i Im(x) @ chol_flat).
+// GB300's FP64 rate is ~2 FMA/clk/SM, so this kernel is FP64-pipe bound with
+// any reasonable register tiling: 64x64 tiles, 4x4 complex outputs per thread.
+#include "kernels.h"
+
+namespace trot {
+
+static constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
+
+template <bool B_NK>
+__global__ void __launch_bounds__(NT)
+zgemm_cr_kernel(int M, int Nn, int K, double alpha, const double2* __restrict__ A, int lda,
+                const double* __restrict__ B, int ldb, double2* __restrict__ C, int ldc, int accumulate) {
+  __shared__ double2 As[BK][BM + 1];
+  __shared__ double Bs[BK][BN + 1];
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  double2 acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = cmk(0.0, 0.0);
+
+  for (int k0 = 0; k0 < K; k0 += BK) {
+    // A tile: BM x BK complex, 4 per thread
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      int e = tid + r * NT;
+      int mm = e / BK, kk = e % BK;
+      int gm = m0 + mm, gk = k0 + kk;
+      As[kk][mm] = (gm < M && gk < K) ? A[(size_t)gm * lda + gk] : cmk(0.0, 0.0);
+    }
+    // B tile: BK x BN real, 4 per thread
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      int e = tid + r * NT;
+      int kk, nn;
+      if (B_NK) { nn = e / BK; kk = e % BK; } else { kk = e / BN; nn = e % BN; }
+      int gn = n0 + nn, gk = k0 + kk;
+      double v = 0.0;
+      if (gn < Nn && gk < K) v = B_NK ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
+      Bs[kk][nn] = v;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < BK; ++kk) {
+      double2 a[4];
+      double bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) crfma(acc[i][j], bv[j], a[i]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int gm = m0 + ty + 16 * i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int gn = n0 + tx + 16 * j;
+      if (gn >= Nn) continue;
+      double2 v = cscale(acc[i][j], alpha);
+      double2* c = C + (size_t)gm * ldc + gn;
+      *c = accumulate ? cadd(*c, v) : v;
+    }
+  }
+}
+
+int launch_zgemm_cr(int M, int Nn, int K, double alpha, const double2* A, int lda, const double* B,
+                    int ldb, bool b_is_nk, double2* C, int ldc, bool accumulate, cudaStream_t st) {
+  if (M <= 0 || Nn <= 0) return TROT_OK;
+  dim3 grid((Nn + BN - 1) / BN, (M + BM - 1) / BM);
+  if (grid.y > 65535) {
+    set_error("zgemm_cr: M=%d too large", M);
+    return TROT_ERR_UNSUPPORTED;
+  }
+  if (b_is_nk)
+    zgemm_cr_kernel<true><<<grid, NT, 0, st>>>(M, Nn, K, alpha, A, lda, B, ldb, C, ldc, accumulate);
+  else
+    zgemm_cr_kernel<false><<<grid, NT, 0, st>>>(M, Nn, K, alpha, A, lda, B, ldb, C, ldc, accumulate);
+  TROT_CHECK_LAUNCH("zgemm_cr_kernel");
+  return TROT_OK;
+}
+
+}  // namespace trot

@@ -1,0 +1,78 @@
+// Host-side launchers shared between the kernel translation units and the C ABI.
+#pragma once
+#include "common.cuh"
+
+namespace trot {
+
+// Bump allocator over the caller's workspace (256-byte aligned slices).
+struct Carver {
+  char* base;
+  size_t size, used = 0;
+  bool ok = true;
+  Carver(void* b, size_t s) : base(static_cast<char*>(b)), size(s) {}
+  template <class T>
+  T* take(size_t count) {
+    size_t off = (used + 255) & ~size_t(255);
+    used = off + count * sizeof(T);
+    if (base == nullptr || used > size) { ok = false; return nullptr; }
+    return reinterpret_cast<T*>(base + off);
+  }
+};
+
+struct StepBuffers {
+  double2 *green, *e1, *fb, *xs, *shift_term, *fb_term, *vhs, *exc;
+  int* node_flag;
+};
+
+Spins make_spins(const trot_system* s);
+
+// Green's function / overlap per walker (green.cu).
+// green: complex (W, ntot*N) half Green's functions, spin blocks concatenated
+// (may be null); det_out: complex (W) overlap = prod_s det(C_s^T w_s)^mult_s (may be null);
+// e1_out: complex (W) sum_s mult_s sum(G_s o rot_h1_s) (may be null).
+int launch_green(const Spins& sp, int W, int N, const double2* wa, const double2* wb,
+                 double2* green, double2* ovlp_out, double2* e1_out, cudaStream_t st);
+
+// C[m][n] (+)= alpha * sum_k A[m][k] * B(k, n), A complex (lda), C complex (ldc).
+// b_is_nk: B stored (N, K) row-major (ldb) — otherwise (K, N) row-major.
+int launch_zgemm_cr(int M, int Nn, int K, double alpha, const double2* A, int lda,
+                    const double* B, int ldb, bool b_is_nk, double2* C, int ldc, bool accumulate,
+                    cudaStream_t st);
+
+// step64.cu
+int launch_fields(int W, int G, double sqrt_dt, const double2* fb, const double* mf_im,
+                  const double* x, double2* xs, double2* shift_term, double2* fb_term, cudaStream_t st);
+
+struct TrotterArgs {
+  int W, N, G, nterms;
+  double sqrt_dt;
+  const double* expH;  // (N, N)
+  const double2* vhs;  // (W, N, N)
+  const double2* in_a; const double2* in_b;
+  double2* out_a; double2* out_b;
+  // step mode (all null otherwise)
+  double2* overlaps;       // in: old, out: new
+  double* weights;         // in/out
+  const double* scalars;   // [E_shift, e_est]
+  const double2* shift_term; const double2* fb_term;
+  int* node_flag;
+  double dt, h0_prop, w_floor, w_cap;
+};
+int launch_trotter(const Spins& sp, const TrotterArgs& a, cudaStream_t st);
+int launch_step_finalize(int W, double* weights, double* scalars, long long* nodes,
+                         const int* node_flag, double damping, double dt, cudaStream_t st);
+
+int exchange_chunks(int G);
+int launch_exchange(const Spins& sp, int W, int N, int G, const double2* green, double2* partial,
+                    cudaStream_t st);
+int launch_energy_combine(int W, int G, int nchunks, double h0, const double2* fb, const double2* e1,
+                          const double2* partial, double2* energy, cudaStream_t st);
+
+// walkers.cu
+int launch_qr(const Spins& sp, int W, int N, double2* wa, double2* wb, double2* norm_out, cudaStream_t st);
+int launch_sr(const Spins& sp, int W, int N, const double* weights, const double* zeta_dev, double zeta,
+              const double2* ina,
+              const double2* inb, double2* outa, double2* outb, double* weights_out, long long* idx,
+              double* cw, cudaStream_t st);
+
+}  // namespace trot
