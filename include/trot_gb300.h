@@ -188,6 +188,20 @@ int trot_sample_uniform(const int64_t* key, int n, double* out, void* stream);
 /* key <- split(key)[0] in place on the device (jax.random.split pattern). */
 int trot_split_key(int64_t* key, void* stream);
 
+/* Local energy with no caller workspace and no allocation: same inputs,
+ * output and numbers as trot_local_energy, with the scratch taken from a
+ * fixed 32 MiB device array built into the library (held on every GPU that
+ * loads it, until the process exits).  For callers that cannot allocate
+ * device memory, e.g. a JAX custom call inside a process whose GPU memory
+ * XLA has pre-allocated.  Systems needing more scratch than 32 MiB
+ * (trot_workspace_size(sys, TROT_OP_LOCAL_ENERGY)) are rejected with
+ * TROT_ERR_WORKSPACE_TOO_SMALL.  The first call on a device resolves the
+ * array's address (cudaGetSymbolAddress) and should come before any stream
+ * capture; all calls share the array, so calls that overlap on the GPU race.
+ * No counterpart in the reference. */
+int trot_local_energy_noalloc(const trot_system* sys, const double* walkers_a, const double* walkers_b,
+                              double* energy_out, void* stream);
+
 /* Per-kernel timers for measurement: trot_profile_enable(n) creates a pool
  * for n launches (0 disables); while enabled every kernel launch of the C ABI
  * is bracketed by CUDA events on its stream.  trot_profile_collect
