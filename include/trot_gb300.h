@@ -202,6 +202,16 @@ int trot_split_key(int64_t* key, void* stream);
 int trot_local_energy_noalloc(const trot_system* sys, const double* walkers_a, const double* walkers_b,
                               double* energy_out, void* stream);
 
+/* Plain BF16 tensor-core GEMM (tcgen05, accumulator in tensor memory):
+ * D (M x N, float32) = A (M x K, bf16) * B (N x K, bf16)^T, all row-major,
+ * M and N multiples of 128, K a multiple of 64, A and B 16-byte aligned.
+ * *status (device int) is set to TROT_ERR_DEVICE_TIMEOUT if a completion
+ * wait ran out (the kernel then frees its tensor memory and returns).  The
+ * building block of the mixed-precision kernels; no counterpart in the
+ * reference (it has no hand-written GEMM). */
+int trot_tc_gemm_bf16(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, int* status,
+                      void* stream);
+
 /* Per-kernel timers for measurement: trot_profile_enable(n) creates a pool
  * for n launches (0 disables); while enabled every kernel launch of the C ABI
  * is bracketed by CUDA events on its stream.  trot_profile_collect

@@ -76,6 +76,7 @@ _SIGNATURES = {
     "trot_sample_uniform": (_i, [_p, _i, _p, _p]),
     "trot_split_key": (_i, [_p, _p]),
     "trot_local_energy_noalloc": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p]),
+    "trot_tc_gemm_bf16": (_i, [_p, _p, _p, _i, _i, _i, _p, _p]),
     "trot_profile_enable": (_i, [_i]),
     "trot_profile_collect": (_i, [_i, ctypes.c_char_p, _p, _p]),
 }
