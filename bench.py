@@ -126,12 +126,14 @@ def build_workload(cfg, precision):
     sysm = tg.System(norb=N, nelec=(na, nb), walker_kind=wk)
     ham = tg.HamChol(h0=ss.h0, h1=ss.h1, chol=ss.chol)
     params = tg.QmcParams(dt=cfg["dt"], n_walkers=W, n_prop_steps=cfg["qr_every"], seed=1234)
+    mixed = precision == "mixed"
     if kind == "uhf_u":
         trial = tg.UhfTrial(ss.mo_a, ss.mo_b)
-        trial_ops, meas_ops = tg.make_uhf_trial_ops(sysm), tg.make_uhf_meas_ops(sysm)
+        trial_ops, meas_ops = tg.make_uhf_trial_ops(sysm), tg.make_uhf_meas_ops(sysm, mixed_precision=mixed)
     else:
         trial = tg.RhfTrial(ss.mo_a)
-        trial_ops, meas_ops = tg.make_rhf_trial_ops(sysm), tg.make_rhf_meas_ops(sysm)
+        trial_ops = tg.make_rhf_trial_ops(sysm)
+        meas_ops = tg.make_rhf_meas_ops(sysm, mixed_precision=mixed)
     meas_ctx = meas_ops.build_meas_ctx(ham, trial)
     prop_ops = tg.make_prop_ops("restricted", wk, mixed_precision=(precision == "mixed"))
     prop_ctx = prop_ops.build_prop_ctx(ham, trial_ops.get_rdm1(trial), params)
@@ -173,7 +175,6 @@ def block_tail(wl, st):
     from trot_gb300 import _lib, native, rng
 
     walkers = tg.walkers.orthonormalize_(st.walkers, wl["sys"].walker_kind)
-    ov = wl["meas_ops"].overlap(walkers, wl["trial"])
     e = wl["meas_ops"].kernels["energy"](walkers, wl["ham"], wl["meas_ctx"], wl["trial"])
     obs = wl.setdefault("obs", torch.empty(2, dtype=torch.float64, device="cuda"))
     _lib.call("trot_block_energy", wl["W"], e.data_ptr(), st.weights.data_ptr(), st.scalars.data_ptr(),
@@ -188,8 +189,10 @@ def flush_l2(buf):
     buf.add_(1.0)
 
 
-def cpu_port_rate(cfg, W_sample, steps, threads=None):
-    """Oracle (numpy complex128) walker-steps/s on a bounded sample of the workload."""
+def cpu_port_rate(cfg, W_sample, steps, threads=None, min_seconds=0.0, max_steps=64):
+    """Oracle (numpy complex128) walker-steps/s on a bounded sample of the
+    workload: W_sample walkers, at least ``steps`` steps and at least
+    ``min_seconds`` of work (capped at ``max_steps``)."""
     from oracle import afqmc_oracle as orc
     from trot_gb300 import synthetic
 
@@ -203,17 +206,19 @@ def cpu_port_rate(cfg, W_sample, steps, threads=None):
     else:
         m = orc.Model(kind, ss.h0, ss.mo_a, orc.build_rhf_meas_ctx(ss.h1, ss.chol, ss.mo_a), prop)
         w = synthetic.perturbed_walkers(ss.mo_a, W_sample, 0.0)
-    fields = synthetic.fields(W_sample, G, steps + 1, seed=9)
+    fields = synthetic.fields(W_sample, G, 2, seed=9)
     params = orc.Params(dt=cfg["dt"])
     st = orc.State(w, np.ones(W_sample), m.overlap(w), 0.0, 0.0, 0)
     m.energy(w)  # warm-up
     st = orc.afqmc_step(st, m, params, fields[0])
     t0 = time.perf_counter()
-    for k in range(steps):
+    k = 0
+    while k < steps or (time.perf_counter() - t0 < min_seconds and k < max_steps):
         m.energy(st.walkers)
-        st = orc.afqmc_step(st, m, params, fields[k + 1])
+        st = orc.afqmc_step(st, m, params, fields[k % 2])
+        k += 1
     dt = time.perf_counter() - t0
-    return W_sample * steps / dt, dt
+    return W_sample * k / dt, dt, k
 
 
 def cpu_cores():
@@ -229,7 +234,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--fp64-steps", type=int, default=3, help="steps of the FP64 path timed for the comparison")
     ap.add_argument("--config", default="cfg2_uhf_n120")
     ap.add_argument("--cpu-sample", type=int, default=0, help="walkers in the CPU baseline sample (0 = auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -250,18 +256,21 @@ def main():
         if rank != 0:
             return
         cores = cpu_cores()
-        sample = args.cpu_sample or 16
-        rates = []
-        for _ in range(max(1, args.steps // 10)):
-            r, _ = cpu_port_rate(cfg, sample, 2)
+        sample = args.cpu_sample or 64
+        rates, secs, ks = [], 0.0, 0
+        for _ in range(max(1, min(3, args.steps // 10))):
+            r, sec, k = cpu_port_rate(cfg, sample, 2, min_seconds=10.0)
             rates.append(r)
+            secs += sec
+            ks += k
         v = statistics.median(rates)
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
                 "warmup": args.warmup, "higher_is_better": True, "dtype": "c128", "data": "synthetic",
                 "config": config, "vs_baseline": None,
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                                 "sample": f"{sample} walkers x 2 steps (prop + E_L), numpy complex128 oracle, "
-                                           f"{len(rates)} repeats, median"},
+                                 "sample": f"{sample} walkers x {ks} steps total (prop + E_L) in {len(rates)} "
+                                           f"timed runs of >= 10 s, numpy complex128 oracle port, median; "
+                                           f"{secs:.1f} s of CPU work"},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -325,6 +334,37 @@ def main():
         e2e_s = float(t.item())
     e2e = {"value": W * k_e2e * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": W * G * 8,
            "d2h_bytes_per_step": W * 16, "steps": k_e2e}
+    # precision: mixed vs FP64 local energy on the run's own (identical) walkers
+    precision_info = None
+    fp64 = None
+    if args.precision == "mixed":
+        import trot_gb300 as tg
+
+        st = wl["state"]
+        if wl["kind"] == "uhf_u":
+            m64 = tg.make_uhf_meas_ops(wl["sys"])
+        else:
+            m64 = tg.make_rhf_meas_ops(wl["sys"])
+        e64 = m64.kernels["energy"](st.walkers, wl["ham"], wl["meas_ctx"], wl["trial"])
+        emx = wl["meas_ops"].kernels["energy"](st.walkers, wl["ham"], wl["meas_ctx"], wl["trial"])
+        d = (emx - e64).abs()
+        precision_info = {"max_abs_dE_L_Ha": float(d.max()), "median_abs_dE_L_Ha": float(d.median()),
+                          "max_abs_E_L_Ha": float(e64.abs().max()), "walkers": W,
+                          "on": "the benchmark's walkers after warm-up + timed + e2e steps (identical walkers)"}
+        # FP64 path on the same workload, same device, a few steps
+        wl64 = build_workload(cfg, "fp64")
+        run_steps(wl64, 1)
+        torch.cuda.synchronize()
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record()
+        run_steps(wl64, args.fp64_steps, k0=1)
+        a1.record()
+        torch.cuda.synchronize()
+        ms64 = a0.elapsed_time(a1)
+        fp64 = {"value": W * args.fp64_steps / (ms64 / 1e3), "unit": UNIT, "steps": args.fp64_steps,
+                "ms_per_step": ms64 / args.fp64_steps}
+        del wl64
     if rank != 0:
         return
 
@@ -333,8 +373,9 @@ def main():
     # roofline of the dominant kernel
     top = max(prof.items(), key=lambda kv: kv[1][0]) if prof else ("none", (0.0, 1))
     tname, (tms, tcnt) = top
-    fl_map = {"vhs": fl["vhs"], "exchange": fl["exchange"], "trotter": fl["taylor"] + fl["onebody"] + fl["overlap"],
-              "force_bias": fl["force_bias"], "green": fl["green"]}
+    fl_map = {"vhs": fl["vhs"], "exchange_exact": fl["exchange"] + fl["force_bias"], "exchange": fl["exchange"],
+              "trotter": fl["taylor"] + fl["onebody"] + fl["overlap"], "force_bias": fl["force_bias"],
+              "green": fl["green"]}
     kfl = next((v for k, v in fl_map.items() if tname.startswith(k)), sum(fl.values()))
     per_launch_s = tms / max(tcnt, 1) / 1e3
     achieved_tflops = kfl * W / per_launch_s / 1e12 if per_launch_s > 0 else 0.0
@@ -354,12 +395,17 @@ def main():
                            parallelism="replicas" if world > 1 else "1 GPU"),
             "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "step_tflops": step_flops / (ms / args.steps / 1e3) / 1e12, "kernels": kernels}
+    if fp64 is not None:
+        line["fp64_path"] = fp64
+        line["speedup_vs_fp64"] = value / fp64["value"]
+    if precision_info is not None:
+        line["precision_check"] = precision_info
     if not args.no_cpu_baseline:
-        sample = args.cpu_sample or 16
-        r, secs = cpu_port_rate(cfg, sample, 2)
+        sample = args.cpu_sample or 64
+        r, secs, ks = cpu_port_rate(cfg, sample, 2, min_seconds=10.0)
         line["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
-                                "sample": f"{sample} walkers x 2 steps (prop + E_L) of the same workload, numpy "
-                                          f"complex128 oracle, {secs:.1f} s"}
+                                "sample": f"{sample} walkers x {ks} steps (prop + E_L) of the same workload, numpy "
+                                          f"complex128 oracle port (BLAS on all cores), {secs:.1f} s"}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

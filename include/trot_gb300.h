@@ -63,6 +63,34 @@ typedef enum {
   TROT_OP_SR = 5
 } trot_op;
 
+/* Operands of the mixed-precision path, prepared once per (trial,
+ * Hamiltonian, dt) by trot_gb300.mixed (host) and pointed to by
+ * trot_system.mixed (this struct lives in host memory; its pointers are
+ * device pointers).
+ *
+ * Local energy / force bias use an exact-slice BF16 product on tensor cores:
+ * every row x of rot_chol (rows (g, i) over orbitals p) and of the half
+ * Green's function is written as x = sum_t 2^(e - 8(t+1)) q_t with integer
+ * slices |q_t| <= 255 (exact in bf16) and one exponent e per row; slice
+ * products accumulate exactly in FP32 (K <= 256) and products with equal
+ * t + u share one accumulator.  The VHS uses a plain 3-term bf16 split
+ * (x = hi + mid + lo) with FP32 accumulation. */
+typedef struct {
+  int slices;            /* slices per operand of the exact product (5) */
+  int max_order;         /* products with t + u <= max_order (4) */
+  int kpad;              /* padded orbital dimension of the exact product (128) */
+  int gammas_per_block[2];   /* Cholesky vectors per 128-row tile, per spin */
+  int n_blocks[2];           /* tiles per spin: ceil(G / gammas_per_block) */
+  const uint16_t* rot_slices[2]; /* bf16 (slices, n_blocks, 128, kpad) per spin */
+  const int32_t* rot_exp[2];     /* int32 (n_blocks, 128) row exponents per spin */
+  int vhs_slices;        /* 3 */
+  int vhs_order;         /* products with t + u <= vhs_order (2) */
+  int n2pad;             /* N*N rounded up to 128 */
+  int gpad;              /* G rounded up to 64 */
+  const uint16_t* chol_t_slices; /* bf16 (vhs_slices, n2pad, gpad): row pq holds L[:, pq] */
+  const float* exp_h1_half_f32;  /* (N, N) */
+} trot_mixed;
+
 /* Static description of one Hamiltonian + trial + propagation context.
  * Mirrors HamChol (trot/ham/chol.py:14-58), RhfMeasCtx / UhfMeasCtx
  * (trot/meas/rhf.py:282-319, trot/meas/uhf.py:277-336), CholAfqmcCtx
@@ -95,7 +123,7 @@ typedef struct {
   const double* exp_h1_half;   /* (N, N) */
   const double* chol_flat;     /* (G, N*N) */
   const double* mf_shifts_im;  /* (G) imaginary parts of mf_shifts (real parts are 0) */
-  const void* mixed;           /* device context from trot_mixed_prepare, or NULL */
+  const trot_mixed* mixed;     /* host struct of mixed-precision operands, or NULL */
 } trot_system;
 
 /* Walker population.  Walkers are updated in place by the step. */
@@ -148,6 +176,12 @@ int trot_apply_trotter(const trot_system* sys, const double* walkers_a, const do
  * Replaces afqmc_step (trot/prop/afqmc.py:79-144). */
 int trot_prop_step(const trot_system* sys, const trot_state* state, const double* fields,
                    double* energy_out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Device status of the last mixed-precision op that used this workspace
+ * (its first bytes): TROT_OK, or TROT_ERR_DEVICE_TIMEOUT when a tensor-core
+ * kernel's completion wait ran out (the kernel then skipped its output, freed
+ * its tensor memory and returned).  Synchronous (cudaMemcpy). */
+int trot_workspace_status(const void* workspace, int* status_out);
 
 /* Reduced QR of every walker with diag(R) real non-negative; Q replaces the
  * walkers in place; norm_out (complex128 (W), may be NULL) receives

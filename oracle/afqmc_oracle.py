@@ -218,9 +218,9 @@ def _coul_exch(g, rot_chol):
     """f_g = rot_chol_g @ g^T per walker; returns (c (W,G), exchange (W,)).
 
     (trot/meas/rhf.py:41-60 "high" mode; trot/meas/uhf.py:220-225)."""
-    f = np.einsum("gij,bkj->bgik", rot_chol, g)
+    f = np.matmul(rot_chol[None], np.swapaxes(g, -1, -2)[:, None])  # (W, G, n, n), BLAS batched
     c = np.einsum("bgii->bg", f)
-    exc = np.einsum("bgij,bgji->b", f, f)
+    exc = np.sum(f * np.swapaxes(f, -1, -2), axis=(1, 2, 3))
     return c, exc
 
 

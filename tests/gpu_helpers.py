@@ -34,11 +34,11 @@ class Setup:
         if kind == "uhf_u":
             self.trial = tg.UhfTrial(mo_a, mo_b)
             self.trial_ops = tg.make_uhf_trial_ops(self.sys)
-            self.meas_ops = tg.make_uhf_meas_ops(self.sys)
+            self.meas_ops = tg.make_uhf_meas_ops(self.sys, mixed_precision=mixed)
         else:
             self.trial = tg.RhfTrial(mo_a)
             self.trial_ops = tg.make_rhf_trial_ops(self.sys)
-            self.meas_ops = tg.make_rhf_meas_ops(self.sys)
+            self.meas_ops = tg.make_rhf_meas_ops(self.sys, mixed_precision=mixed)
         self.meas_ctx = self.meas_ops.build_meas_ctx(self.ham, self.trial)
         self.prop_ops = tg.make_prop_ops("restricted", wk, mixed_precision=mixed)
         rdm1 = self.trial_ops.get_rdm1(self.trial)

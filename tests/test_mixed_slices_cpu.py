@@ -1,0 +1,46 @@
+"""Host-side operand preparation of the mixed-precision path (no GPU)."""
+import numpy as np
+import torch
+
+from trot_gb300 import mixed
+
+
+def test_exact_slices_reconstruct_rows():
+    rng = np.random.default_rng(0)
+    x = rng.normal(size=(7, 120)) * np.exp(rng.normal(size=(7, 1)) * 5)
+    x[3] = 0.0
+    x[4, :] = 2.0 ** 5  # exact power of two: the row max hits the slice range boundary
+    q, e = mixed.exact_slices(x)
+    assert q.shape == (mixed.SLICES, 7, 120)
+    assert np.all(np.abs(q) <= 255) and np.all(q == np.rint(q))
+    # every slice is exactly representable in bf16
+    qb = torch.from_numpy(q).to(torch.bfloat16).to(torch.float32).numpy()
+    np.testing.assert_array_equal(qb, q)
+    rec = sum(q[t].astype(np.float64) * np.ldexp(1.0, e - 8 * (t + 1))[:, None] for t in range(mixed.SLICES))
+    mx = np.max(np.abs(x), axis=1, keepdims=True)
+    err = np.abs(rec - x) / np.where(mx > 0, mx, 1.0)
+    assert np.max(err) <= 2.0 ** (-8 * mixed.SLICES)
+    assert np.all(rec[3] == 0.0)
+
+
+def test_plain_split_is_fp32_accurate():
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=(50, 64))
+    parts = mixed.plain_split(x)
+    rec = sum(p.to(torch.float64).numpy() for p in parts)
+    assert np.max(np.abs(rec - x) / np.abs(x)) < 2.0 ** -23
+
+
+def test_rot_tiles_layout():
+    rng = np.random.default_rng(2)
+    G, n, N = 25, 12, 120
+    rc = rng.normal(size=(G, n, N))
+    q, e, gb, nblk = mixed.rot_tiles(rc)
+    assert gb == 10 and nblk == 3
+    assert tuple(q.shape) == (mixed.SLICES, nblk, 128, mixed.KPAD)
+    qd = q.to(torch.float64).numpy()
+    # row (g=13, i=4) lives in block 1, row 3*12+4, orbitals 0..N-1; padding is zero
+    rec = sum(qd[t, 1, 3 * n + 4, :N] * np.ldexp(1.0, int(e[1, 3 * n + 4]) - 8 * (t + 1)) for t in range(mixed.SLICES))
+    np.testing.assert_allclose(rec, rc[13, 4], rtol=0, atol=2.0 ** -40 * np.max(np.abs(rc[13, 4])))
+    assert np.all(qd[:, :, :, N:] == 0)
+    assert np.all(qd[:, 2, 5 * n:, :] == 0)  # last block holds 5 vectors

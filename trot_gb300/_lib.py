@@ -29,6 +29,16 @@ _d = ctypes.c_double
 _i = ctypes.c_int
 
 
+class TrotMixed(ctypes.Structure):
+    """trot_mixed (include/trot_gb300.h)."""
+
+    _fields_ = [
+        ("slices", _i), ("max_order", _i), ("kpad", _i), ("gammas_per_block", _i * 2), ("n_blocks", _i * 2),
+        ("rot_slices", _p * 2), ("rot_exp", _p * 2), ("vhs_slices", _i), ("vhs_order", _i), ("n2pad", _i),
+        ("gpad", _i), ("chol_t_slices", _p), ("exp_h1_half_f32", _p),
+    ]
+
+
 class TrotSystem(ctypes.Structure):
     """trot_system (include/trot_gb300.h)."""
 
@@ -76,6 +86,7 @@ _SIGNATURES = {
     "trot_sample_uniform": (_i, [_p, _i, _p, _p]),
     "trot_split_key": (_i, [_p, _p]),
     "trot_local_energy_noalloc": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p]),
+    "trot_workspace_status": (_i, [_p, _p]),
     "trot_tc_gemm_bf16": (_i, [_p, _p, _p, _i, _i, _i, _p, _p]),
     "trot_profile_enable": (_i, [_i]),
     "trot_profile_collect": (_i, [_i, ctypes.c_char_p, _p, _p]),

@@ -110,7 +110,6 @@ static int check_prop(const trot_system* s) {
   return TROT_OK;
 }
 
-#define TROT_TRY(x) do { int _r = (x); if (_r != TROT_OK) return _r; } while (0)
 
 // force bias from the half Green's functions: fb = sum_s mult_s rot_chol_s G_s
 static int force_bias_from_green(const trot_system* s, const Spins& sp, const double2* green, double2* fb,
@@ -137,8 +136,11 @@ size_t trot_workspace_size(const trot_system* s, int op) {
   Spins sp = make_spins(s);
   Carver c(nullptr, 0);
   StepBuffers b;
+  if (s->precision == TROT_MIXED && op != TROT_OP_SR && op != TROT_OP_QR) {
+    if (!s->mixed) return 0;
+    return mixed_workspace_size(s, op) + 256;
+  }
   size_t n = carve_step(s, sp, c, b, op);
-  if (s->precision == TROT_MIXED) n += mixed_workspace_size(s, op) + 256;
   return n + 256;
 }
 
@@ -158,15 +160,15 @@ int trot_force_bias(const trot_system* s, const double* wa, const double* wb, do
   TROT_TRY(check_meas(s, false));
   if (!out) { set_error("null output"); return TROT_ERR_NULL_PTR; }
   Spins sp = make_spins(s);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (s->precision == TROT_MIXED)
+    return mixed_force_bias(s, sp, (const double2*)wa, (const double2*)wb, (double2*)out, ws, ws_bytes, st);
   Carver c(ws, ws_bytes);
   StepBuffers b;
   carve_step(s, sp, c, b, TROT_OP_FORCE_BIAS);
   if (!c.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, c.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
-  cudaStream_t st = (cudaStream_t)stream;
   TROT_TRY(launch_green(sp, s->n_walkers, s->norb, (const double2*)wa, (const double2*)wb, b.green, nullptr,
                         nullptr, st));
-  if (s->precision == TROT_MIXED)
-    return mixed_force_bias(s, sp, b.green, (double2*)out, c, st);
   return force_bias_from_green(s, sp, b.green, (double2*)out, st);
 }
 
@@ -177,14 +179,15 @@ int trot_local_energy(const trot_system* s, const double* wa, const double* wb, 
   TROT_TRY(check_meas(s, true));
   if (!out) { set_error("null output"); return TROT_ERR_NULL_PTR; }
   Spins sp = make_spins(s);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (s->precision == TROT_MIXED)
+    return mixed_local_energy(s, sp, (const double2*)wa, (const double2*)wb, (double2*)out, ws, ws_bytes, st);
   Carver c(ws, ws_bytes);
   StepBuffers b;
   carve_step(s, sp, c, b, TROT_OP_LOCAL_ENERGY);
   if (!c.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, c.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
-  cudaStream_t st = (cudaStream_t)stream;
   const int W = s->n_walkers, N = s->norb, G = s->nchol;
   TROT_TRY(launch_green(sp, W, N, (const double2*)wa, (const double2*)wb, b.green, nullptr, b.e1, st));
-  if (s->precision == TROT_MIXED) return mixed_local_energy(s, sp, b.green, b.e1, (double2*)out, c, st);
   TROT_TRY(force_bias_from_green(s, sp, b.green, b.fb, st));
   TROT_TRY(launch_exchange(sp, W, N, G, b.green, b.exc, st));
   return launch_energy_combine(W, G, exchange_chunks(G), s->h0, b.fb, b.e1, b.exc, (double2*)out, st);
@@ -198,16 +201,16 @@ int trot_apply_trotter(const trot_system* s, const double* wa, const double* wb,
   TROT_TRY(check_prop(s));
   if (!xs) { set_error("null fields"); return TROT_ERR_NULL_PTR; }
   Spins sp = make_spins(s);
-  Carver c(ws, ws_bytes);
-  StepBuffers b;
-  carve_step(s, sp, c, b, TROT_OP_APPLY_TROTTER);
-  if (!c.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, c.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
   cudaStream_t st = (cudaStream_t)stream;
   const int W = s->n_walkers, N = s->norb, G = s->nchol;
   TrotterArgs a{};
   a.W = W; a.N = N; a.G = G; a.nterms = s->n_exp_terms; a.sqrt_dt = s->sqrt_dt; a.expH = s->exp_h1_half;
   a.in_a = (const double2*)wa; a.in_b = (const double2*)wb; a.out_a = (double2*)oa; a.out_b = (double2*)ob;
-  if (s->precision == TROT_MIXED) return mixed_apply_trotter(s, sp, (const double2*)xs, a, c, st);
+  if (s->precision == TROT_MIXED) return mixed_apply_trotter(s, sp, (const double2*)xs, a, ws, ws_bytes, st);
+  Carver c(ws, ws_bytes);
+  StepBuffers b;
+  carve_step(s, sp, c, b, TROT_OP_APPLY_TROTTER);
+  if (!c.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, c.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
   TROT_TRY(launch_zgemm_cr(W, N * N, G, 1.0, (const double2*)xs, G, s->chol_flat, N * N, false, b.vhs, N * N,
                            false, st));
   a.vhs = b.vhs;
@@ -226,16 +229,16 @@ int trot_prop_step(const trot_system* s, const trot_state* state, const double* 
     return TROT_ERR_NULL_PTR;
   }
   Spins sp = make_spins(s);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (s->precision == TROT_MIXED)
+    return mixed_prop_step(s, sp, state, fields, (double2*)energy_out, ws, ws_bytes, st);
   Carver c(ws, ws_bytes);
   StepBuffers b;
   carve_step(s, sp, c, b, TROT_OP_PROP_STEP);
   if (!c.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, c.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
-  cudaStream_t st = (cudaStream_t)stream;
   const int W = s->n_walkers, N = s->norb, G = s->nchol;
   double2* wa = (double2*)state->walkers_a;
   double2* wb = (double2*)state->walkers_b;
-  if (s->precision == TROT_MIXED)
-    return mixed_prop_step(s, sp, state, fields, (double2*)energy_out, b, c, st);
   // 1. Green's functions (+ one-body energy) of the current walkers
   TROT_TIMED("green", st, launch_green(sp, W, N, wa, wb, b.green, nullptr, energy_out ? b.e1 : nullptr, st));
   // 2. force bias
@@ -261,6 +264,13 @@ int trot_prop_step(const trot_system* s, const trot_state* state, const double* 
   // 7. population-control shift, node count
   TROT_TIMED("step_finalize", st, launch_step_finalize(W, state->weights, state->scalars, (long long*)state->node_encounters,
                                                        b.node_flag, s->pop_control_damping, s->dt, st));
+  return TROT_OK;
+}
+
+int trot_workspace_status(const void* workspace, int* status_out) {
+  if (!workspace || !status_out) { set_error("null pointer"); return TROT_ERR_NULL_PTR; }
+  cudaError_t e = cudaMemcpy(status_out, workspace, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e, "trot_workspace_status");
   return TROT_OK;
 }
 

@@ -2,6 +2,8 @@
 #pragma once
 #include "common.cuh"
 
+#define TROT_TRY(x) do { int _r = (x); if (_r != TROT_OK) return _r; } while (0)
+
 namespace trot {
 
 // Bump allocator over the caller's workspace (256-byte aligned slices).

@@ -89,8 +89,7 @@ def force_bias_batched(walkers, ham_data, meas_ctx, trial_data, walker_kind, pre
     native.check_walker_tensor(wa, ca.shape[0], ca.shape[1])
     if wb is not None:
         native.check_walker_tensor(wb, cb.shape[0], cb.shape[1], W)
-    s = native.system(kind, W, trial_data, meas_ctx, prop_ctx if precision == _lib.MIXED else None,
-                      precision=precision)
+    s = native.system(kind, W, trial_data, meas_ctx, None, precision=precision)
     G = s.nchol
     out = torch.empty((W, G), dtype=torch.complex128, device=wa.device)
     ws, nws = native.ws_for(s, _lib.OP_FORCE_BIAS)
@@ -108,8 +107,7 @@ def local_energy_batched(walkers, ham_data, meas_ctx, trial_data, walker_kind, p
     native.check_walker_tensor(wa, ca.shape[0], ca.shape[1])
     if wb is not None:
         native.check_walker_tensor(wb, cb.shape[0], cb.shape[1], W)
-    s = native.system(kind, W, trial_data, meas_ctx, prop_ctx if precision == _lib.MIXED else None,
-                      h0=_h0(ham_data), precision=precision)
+    s = native.system(kind, W, trial_data, meas_ctx, None, h0=_h0(ham_data), precision=precision)
     out = torch.empty(W, dtype=torch.complex128, device=wa.device)
     ws, nws = native.ws_for(s, _lib.OP_LOCAL_ENERGY)
     _lib.call("trot_local_energy", ctypes.byref(s), native.ptr(wa), native.ptr(wb), out.data_ptr(), ws, nws,
@@ -117,22 +115,24 @@ def local_energy_batched(walkers, ham_data, meas_ctx, trial_data, walker_kind, p
     return out
 
 
-def _kernels(walker_kind):
+def _kernels(walker_kind, precision=_lib.FP64):
     @batched
     def force_bias(walkers, ham_data, meas_ctx, trial_data):
-        return force_bias_batched(walkers, ham_data, meas_ctx, trial_data, walker_kind)
+        return force_bias_batched(walkers, ham_data, meas_ctx, trial_data, walker_kind, precision)
 
     @batched
     def energy(walkers, ham_data, meas_ctx, trial_data):
-        return local_energy_batched(walkers, ham_data, meas_ctx, trial_data, walker_kind)
+        return local_energy_batched(walkers, ham_data, meas_ctx, trial_data, walker_kind, precision)
 
     return {k_force_bias: force_bias, k_energy: energy}
 
 
-def make_rhf_meas_ops(sys: System, memory_mode: str = "high") -> MeasOps:
+def make_rhf_meas_ops(sys: System, memory_mode: str = "high", mixed_precision: bool = False) -> MeasOps:
     """trot/meas/rhf.py:322-367.  ``memory_mode`` is accepted for signature
     compatibility: the CUDA exchange kernel always streams over Cholesky
-    vectors, so "high" and "low" compute the same numbers."""
+    vectors, so "high" and "low" compute the same numbers.  With
+    ``mixed_precision`` the force bias and local energy run on the tensor
+    cores (exact-slice BF16 products, float-float epilogue)."""
     if memory_mode not in ("high", "low"):
         raise ValueError(f"Unsupported RHF measurement memory_mode: {memory_mode!r}")
     if sys.walker_kind not in ("restricted", "unrestricted"):
@@ -140,20 +140,20 @@ def make_rhf_meas_ops(sys: System, memory_mode: str = "high") -> MeasOps:
     ops = MeasOps(
         overlap=_make_overlap(sys.walker_kind),
         build_meas_ctx=lambda ham_data, trial_data: build_rhf_meas_ctx(ham_data, trial_data, memory_mode),
-        kernels=_kernels(sys.walker_kind),
+        kernels=_kernels(sys.walker_kind, _lib.MIXED if mixed_precision else _lib.FP64),
     )
     object.__setattr__(ops, "walker_kind", sys.walker_kind)
     return ops
 
 
-def make_uhf_meas_ops(sys: System) -> MeasOps:
-    """trot/meas/uhf.py:339-379."""
+def make_uhf_meas_ops(sys: System, mixed_precision: bool = False) -> MeasOps:
+    """trot/meas/uhf.py:339-379 (``mixed_precision`` as in make_rhf_meas_ops)."""
     if sys.walker_kind != "unrestricted":
         raise NotImplementedError(f"CUDA path: UHF measurements with {sys.walker_kind} walkers")
     ops = MeasOps(
         overlap=_make_overlap(sys.walker_kind),
         build_meas_ctx=build_uhf_meas_ctx,
-        kernels=_kernels(sys.walker_kind),
+        kernels=_kernels(sys.walker_kind, _lib.MIXED if mixed_precision else _lib.FP64),
     )
     object.__setattr__(ops, "walker_kind", sys.walker_kind)
     return ops

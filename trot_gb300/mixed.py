@@ -1,0 +1,138 @@
+"""Operands of the mixed-precision (tensor-core) path.
+
+Built once per (trial, Hamiltonian, dt) on the host and kept on the device:
+
+* exact-slice BF16 copies of the half-rotated Cholesky vectors for the local
+  energy / force bias: each row (g, i) over orbitals p is written as
+  sum_t 2^(e - 8(t+1)) q_t (t < 5) with integer slices |q_t| <= 255 and one
+  exponent per row, laid out as 128-row tiles of whole Cholesky vectors;
+* a 3-term BF16 split (hi + mid + lo) of the Cholesky vectors, transposed to
+  (N*N, G), for the VHS build;
+* exp(-dt/2 h1_eff) in FP32 for the one-body half steps.
+
+``context(meas_ctx, prop_ctx, kind)`` returns the cached ``MixedCtx`` whose
+``data_ptr()`` is the address of the ``trot_mixed`` struct the C ABI reads.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .core import device
+
+SLICES = 5
+MAX_ORDER = 4
+KPAD = 128
+VHS_SLICES = 3
+VHS_ORDER = 2
+
+
+def exact_slices(x: np.ndarray, slices: int = SLICES, bits: int = 8):
+    """Fixed-point slices of the rows (last axis) of ``x``: returns
+    (q (slices, ...) float32 integers in [-255, 255], e int32 row exponents)
+    with x ~= sum_t q_t 2^(e - bits (t+1))."""
+    x = np.asarray(x, dtype=np.float64)
+    mx = np.max(np.abs(x), axis=-1)
+    e = np.where(mx > 0, np.ceil(np.log2(np.where(mx > 0, mx, 1.0))), 0.0).astype(np.int32)
+    r = x.copy()
+    out = []
+    lim = float(2 ** bits - 1)
+    for t in range(slices):
+        sc = np.ldexp(1.0, e - bits * (t + 1))[..., None]
+        q = np.clip(np.rint(r / sc), -lim, lim)
+        out.append(q.astype(np.float32))
+        r = r - q * sc
+    return np.stack(out), e
+
+
+def plain_split(x: np.ndarray, slices: int = VHS_SLICES) -> list[torch.Tensor]:
+    """x ~= sum of bf16 terms, each the round-to-nearest bf16 of the remainder."""
+    r = torch.as_tensor(np.asarray(x, dtype=np.float64))
+    out = []
+    for _ in range(slices):
+        h = r.to(torch.float32).to(torch.bfloat16)
+        out.append(h)
+        r = r - h.to(torch.float64)
+    return out
+
+
+def gammas_per_block(n: int) -> int:
+    return max(1, 128 // n)
+
+
+def rot_tiles(rot_chol: np.ndarray):
+    """(G, n, N) -> bf16 slices (SLICES, nblk, 128, KPAD) and exponents (nblk, 128)."""
+    G, n, N = rot_chol.shape
+    if n > 64 or N > KPAD:
+        raise NotImplementedError(f"mixed path: n={n}, N={N} outside the tensor-core tile limits (n<=64, N<={KPAD})")
+    gb = gammas_per_block(n)
+    nblk = (G + gb - 1) // gb
+    rows = np.zeros((nblk, 128, KPAD), dtype=np.float64)
+    for blk in range(nblk):
+        g0, g1 = blk * gb, min(G, (blk + 1) * gb)
+        r = rot_chol[g0:g1].reshape(-1, N)
+        rows[blk, : r.shape[0], :N] = r
+    q, e = exact_slices(rows)
+    return torch.from_numpy(q).to(torch.bfloat16), torch.from_numpy(e.astype(np.int32)), gb, nblk
+
+
+class MixedCtx:
+    """Device operands + the host ``trot_mixed`` struct pointing at them."""
+
+    def __init__(self, rot_a, rot_b, chol_flat=None, exp_h1_half=None):
+        dev = device()
+        s = _lib.TrotMixed()
+        s.slices, s.max_order, s.kpad = SLICES, MAX_ORDER, KPAD
+        self._keep = []
+        for k, rc in enumerate((rot_a, rot_b)):
+            if rc is None:
+                continue
+            q, e, gb, nblk = rot_tiles(rc)
+            q, e = q.to(dev), e.to(dev)
+            self._keep += [q, e]
+            s.gammas_per_block[k], s.n_blocks[k] = gb, nblk
+            s.rot_slices[k], s.rot_exp[k] = q.data_ptr(), e.data_ptr()
+        self.struct = s
+        if chol_flat is None:
+            return
+        G, N2 = chol_flat.shape
+        n2pad = (N2 + 127) // 128 * 128
+        gpad = (G + 63) // 64 * 64
+        lt = np.zeros((n2pad, gpad), dtype=np.float64)
+        lt[:N2, :G] = chol_flat.T
+        sl = torch.stack(plain_split(lt)).to(dev).contiguous()
+        self._keep.append(sl)
+        s.vhs_slices, s.vhs_order, s.n2pad, s.gpad = VHS_SLICES, VHS_ORDER, n2pad, gpad
+        s.chol_t_slices = sl.data_ptr()
+        eh = torch.as_tensor(np.asarray(exp_h1_half, dtype=np.float32)).to(dev).contiguous()
+        self._keep.append(eh)
+        s.exp_h1_half_f32 = eh.data_ptr()
+        self.struct = s
+
+    def data_ptr(self) -> int:
+        return ctypes.addressof(self.struct)
+
+
+def context(meas_ctx=None, prop_ctx=None) -> MixedCtx:
+    """Mixed operands for this (meas_ctx, prop_ctx) pair (either may be None),
+    built on first use and cached on the context object."""
+    owner = meas_ctx if meas_ctx is not None else prop_ctx
+    cache = owner.__dict__.setdefault("_mixed_cache", {})
+    key = id(prop_ctx) if meas_ctx is not None else None
+    hit = cache.get(key)
+    if hit is not None and hit[0] is prop_ctx:
+        return hit[1]
+    ra = rb = None
+    if meas_ctx is not None:
+        _, _, ra, rb = meas_ctx.spin_arrays()
+        ra = ra.cpu().numpy()
+        rb = None if rb is None else rb.cpu().numpy()
+    cf = eh = None
+    if prop_ctx is not None:
+        cf, eh = prop_ctx.chol_flat.cpu().numpy(), prop_ctx.exp_h1_half.cpu().numpy()
+    m = MixedCtx(ra, rb, cf, eh)
+    cache[key] = (prop_ctx, m)
+    return m

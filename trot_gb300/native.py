@@ -66,7 +66,7 @@ def check_walker_tensor(w, N, n, W=None):
 
 
 def system(kind, n_walkers, trial, meas_ctx=None, prop_ctx=None, h0=0.0, params=None,
-           precision=_lib.FP64) -> _lib.TrotSystem:
+           precision=_lib.FP64, mixed=None) -> _lib.TrotSystem:
     """Fill a trot_system for one call. Keeps no references: the caller's
     objects own the device buffers for the duration of the (stream-ordered) call."""
     s = _lib.TrotSystem()
@@ -91,7 +91,12 @@ def system(kind, n_walkers, trial, meas_ctx=None, prop_ctx=None, h0=0.0, params=
         s.h0_prop = float(prop_ctx.h0_prop)
         s.dt = float(prop_ctx.dt)
         s.sqrt_dt = float(prop_ctx.sqrt_dt)
-        s.mixed = ptr(getattr(prop_ctx, "mixed", None))
+    if precision == _lib.MIXED:
+        if mixed is None:
+            from . import mixed as _mixed
+
+            mixed = _mixed.context(meas_ctx, prop_ctx)
+        s.mixed = mixed.data_ptr()
     if params is not None:
         s.n_exp_terms = int(params.n_exp_terms)
         s.weight_floor = float(getattr(params, "weight_floor", 1.0e-3))

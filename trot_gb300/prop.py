@@ -35,7 +35,6 @@ class CholAfqmcCtx:
     h0_prop: float
     chol_flat: torch.Tensor  # (G, N*N) float64
     norb: int
-    mixed: Any = None  # device context of the mixed-precision path
 
     @property
     def mf_shifts(self) -> torch.Tensor:
@@ -68,10 +67,6 @@ def _build_prop_ctx(ham_data: HamChol, rdm1, dt: float, mixed_precision: bool = 
     ctx = CholAfqmcCtx(dt=float(dt), sqrt_dt=float(np.sqrt(dt)), exp_h1_half=as_dev(eh),
                        mf_shifts_im=as_dev(t), h0_prop=h0_prop, chol_flat=as_dev(chol_flat),
                        norb=int(h1.shape[0]))
-    if mixed_precision:
-        from . import mixed
-
-        ctx = mixed.attach(ctx)
     return ctx
 
 
@@ -109,7 +104,10 @@ def make_trotter_ops(ham_basis: str, walker_kind: str, mixed_precision: bool = F
         s.sqrt_dt, s.dt = ctx.sqrt_dt, ctx.dt
         s.exp_h1_half, s.chol_flat = native.ptr(ctx.exp_h1_half), native.ptr(ctx.chol_flat)
         s.mf_shifts_im = native.ptr(ctx.mf_shifts_im)
-        s.mixed = native.ptr(ctx.mixed)
+        if prec == _lib.MIXED:
+            from . import mixed
+
+            s.mixed = mixed.context(None, ctx).data_ptr()
         s.mo_a = s.mo_b = s.exp_h1_half  # not read by the Trotter op; keeps the struct check satisfied
         oa = torch.empty_like(wa)
         ob = torch.empty_like(wb) if unres else None

@@ -106,6 +106,9 @@ CONFIGS = {
                          dt=0.005, n_steps=50, qr_every=5, kind="rhf_r"),
     "cfg2_uhf_n120": dict(norb=120, nelec=(12, 10), nchol=600, decay=150.0, n_walkers=1024,
                           dt=0.005, n_steps=200, qr_every=10, kind="uhf_u"),
+    # the cfg2 system with fewer walkers: small case for profiler captures
+    "cfg2_uhf_n120_w256": dict(norb=120, nelec=(12, 10), nchol=600, decay=150.0, n_walkers=256,
+                               dt=0.005, n_steps=200, qr_every=10, kind="uhf_u"),
     "cfg3_rhf_n80": dict(norb=80, nelec=(10, 10), nchol=400, decay=30.0, n_walkers=512,
                          dt=0.01, n_steps=200, qr_every=20, kind="rhf_r"),
 }
