@@ -125,6 +125,46 @@ def _array_result(obj):
     return f
 
 
+class _AtIndex:
+    def __init__(self, arr, idx):
+        self.arr, self.idx = arr, idx
+
+    def set(self, v):
+        out = np.array(self.arr, copy=True).view(JArr)
+        out[self.idx] = v
+        return out
+
+    def add(self, v):
+        out = np.array(self.arr, copy=True).view(JArr)
+        out[self.idx] += v
+        return out
+
+
+class _At:
+    def __init__(self, arr):
+        self.arr = arr
+
+    def __getitem__(self, idx):
+        return _AtIndex(self.arr, idx)
+
+
+class JArr(np.ndarray):
+    """ndarray with jax's functional ``x.at[idx].set(v)`` update syntax."""
+
+    @property
+    def at(self):
+        return _At(self)
+
+
+def _jarr(fn):
+    def f(*a, **k):
+        r = fn(*a, **k)
+        return r.view(JArr) if isinstance(r, np.ndarray) else r
+
+    f.__name__ = getattr(fn, "__name__", "f")
+    return f
+
+
 class _Dummy:
     def __init__(self, *a, **k):
         self.args = a
@@ -140,6 +180,8 @@ def install():
             setattr(jnp, k, _array_result(getattr(np, k)))
     jnp.linalg = np.linalg
     jnp.ndarray = np.ndarray
+    for name in ("zeros", "zeros_like", "ones", "eye", "array", "asarray", "full"):
+        setattr(jnp, name, _jarr(getattr(np, name)))
     lax = types.ModuleType("jax.lax")
     lax.complex = lambda a, b: np.asarray(a) + 1.0j * np.asarray(b)
     lax.scan = _scan

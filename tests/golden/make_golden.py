@@ -40,6 +40,8 @@ from trot.trial import uhf as tuhf  # noqa: E402
 from trot import walkers as wk  # noqa: E402
 
 from trot_gb300 import synthetic  # noqa: E402
+from trot.meas import cisd as mcisd  # noqa: E402
+from trot.trial import cisd as tcisd  # noqa: E402
 
 INJ = _jaxshim.INJECT
 
@@ -166,7 +168,32 @@ def _save_state(out, prefix, st, kind):
     out[prefix + "nodes"] = int(st.node_encounters)
 
 
+def cisd_case(name, norb, nocc, nchol, n_walkers, seed=0, h0=0.4, noise=0.1):
+    cs = synthetic.make_cisd_system(norb, nocc, nchol, decay=30.0, seed=seed, h0=h0)
+    ham = HamChol(h0=np.asarray(h0), h1=cs.h1, chol=cs.chol, basis="restricted")
+    sysm = System(norb=norb, nelec=(nocc, nocc), walker_kind="restricted")
+    trial = tcisd.CisdTrial(ci1=cs.ci1, ci2=cs.ci2)
+    meas_ops = mcisd.make_cisd_meas_ops(sysm, memory_mode="high", mixed_precision=False, testing=True)
+    trial_ops = tcisd.make_cisd_trial_ops(sysm)
+    meas_ctx = meas_ops.build_meas_ctx(ham, trial)
+    ref = np.eye(norb)[:, :nocc]
+    w = synthetic.perturbed_walkers(ref, n_walkers, noise, seed + 5)
+    vm = _jaxshim.vmap
+    out = dict(h0=h0, h1=cs.h1, chol=cs.chol, ci1=cs.ci1, ci2=cs.ci2, walkers=w)
+    out["overlap"] = np.asarray(vm(trial_ops.overlap, in_axes=(0, None))(w, trial))
+    out["overlap_meas"] = np.asarray(vm(meas_ops.overlap, in_axes=(0, None))(w, trial))
+    out["force_bias"] = np.asarray(vm(meas_ops.require_kernel("force_bias"), in_axes=(0, None, None, None))(
+        w, ham, meas_ctx, trial))
+    out["energy"] = np.asarray(vm(meas_ops.require_kernel("energy"), in_axes=(0, None, None, None))(
+        w, ham, meas_ctx, trial))
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **{k: np.asarray(v) for k, v in out.items()})
+    print(f"wrote {path}: {os.path.getsize(path) / 1e3:.0f} kB")
+
+
 if __name__ == "__main__":
+    cisd_case("cisd_small", norb=12, nocc=3, nchol=20, n_walkers=4)
+    cisd_case("cisd_n20", norb=20, nocc=5, nchol=50, n_walkers=3, seed=1)
     case("rhf_r_small", norb=10, nelec=(3, 3), nchol=16, n_walkers=5, kind="rhf_r")
     case("rhf_u_small", norb=9, nelec=(3, 3), nchol=14, n_walkers=4, kind="rhf_u")
     case("uhf_u_small", norb=11, nelec=(4, 2), nchol=18, n_walkers=5, kind="uhf_u")

@@ -94,3 +94,15 @@ def test_mixed_step(kind, N, nelec, G, W, decay):
     assert np.array_equal(wf > 0, wm > 0)
     if live.any():
         assert rel(wm[live], wf[live]) <= 1e-3
+
+
+@pytest.mark.parametrize("kind,N,nelec,G,W", [("uhf_u", 40, (6, 5), 96, 700), ("rhf_r", 30, (7, 7), 64, 333)])
+def test_mixed_energy_many_walker_tiles(kind, N, nelec, G, W):
+    """Enough walkers that every CTA of the exchange kernel runs several walker
+    tiles (both TMEM accumulator buffers, ring wrap-around)."""
+    ss, walkers, F, M = _setups(kind, N, nelec, G, W, 30.0, 0.1)
+    w = F.walkers(walkers)
+    e64 = cpu(F.energy(w))
+    emx = cpu(M.energy(w))
+    assert np.max(np.abs(emx - e64)) <= 1e-5
+    assert rel(cpu(M.force_bias(w)), cpu(F.force_bias(w))) <= 1e-9

@@ -35,10 +35,12 @@ def test_rot_tiles_layout():
     rng = np.random.default_rng(2)
     G, n, N = 25, 12, 120
     rc = rng.normal(size=(G, n, N))
-    q, e, gb, nblk = mixed.rot_tiles(rc)
+    img, e, gb, nblk = mixed.rot_tiles(rc)
     assert gb == 10 and nblk == 3
-    assert tuple(q.shape) == (mixed.SLICES, nblk, 128, mixed.KPAD)
-    qd = q.to(torch.float64).numpy()
+    assert tuple(img.shape) == (nblk, mixed.SLICES, 128, mixed.KPAD)
+    # undo the core-matrix order: index (rg, kg, ri, ki) -> (row 8 rg + ri, k 8 kg + ki)
+    im = img.to(torch.float64).numpy().reshape(nblk, mixed.SLICES, 16, 16, 8, 8)
+    qd = im.transpose(1, 0, 2, 4, 3, 5).reshape(mixed.SLICES, nblk, 128, mixed.KPAD)
     # row (g=13, i=4) lives in block 1, row 3*12+4, orbitals 0..N-1; padding is zero
     rec = sum(qd[t, 1, 3 * n + 4, :N] * np.ldexp(1.0, int(e[1, 3 * n + 4]) - 8 * (t + 1)) for t in range(mixed.SLICES))
     np.testing.assert_allclose(rec, rc[13, 4], rtol=0, atol=2.0 ** -40 * np.max(np.abs(rc[13, 4])))

@@ -42,15 +42,119 @@ TROT_D ff ff_shfl_xor(ff x, int o) {
   return ff{__shfl_xor_sync(0xffffffffu, x.hi, o), __shfl_xor_sync(0xffffffffu, x.lo, o)};
 }
 
+// ------------------------------------------------------------------ Green's functions in float-float
+// Same quantities as green_kernel (green.cu): M_s = C_s^T w_s, M_s^{-1} by
+// FP64 Gauss-Jordan, G_s = (w_s M_s^{-1})^T and e1 = sum_s mult_s sum G_s o rot_h1_s,
+// with the two N x n^2 products in float-float (FP32 pairs, ~2^-44 relative)
+// on the FP32 pipe instead of FP64.  One CTA per walker.
+struct ffc { ff re, im; };
+TROT_D ff ff_from_d(double x) {
+  const float h = __double2float_rn(x);
+  return ff{h, __double2float_rn(x - (double)h)};
+}
+TROT_D ff ff_fma(ff acc, ff a, ff b) { return ff_add(acc, ff_mul(a, b)); }
+
+__global__ void __launch_bounds__(256)
+green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* __restrict__ wb,
+                double2* __restrict__ green, double2* __restrict__ e1_out) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ double2 red[32];
+  __shared__ int piv;
+  const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
+  ffc* Wf = reinterpret_cast<ffc*>(smem_raw);                    // N x n
+  ff* Cf = reinterpret_cast<ff*>(Wf + (size_t)N * nmax);          // N x n
+  double2* Md = reinterpret_cast<double2*>(Cf + (size_t)N * nmax + ((N * nmax) & 1));  // n x n
+  double2* Mi = Md + nmax * nmax;                                 // n x n
+  ffc* Mif = reinterpret_cast<ffc*>(Mi + nmax * nmax);            // n x n
+  ff e1r{0.f, 0.f}, e1i{0.f, 0.f};
+  for (int s = 0; s < sp.nspin; ++s) {
+    const int n = sp.n[s];
+    const double2* w = (s == 0 ? wa : wb) + (size_t)b * N * n;
+    const double* C = sp.mo[s];
+    __syncthreads();
+    for (int e = tid; e < N * n; e += nt) {
+      const double2 x = w[e];
+      Wf[e] = ffc{ff_from_d(x.x), ff_from_d(x.y)};
+      Cf[e] = ff_from_d(C[e]);
+    }
+    __syncthreads();
+    for (int e = tid; e < n * n; e += nt) {
+      const int i = e / n, j = e % n;
+      ff ar{0.f, 0.f}, ai{0.f, 0.f};
+      for (int p = 0; p < N; ++p) {
+        const ff c = Cf[p * n + i];
+        const ffc x = Wf[p * n + j];
+        ar = ff_fma(ar, c, x.re);
+        ai = ff_fma(ai, c, x.im);
+      }
+      Md[e] = make_double2(ff_d(ar), ff_d(ai));
+    }
+    __syncthreads();
+    block_gauss_jordan(Md, n, n, Mi, &piv, red);
+    for (int e = tid; e < n * n; e += nt) Mif[e] = ffc{ff_from_d(Mi[e].x), ff_from_d(Mi[e].y)};
+    __syncthreads();
+    const double* H = sp.rot_h1[s];
+    double2* gout = green + (size_t)b * sp.ntot * N + (size_t)sp.off[s] * N;
+    const float m = (float)sp.mult[s];
+    for (int e = tid; e < n * N; e += nt) {
+      const int i = e / N, p = e % N;
+      ff gr{0.f, 0.f}, gi{0.f, 0.f};
+      for (int j = 0; j < n; ++j) {
+        const ffc x = Wf[p * n + j], y = Mif[j * n + i];
+        gr = ff_fma(gr, x.re, y.re);
+        gr = ff_sub(gr, ff_mul(x.im, y.im));
+        gi = ff_fma(gi, x.re, y.im);
+        gi = ff_fma(gi, x.im, y.re);
+      }
+      gout[e] = make_double2(ff_d(gr), ff_d(gi));
+      if (H) {
+        const ff h = ff_from_d(H[e]);
+        e1r = ff_add(e1r, ff_mul(h, ff{gr.hi * m, gr.lo * m}));
+        e1i = ff_add(e1i, ff_mul(h, ff{gi.hi * m, gi.lo * m}));
+      }
+    }
+  }
+  if (e1_out) {
+    double2 v = make_double2(ff_d(e1r), ff_d(e1i));
+    v = block_sum2(v, red);
+    if (tid == 0) e1_out[b] = v;
+  }
+}
+
+static int launch_green_ff(const Spins& sp, int W, int N, const double2* wa, const double2* wb, double2* green,
+                           double2* e1_out, cudaStream_t st) {
+  const int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
+  const size_t smem = (size_t)N * nmax * (sizeof(ffc) + sizeof(ff)) + 16 + (size_t)nmax * nmax * 3 * 16;
+  if (smem > 200 * 1024) {
+    set_error("green_ff: %zu bytes of shared memory needed", smem);
+    return TROT_ERR_UNSUPPORTED;
+  }
+  if (smem > 48 * 1024) cudaFuncSetAttribute(green_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  green_ff_kernel<<<W, 256, smem, st>>>(sp, N, wa, wb, green, e1_out);
+  TROT_CHECK_LAUNCH("green_ff_kernel");
+  return TROT_OK;
+}
+
 // ------------------------------------------------------------------ layouts
 static constexpr int kKP = 128;       // padded orbital dimension of the exact product
-static constexpr int kBN = 96;        // MMA N of the exchange tile (columns = walker rows)
+static constexpr int kBN = 48;        // MMA N of the exchange tile (columns = walker rows)
 static constexpr int kGroups = 5;     // accumulators for t + u = 0..4
 static constexpr int kSlices = 5;
+static constexpr int kSlots = 3;      // ring of Green's-function slice buffers
+static constexpr int kMaxOcc = 16;    // largest n the epilogue handles (2 * n_pad <= 32 columns per walker)
+static constexpr uint32_t kAImg = (uint32_t)kSlices * 128 * kKP * 2;  // 163840 B: 5 rot slices of a tile
+static constexpr uint32_t kBImg = (uint32_t)kBN * kKP * 2;            // 12288 B: one green slice of a tile
+
+// Row-major [rows x 128] bf16 tile -> core-matrix order (8 x 8 blocks, K fastest):
+// element (r, k) at 16-bit index (r/8)*1024 + (k/8)*64 + (r%8)*8 + k%8.
+TROT_HD uint32_t img_idx(int r, int k) {
+  return (uint32_t)((r >> 3) * 1024 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7));
+}
 
 struct SpinLayout {
-  int n, n_pad, S, WB, nwb;  // rows per walker S = 2 n_pad, walkers per tile WB
-  int gb, nblk, blk_off;     // Cholesky vectors per tile, tiles, offset in the partial array
+  int n, n_pad, S, WB, ntiles;  // rows per walker S = 2 n_pad, walkers per tile WB, walker tiles
+  int gb, nblk, blk_off;        // Cholesky vectors per 128-row tile, tiles, offset in the partial array
 };
 
 static SpinLayout spin_layout(const trot_system* s, const Spins& sp, int q) {
@@ -59,20 +163,19 @@ static SpinLayout spin_layout(const trot_system* s, const Spins& sp, int q) {
   L.n_pad = L.n + (L.n & 1);
   L.S = 2 * L.n_pad;
   L.WB = kBN / L.S;
-  L.nwb = (s->n_walkers + L.WB - 1) / L.WB;
+  L.ntiles = (s->n_walkers + L.WB - 1) / L.WB;
   const int mq = (s->kind == TROT_UHF_U) ? q : 0;
   L.gb = s->mixed->gammas_per_block[mq];
   L.nblk = s->mixed->n_blocks[mq];
   L.blk_off = q == 0 ? 0 : s->mixed->n_blocks[0];
-  if (s->kind != TROT_UHF_U && q == 1) L.blk_off = s->mixed->n_blocks[0];
   return L;
 }
 
 struct MixedBuffers {
   double2* green;
   double2* e1;
-  uint16_t* gq[2];
-  int32_t* ge[2];
+  uint16_t* gq[2];   // per spin: [tile][slice][kBN rows][kKP] in core-matrix order
+  int32_t* ge[2];    // per spin: [tile][kBN] row exponents
   double2* cs[2];
   double2* xpart;
   double2* fb;
@@ -97,8 +200,8 @@ static size_t carve_mixed(const trot_system* s, const Spins& sp, Carver& c, Mixe
     m.nblk_total = 0;
     for (int q = 0; q < sp.nspin; ++q) {
       SpinLayout L = spin_layout(s, sp, q);
-      m.gq[q] = c.take<uint16_t>((size_t)kSlices * W * L.S * kKP);
-      m.ge[q] = c.take<int32_t>(W * L.S);
+      m.gq[q] = c.take<uint16_t>((size_t)L.ntiles * kSlices * kBN * kKP);
+      m.ge[q] = c.take<int32_t>((size_t)L.ntiles * kBN);
       m.cs[q] = c.take<double2>(W * G);
       m.nblk_total += L.nblk;
     }
@@ -129,16 +232,21 @@ size_t mixed_workspace_size(const trot_system* s, int op) {
 // Rows (b, spin, c in {re, im}, j) of the half Green's function over orbitals
 // p, as exact fixed-point bf16 slices: v = round(x 2^(40 - e)) (|v| <= 2^40),
 // balanced base-256 digits q_0..q_4 (|q| <= 255), x ~= sum_t q_t 2^(e - 8(t+1)).
-// Output layout per spin: [slice][walker][row in 0..S)][kpad], rows j >= n zero.
+// Written straight into the shared-memory image of the exchange kernel's B
+// operand: per walker tile, per slice, kBN rows (walker bl, row c*n_pad + j) x
+// kKP orbitals in core-matrix order; padding rows are zero.  One CTA per tile.
 __global__ void __launch_bounds__(256)
-green_slices_kernel(int N, int n, int n_pad, int W, int ntot, int off, const double2* __restrict__ green,
+green_slices_kernel(int N, int n, int n_pad, int WB, int W, int ntot, int off, const double2* __restrict__ green,
                     uint16_t* __restrict__ gq, int32_t* __restrict__ ge) {
-  const int b = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int S = 2 * n_pad;
-  for (int row = warp; row < S; row += blockDim.x >> 5) {
-    const int c = row / n_pad, j = row % n_pad;
-    const bool valid = j < n;
-    const double* src = reinterpret_cast<const double*>(green + (size_t)b * ntot * N + (size_t)(off + j) * N);
+  for (int row = warp; row < kBN; row += blockDim.x >> 5) {
+    const int bl = row / S, rr = row % S;
+    const int b = tile * WB + bl;
+    const int c = rr / n_pad, j = rr % n_pad;
+    const bool valid = bl < WB && b < W && j < n;
+    const double* src = valid ? reinterpret_cast<const double*>(green + (size_t)b * ntot * N + (size_t)(off + j) * N)
+                              : nullptr;
     double x[kKP / 32];
     unsigned long long mx = 0;
 #pragma unroll
@@ -158,25 +266,19 @@ green_slices_kernel(int N, int n, int n_pad, int W, int ntot, int off, const dou
       const double m = frexp(__longlong_as_double((long long)mx), &ex);  // mx = m 2^ex, m in [0.5, 1)
       e = (m == 0.5) ? ex - 1 : ex;                                       // mx <= 2^e
     }
-    const size_t rowg = (size_t)b * S + row;
-    if (lane == 0) ge[rowg] = e;
+    if (lane == 0) ge[(size_t)tile * kBN + row] = e;
 #pragma unroll
     for (int k = 0; k < kKP / 32; ++k) {
       const int p = lane + 32 * k;
       long long v = (long long)rint(ldexp(x[k], 8 * kSlices - e));
-      int q[kSlices];
 #pragma unroll
       for (int t = 0; t < kSlices; ++t) {
         const int sh = 8 * (kSlices - 1 - t);
         long long d = sh > 0 ? ((v + (1ll << (sh - 1))) >> sh) : v;
         d = d > 255 ? 255 : (d < -255 ? -255 : d);
-        q[t] = (int)d;
         v -= d << sh;
-      }
-#pragma unroll
-      for (int t = 0; t < kSlices; ++t) {
-        const __nv_bfloat16 h = __int2bfloat16_rn(q[t]);
-        gq[((size_t)t * W * S + rowg) * kKP + p] = *reinterpret_cast<const uint16_t*>(&h);
+        const __nv_bfloat16 h = __int2bfloat16_rn((int)d);
+        gq[((size_t)tile * kSlices + t) * kBN * kKP + img_idx(row, p)] = *reinterpret_cast<const uint16_t*>(&h);
       }
     }
   }
@@ -184,214 +286,264 @@ green_slices_kernel(int N, int n, int n_pad, int W, int ntot, int off, const dou
 
 // ------------------------------------------------------------------ exact exchange / trace kernel
 // One CTA = one tile of gb Cholesky vectors (128 rows (g, i)) against a range of
-// walker tiles (WB walkers x S rows).  The four rot_chol slices of the tile stay
-// in shared memory; the Green's-function slices stream through two buffers.
-// Products q_t (rot) x q_u (green) with t + u = d accumulate exactly in TMEM
-// accumulator d (d = 0..4, 96 columns each).  The epilogue rebuilds
-// f_g[i][j] = 2^(eA + eB - 16) sum_d 2^(-8 d) A_d as float-float and forms, per
-// walker, sum_g sum_ij f_gij f_gji (exchange, trot/meas/rhf.py:33-60) and
-// c_g = sum_i f_gii (Coulomb / force bias, trot/meas/rhf.py:119-125).
+// walker tiles (WB walkers x S rows, kBN MMA columns).  Warp 8 (one lane) is
+// the producer: it bulk-copies the five rot_chol slices of the tile into shared
+// memory once, streams the Green's-function slices of each walker tile through
+// a 3-slot ring, and issues the MMAs: products q_t (rot) x q_u (green) with
+// t + u = d accumulate exactly in TMEM group d (d = 0..4), in one of two
+// accumulator buffers, so the MMAs of walker tile k+1 overlap the epilogue of
+// tile k.  Warps 0-7 are the epilogue (two warps per TMEM lane quadrant, each
+// taking half of the columns j): they rebuild
+// f_g[i][j] = 2^(eA + eB - 16) sum_d 2^(-8 d) A_d in float-float and form, per
+// walker, the exchange sum_g sum_ij f_gij f_gji (trot/meas/rhf.py:33-60) and the
+// traces c_g = sum_i f_gii (Coulomb / force bias, trot/meas/rhf.py:119-125).
 struct ExArgs {
   SpinLayout L;
-  int G, W, mult, wb_per_cta;
-  const uint16_t* rot_q;
-  const int32_t* rot_e;
-  const uint16_t* green_q;
-  const int32_t* green_e;
+  int G, W, mult, tiles_per_cta;
+  const uint16_t* rot_img;   // [nblk][slices][128][kKP] core-matrix order
+  const int32_t* rot_e;      // [nblk][128]
+  const uint16_t* green_img; // [ntiles][slices][kBN][kKP]
+  const int32_t* green_e;    // [ntiles][kBN]
   double2* cs;
   double2* xpart;
   int nblk_total;
   int* status;
 };
 
-static constexpr size_t kExSmemA = (size_t)kSlices * 128 * kKP * 2;   // 163840
-static constexpr size_t kExSmemB = (size_t)2 * kBN * kKP * 2;         // 49152
-static constexpr size_t kExSmemF = (size_t)128 * 32 * sizeof(ff);     // 32768, aliases the B buffers
-static_assert(kExSmemF <= kExSmemB, "epilogue buffer must fit in the idle B buffers");
-static constexpr size_t kExSmem = kExSmemA + kExSmemB + 128 * 4 + kBN * 4 + 128 * 2 * sizeof(ff) +
-                                  8 * 2 * sizeof(ff) + 3 * 8 + 16 + 128;
+static constexpr int kExThreads = 288;  // 8 epilogue warps + 1 producer warp
+static constexpr size_t kExOffRing = kAImg;
+static constexpr size_t kExOffF = kExOffRing + (size_t)kSlots * kBImg;        // [128][16] ff
+static constexpr size_t kExOffEA = kExOffF + (size_t)128 * kMaxOcc * sizeof(ff);
+static constexpr size_t kExOffC = kExOffEA + 128 * 4;                          // [128][2] ff traces
+static constexpr size_t kExOffRed = kExOffC + 128 * 2 * sizeof(ff);            // [8 warps][2] ff
+static constexpr size_t kExOffBar = kExOffRed + 8 * 2 * sizeof(ff);            // 11 mbarriers + flags
+static constexpr size_t kExSmem = kExOffBar + 16 * 8 + 64;
 
-TROT_D uint32_t off128(int r, int k) {  // core-matrix layout for a [rows x 128] K-major tile
-  return (uint32_t)((r >> 3) * 2048 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
-}
-
-__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v) {
-  uint32_t r0, r1, r2, r3;
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-               : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-  v[0] = __uint_as_float(r0); v[1] = __uint_as_float(r1); v[2] = __uint_as_float(r2); v[3] = __uint_as_float(r3);
-}
-
-__global__ void __launch_bounds__(128, 1) exchange_exact_kernel(ExArgs a) {
+__global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
   unsigned char* sA = base;
-  unsigned char* sB = sA + kExSmemA;
-  ff* sF = reinterpret_cast<ff*>(sB);  // [128][32]; used only after every MMA of the tile completed
-  int* eA = reinterpret_cast<int*>(sB + kExSmemB);
-  int* eB = eA + 128;
-  ff* sC = reinterpret_cast<ff*>(eB + kBN);      // [128][2] traces (re, im)
-  ff* sRed = sC + 128 * 2;                       // [4 warps][2]
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(sRed + 16);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 3);
+  unsigned char* ring = base + kExOffRing;
+  ff* sF = reinterpret_cast<ff*>(base + kExOffF);
+  int* eA = reinterpret_cast<int*>(base + kExOffEA);
+  ff* sC = reinterpret_cast<ff*>(base + kExOffC);
+  ff* sRed = reinterpret_cast<ff*>(base + kExOffRed);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + kExOffBar);
+  uint64_t* a_full = bars;
+  uint64_t* full = bars + 1;        // [kSlots]
+  uint64_t* empty = bars + 4;       // [kSlots]
+  uint64_t* acc_full = bars + 7;    // [2]
+  uint64_t* acc_empty = bars + 9;   // [2]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 11);
+  int* flag = reinterpret_cast<int*>(bars + 12);  // epilogue go/stop broadcast
 
   const SpinLayout& L = a.L;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int blk = blockIdx.x;
-  const int wb0 = blockIdx.y * a.wb_per_cta, wb1 = min(L.nwb, wb0 + a.wb_per_cta);
-  if (wb0 >= wb1) return;
+  const int t0 = blockIdx.y * a.tiles_per_cta, t1 = min(L.ntiles, t0 + a.tiles_per_cta);
+  if (t0 >= t1) return;
+  const int ntl = t1 - t0;
 
-  if (warp == 0) tc::tmem_alloc(tslot, 512);
-  if (tid == 0) {
-    tc::mbar_init(&mbar[0], 1);
-    tc::mbar_init(&mbar[1], 1);
+  if (warp == 8) tc::tmem_alloc(tslot, 512);
+  if (tid == 256) {
+    tc::mbar_init(a_full, 1);
+    for (int k = 0; k < kSlots; ++k) {
+      tc::mbar_init(&full[k], 1);
+      tc::mbar_init(&empty[k], 1);
+    }
+    for (int k = 0; k < 2; ++k) {
+      tc::mbar_init(&acc_full[k], 1);
+      tc::mbar_init(&acc_empty[k], 8);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  // resident A: four rot_chol slices of this tile
-  for (int c = tid; c < kSlices * 128 * (kKP / 8); c += 128) {
-    const int t = c / (128 * (kKP / 8)), rem = c % (128 * (kKP / 8)), r = rem / (kKP / 8), g = rem % (kKP / 8);
-    const uint4 v = *reinterpret_cast<const uint4*>(a.rot_q + (((size_t)t * L.nblk + blk) * 128 + r) * kKP + g * 8);
-    *reinterpret_cast<uint4*>(sA + (size_t)t * 128 * kKP * 2 + off128(r, g * 8)) = v;
-  }
-  eA[tid] = a.rot_e[(size_t)blk * 128 + tid];
-  tc::fence_proxy_async();
+  if (tid < 128) eA[tid] = a.rot_e[(size_t)blk * 128 + tid];
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = *tslot;
-  const uint32_t idesc = tc::idesc_bf16_f32(128, kBN);
-  const uint32_t sA_u = tc::smem_u32(sA), sB_u = tc::smem_u32(sB);
-  uint32_t phase[2] = {0u, 0u};
-  bool ok = true;
-  const size_t slice_stride = (size_t)a.W * L.S;  // rows per slice of the green operand
-  const int rows_valid_tile = min(L.gb, a.G - blk * L.gb) * L.n;
 
-  for (int wb = wb0; wb < wb1 && ok; ++wb) {
-    const int row0 = wb * L.WB * L.S;
-    const int nrows = min(L.WB * L.S, a.W * L.S - row0);
-    for (int u = 0; u < kSlices && ok; ++u) {
-      const int buf = u & 1;
-      if (u >= kGroups) break;
-      if (u >= 2) {
-        ok = tc::mbar_wait(&mbar[buf], phase[buf]);
-        phase[buf] ^= 1u;
+  if (warp == 8) {
+    // ------------------------------------------------ producer: loads + MMAs (one lane)
+    if (lane == 0) {
+      bool ok = true;
+      const uint32_t idesc = tc::idesc_bf16_f32(128, kBN);
+      const uint32_t sA_u = tc::smem_u32(sA), ring_u = tc::smem_u32(ring);
+      tc::mbar_expect_tx(a_full, kAImg);
+      tc::bulk_g2s(sA, a.rot_img + (size_t)blk * (kAImg / 2), kAImg, a_full);
+      const int total = ntl * kSlices;
+      int nl = 0;  // slices issued
+      for (int sidx = 0; sidx < total && ok; ++sidx) {
+        const int i = sidx / kSlices, u = sidx % kSlices;
+        // keep up to kSlots slice copies in flight ahead of the MMAs
+        while (nl < total && nl < sidx + kSlots && ok) {
+          const int slot = nl % kSlots;
+          if (nl >= kSlots) ok = tc::mbar_wait(&empty[slot], (uint32_t)((nl / kSlots - 1) & 1));
+          if (!ok) break;
+          const int ti = t0 + nl / kSlices, tu = nl % kSlices;
+          tc::mbar_expect_tx(&full[slot], kBImg);
+          tc::bulk_g2s(ring + (size_t)slot * kBImg, a.green_img + ((size_t)ti * kSlices + tu) * (kBImg / 2), kBImg,
+                       &full[slot]);
+          ++nl;
+        }
         if (!ok) break;
-      }
-      unsigned char* dstB = sB + (size_t)buf * kBN * kKP * 2;
-      for (int c = tid; c < kBN * (kKP / 8); c += 128) {
-        const int r = c / (kKP / 8), g = c % (kKP / 8);
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (r < nrows) v = *reinterpret_cast<const uint4*>(a.green_q + ((size_t)u * slice_stride + row0 + r) * kKP + g * 8);
-        *reinterpret_cast<uint4*>(dstB + off128(r, g * 8)) = v;
-      }
-      if (u == 0 && tid < kBN) eB[tid] = tid < nrows ? a.green_e[row0 + tid] : 0;
-      tc::fence_proxy_async();
-      tc::fence_before_sync();
-      __syncthreads();
-      tc::fence_after_sync();
-      if (tid == 0) {
+        const int abuf = i & 1;
+        if (u == 0) {
+          if (i == 0) ok = tc::mbar_wait(a_full, 0u);
+          if (ok && i >= 2) ok = tc::mbar_wait(&acc_empty[abuf], (uint32_t)(((i - 2) / 2) & 1));
+          if (!ok) break;
+        }
+        const int slot = sidx % kSlots;
+        ok = tc::mbar_wait(&full[slot], (uint32_t)((sidx / kSlots) & 1));
+        if (!ok) break;
+        tc::fence_after_sync();
         const int tmax = min(kSlices - 1, (kGroups - 1) - u);
         for (int t = 0; t <= tmax; ++t) {
           const int d = t + u;
-          const int first_u = d > kSlices - 1 ? d - (kSlices - 1) : 0;  // first slice u that feeds group d
 #pragma unroll
           for (int ks = 0; ks < kKP / 16; ++ks) {
             const uint64_t ad = tc::smem_desc(sA_u + (uint32_t)(t * 128 * kKP * 2 + ks * 256), 128, kKP * 16);
-            const uint64_t bd = tc::smem_desc(sB_u + (uint32_t)(buf * kBN * kKP * 2 + ks * 256), 128, kKP * 16);
-            tc::mma_bf16(taddr + (uint32_t)(d * kBN), ad, bd, idesc, (u == first_u && ks == 0) ? 0u : 1u);
+            const uint64_t bd = tc::smem_desc(ring_u + (uint32_t)(slot * kBImg + ks * 256), 128, kKP * 16);
+            tc::mma_bf16(taddr + (uint32_t)(abuf * kGroups * kBN + d * kBN), ad, bd, idesc,
+                         (u == 0 && ks == 0) ? 0u : 1u);
           }
         }
-        tc::mma_commit(&mbar[buf]);
+        tc::mma_commit(&empty[slot]);
+        if (u == kSlices - 1) tc::mma_commit(&acc_full[abuf]);
+      }
+      if (!ok) {
+        atomicExch(a.status, (int)TROT_ERR_DEVICE_TIMEOUT);
+        // let issued copies / MMAs drain (bounded) before the CTA frees its memory
+        for (int k = 0; k < kSlots; ++k) tc::mbar_wait(&empty[k], 0u, 1000000u);
       }
     }
-    if (!ok) break;
-    // all MMAs of this walker tile: the last commit on each buffer
-    for (int bb = 0; bb < 2 && ok; ++bb) {
-      ok = tc::mbar_wait(&mbar[bb], phase[bb]);
-      phase[bb] ^= 1u;
-    }
-    if (!ok) break;
-    tc::fence_after_sync();
-
-    // ---------------- epilogue: one walker of the tile at a time
-    const int r = tid;
-    const bool rvalid = r < rows_valid_tile;
+    __syncwarp();
+  } else {
+    // ------------------------------------------------ epilogue: 8 warps
+    const int q = warp & 3, h = warp >> 2;
+    const int r = q * 32 + lane;
     const int i = r % L.n, gl = r / L.n;
-    const uint32_t tlane = taddr + ((uint32_t)(warp * 32) << 16);
-    for (int bl = 0; bl < L.WB; ++bl) {
-      const int b = wb * L.WB + bl;
-      if (b >= a.W) break;
-      for (int c4 = 0; c4 < L.S / 4; ++c4) {
-        float v[kGroups][4];
+    const int jh = (L.n + 1) / 2, j0 = h * jh, j1 = min(L.n, j0 + jh), cnt = j1 - j0;
+    const int etid = tid;  // 0..255
+    for (int it = 0; it < ntl; ++it) {
+      const int tile = t0 + it, abuf = it & 1;
+      if (etid == 0) *flag = tc::mbar_wait(&acc_full[abuf], (uint32_t)((it / 2) & 1)) ? 1 : 0;
+      tc::named_bar(1, 256);
+      if (!*flag) {
+        if (etid == 0) atomicExch(a.status, (int)TROT_ERR_DEVICE_TIMEOUT);
+        break;
+      }
+      tc::fence_after_sync();
+      const int rows_valid = min(L.gb, a.G - blk * L.gb) * L.n;
+      const bool rvalid = r < rows_valid;
+      const uint32_t tlane = taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(abuf * kGroups * kBN);
+      const int32_t* eB = a.green_e + (size_t)tile * kBN;
+      for (int bl = 0; bl < L.WB; ++bl) {
+        const int b = tile * L.WB + bl;
+        if (b >= a.W) break;  // uniform across the epilogue warps
+        // f values for my row and my j-half: re (column bl*S + j), im (column bl*S + n_pad + j)
+        ff fre[(kMaxOcc + 1) / 2], fim[(kMaxOcc + 1) / 2];
+        {
+          uint32_t raw[2][kGroups][(kMaxOcc + 1) / 2];
 #pragma unroll
-        for (int d = 0; d < kGroups; ++d) tmem_ld4(tlane + (uint32_t)(d * kBN + bl * L.S + c4 * 4), v[d]);
+          for (int c = 0; c < 2; ++c)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int col = c4 * 4 + q;
-          ff x = ff_two_sum(v[0][q], v[1][q] * 0.00390625f);
-          float lo = x.lo + v[2][q] * 1.52587890625e-05f;
-          lo += v[3][q] * 5.9604644775390625e-08f;
-          lo += v[4][q] * 2.3283064365386963e-10f;
-          x = ff_fast(x.hi, lo);
-          const int e = eA[r] + eB[bl * L.S + col] - 16;
-          sF[r * 32 + col] = ff{ldexpf(x.hi, e), ldexpf(x.lo, e)};
+            for (int d = 0; d < kGroups; ++d)
+#pragma unroll
+              for (int jj = 0; jj < (kMaxOcc + 1) / 2; ++jj)
+                if (jj < cnt) raw[c][d][jj] = tc::tmem_ld1(tlane + (uint32_t)(d * kBN + bl * L.S + c * L.n_pad + j0 + jj));
+          tc::tmem_wait_ld();
+#pragma unroll
+          for (int c = 0; c < 2; ++c)
+#pragma unroll
+            for (int jj = 0; jj < (kMaxOcc + 1) / 2; ++jj) {
+              if (jj >= cnt) continue;
+              float g[kGroups];
+#pragma unroll
+              for (int d = 0; d < kGroups; ++d) {
+                uint32_t v = raw[c][d][jj];
+                asm volatile("" : "+r"(v));  // consume after tcgen05.wait::ld
+                g[d] = __uint_as_float(v);
+              }
+              ff x = ff_two_sum(g[0], g[1] * 0.00390625f);
+              float lo = x.lo + g[2] * 1.52587890625e-05f;
+              lo += g[3] * 5.9604644775390625e-08f;
+              lo += g[4] * 2.3283064365386963e-10f;
+              x = ff_fast(x.hi, lo);
+              const int e = eA[r] + eB[bl * L.S + c * L.n_pad + j0 + jj] - 16;
+              const ff y{ldexpf(x.hi, e), ldexpf(x.lo, e)};
+              if (c == 0) fre[jj] = y; else fim[jj] = y;
+            }
         }
-      }
-      __syncthreads();
-      ff xr{0.f, 0.f}, xi{0.f, 0.f};
-      if (rvalid) {
-        const int base_row = gl * L.n;
-        for (int j = 0; j < L.n; ++j) {
-          const ff ar = sF[r * 32 + j], ai = sF[r * 32 + L.n_pad + j];
-          const ff br = sF[(base_row + j) * 32 + i], bi = sF[(base_row + j) * 32 + L.n_pad + i];
-          xr = ff_add(xr, ff_sub(ff_mul(ar, br), ff_mul(ai, bi)));
-          xi = ff_add(xi, ff_add(ff_mul(ar, bi), ff_mul(ai, br)));
-        }
-        sC[2 * r] = sF[r * 32 + i];
-        sC[2 * r + 1] = sF[r * 32 + L.n_pad + i];
-      }
-      // exchange: sum over the tile's rows
-      for (int o = 16; o > 0; o >>= 1) {
-        xr = ff_add(xr, ff_shfl_xor(xr, o));
-        xi = ff_add(xi, ff_shfl_xor(xi, o));
-      }
-      if (lane == 0) {
-        sRed[2 * warp] = xr;
-        sRed[2 * warp + 1] = xi;
-      }
-      __syncthreads();
-      if (tid == 0) {
-        ff tr = sRed[0], ti = sRed[1];
-        for (int w = 1; w < 4; ++w) {
-          tr = ff_add(tr, sRed[2 * w]);
-          ti = ff_add(ti, sRed[2 * w + 1]);
-        }
-        a.xpart[(size_t)b * a.nblk_total + L.blk_off + blk] =
-            make_double2((double)a.mult * ff_d(tr), (double)a.mult * ff_d(ti));
-      }
-      // traces: c_g = sum_i f_gii for each Cholesky vector of the tile
-      if (tid < L.gb) {
-        const int g = blk * L.gb + tid;
-        if (g < a.G) {
-          ff tr{0.f, 0.f}, ti{0.f, 0.f};
-          for (int ii = 0; ii < L.n; ++ii) {
-            tr = ff_add(tr, sC[2 * (tid * L.n + ii)]);
-            ti = ff_add(ti, sC[2 * (tid * L.n + ii) + 1]);
+        // exchange: sum_j f_ij f_ji, re parts of f_ji first, then im parts
+        ff xr{0.f, 0.f}, xi{0.f, 0.f};
+        const int brow = gl * L.n;
+        for (int pass = 0; pass < 2; ++pass) {
+#pragma unroll
+          for (int jj = 0; jj < (kMaxOcc + 1) / 2; ++jj)
+            if (jj < cnt) sF[r * kMaxOcc + j0 + jj] = pass == 0 ? fre[jj] : fim[jj];
+          tc::named_bar(1, 256);
+          if (rvalid) {
+#pragma unroll
+            for (int jj = 0; jj < (kMaxOcc + 1) / 2; ++jj) {
+              if (jj >= cnt) continue;
+              const ff o = sF[(brow + j0 + jj) * kMaxOcc + i];  // re (pass 0) or im (pass 1) of f_ji
+              if (pass == 0) {  // (a + ib)(c + id): += a c, += b c (imag)
+                xr = ff_add(xr, ff_mul(fre[jj], o));
+                xi = ff_add(xi, ff_mul(fim[jj], o));
+              } else {          // -= b d, += a d (imag)
+                xr = ff_sub(xr, ff_mul(fim[jj], o));
+                xi = ff_add(xi, ff_mul(fre[jj], o));
+              }
+            }
           }
-          a.cs[(size_t)b * a.G + g] = make_double2(ff_d(tr), ff_d(ti));
+          tc::named_bar(1, 256);
         }
+        if (rvalid && i >= j0 && i < j1) {
+          sC[2 * r] = fre[i - j0];
+          sC[2 * r + 1] = fim[i - j0];
+        }
+        if (!rvalid) { xr = ff{0.f, 0.f}; xi = ff{0.f, 0.f}; }
+        for (int o = 16; o > 0; o >>= 1) {
+          xr = ff_add(xr, ff_shfl_xor(xr, o));
+          xi = ff_add(xi, ff_shfl_xor(xi, o));
+        }
+        if (lane == 0) {
+          sRed[2 * warp] = xr;
+          sRed[2 * warp + 1] = xi;
+        }
+        tc::named_bar(1, 256);
+        if (etid == 0) {
+          ff tr = sRed[0], ti = sRed[1];
+          for (int w = 1; w < 8; ++w) {
+            tr = ff_add(tr, sRed[2 * w]);
+            ti = ff_add(ti, sRed[2 * w + 1]);
+          }
+          a.xpart[(size_t)b * a.nblk_total + L.blk_off + blk] =
+              make_double2((double)a.mult * ff_d(tr), (double)a.mult * ff_d(ti));
+        }
+        if (etid < L.gb) {
+          const int g = blk * L.gb + etid;
+          if (g < a.G) {
+            ff tr{0.f, 0.f}, ti{0.f, 0.f};
+            for (int ii = 0; ii < L.n; ++ii) {
+              tr = ff_add(tr, sC[2 * (etid * L.n + ii)]);
+              ti = ff_add(ti, sC[2 * (etid * L.n + ii) + 1]);
+            }
+            a.cs[(size_t)b * a.G + g] = make_double2(ff_d(tr), ff_d(ti));
+          }
+        }
+        tc::named_bar(1, 256);
       }
-      __syncthreads();
+      // this accumulator buffer is free again
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&acc_empty[abuf]);
     }
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
   }
-  if (!ok && tid == 0) atomicExch(a.status, (int)TROT_ERR_DEVICE_TIMEOUT);
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(taddr, 512);
+  if (warp == 8) tc::tmem_dealloc(taddr, 512);
 }
 
 // fb = sum_s mult_s c_s   (complex, W x G)
@@ -405,9 +557,22 @@ __global__ void fb_combine_kernel(int n, int nspin, int m0, int m1, const double
 }
 
 // ------------------------------------------------------------------ VHS
-// Shifted fields as a 3-term bf16 split, rows (walker, re/im), K = G padded.
+// VHS rows (walker b, re/im) = sum over g of x_shifted[b][g] L_g, as
+// D = sum_{t + u <= 2} X_t . Lt_u^T with 3-term bf16 splits, FP32 accumulation.
+// Operands are stored as shared-memory images per K chunk of 64:
+//   X: [mtile][kchunk][slice][128][64]  (mtile = 128 rows (b, re/im))
+//   L: [ntile][kchunk][slice][128][64]  (ntile = 128 orbital pairs pq)
+// each 128 x 64 slice tile in core-matrix order (tc::tile_off).
+static constexpr int kVK = 64;
+static constexpr uint32_t kVSlice = 128 * kVK * 2;        // 16 KB
+static constexpr uint32_t kVStage = 6 * kVSlice;          // 3 X + 3 L slices: 96 KB
+static constexpr int kVThreads = 160;                     // 4 epilogue warps + 1 producer warp
+static constexpr size_t kVhsSmem = 2 * (size_t)kVStage + 16 * 8 + 1024;
+
+// Shifted fields -> 3-term bf16 split in the X image layout.
 __global__ void x_slices_kernel(int W, int G, int gpad, int mpad, const double2* __restrict__ xs,
                                 uint16_t* __restrict__ xq) {
+  const int nkc = gpad / kVK;
   const size_t total = (size_t)mpad * gpad;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
     const int row = (int)(e / gpad), g = (int)(e % gpad);
@@ -421,121 +586,201 @@ __global__ void x_slices_kernel(int W, int G, int gpad, int mpad, const double2*
     const float r1 = x - __bfloat162float(h);
     const __nv_bfloat16 m = __float2bfloat16_rn(r1);
     const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
-    xq[e] = *reinterpret_cast<const uint16_t*>(&h);
-    xq[total + e] = *reinterpret_cast<const uint16_t*>(&m);
-    xq[2 * total + e] = *reinterpret_cast<const uint16_t*>(&l);
+    const int mt = row >> 7, rr = row & 127, kc = g / kVK, kk = g % kVK;
+    const size_t base = (((size_t)mt * nkc + kc) * 3) * (kVSlice / 2) + tc::tile_off(rr, kk) / 2;
+    xq[base] = *reinterpret_cast<const uint16_t*>(&h);
+    xq[base + kVSlice / 2] = *reinterpret_cast<const uint16_t*>(&m);
+    xq[base + kVSlice] = *reinterpret_cast<const uint16_t*>(&l);
   }
 }
 
-// D (mpad x n2pad, f32) = sum_{t + u <= 2} X_t (mpad x gpad) . Lt_u (n2pad x gpad)^T
-// 128 x 128 tile per CTA, K in chunks of 64, operand chunks double-buffered.
-static constexpr int kVK = 64;
-static constexpr size_t kVhsStage = (size_t)3 * 128 * kVK * 2 * 2;  // X and L slices: 96 KB
-static constexpr size_t kVhsSmem = 2 * kVhsStage + 64 + 1024;
-
-__global__ void __launch_bounds__(128, 1)
-vhs_gemm_kernel(int mpad, int n2pad, int gpad, const uint16_t* __restrict__ xq, const uint16_t* __restrict__ lq,
-                float* __restrict__ D, int* status) {
+__global__ void __launch_bounds__(kVThreads, 1)
+vhs_gemm_kernel(int mtiles, int ntiles, int gpad, int n2pad, const uint16_t* __restrict__ xq,
+                const uint16_t* __restrict__ lq, float* __restrict__ D, int* status) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(base + 2 * kVhsStage);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 2);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + 2 * kVStage);
+  uint64_t* full = bars;           // [2] stages
+  uint64_t* empty = bars + 2;      // [2]
+  uint64_t* acc_full = bars + 4;   // [2]
+  uint64_t* acc_empty = bars + 6;  // [2]
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 8);
+  int* flag = reinterpret_cast<int*>(bars + 9);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int n0 = blockIdx.x * 128, m0 = blockIdx.y * 128;
-  if (warp == 0) tc::tmem_alloc(tslot, 128);
-  if (tid == 0) {
-    tc::mbar_init(&mbar[0], 1);
-    tc::mbar_init(&mbar[1], 1);
+  const int nkc = gpad / kVK;
+  // this CTA's tiles: linear index over (mtile, ntile), strided by the grid
+  const int ntot = mtiles * ntiles;
+  if (warp == 4) tc::tmem_alloc(tslot, 256);
+  if (tid == 128) {
+    for (int k = 0; k < 2; ++k) {
+      tc::mbar_init(&full[k], 1);
+      tc::mbar_init(&empty[k], 1);
+      tc::mbar_init(&acc_full[k], 1);
+      tc::mbar_init(&acc_empty[k], 4);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = *tslot;
-  const uint32_t idesc = tc::idesc_bf16_f32(128, 128);
-  const size_t xs_stride = (size_t)mpad * gpad, ls_stride = (size_t)n2pad * gpad;
-  const int nk = gpad / kVK;
-  uint32_t phase[2] = {0u, 0u};
-  int pending[2] = {0, 0};
-  bool ok = true;
-  for (int kt = 0; kt < nk && ok; ++kt) {
-    const int buf = kt & 1;
-    if (pending[buf]) {
-      ok = tc::mbar_wait(&mbar[buf], phase[buf]);
-      phase[buf] ^= 1u;
-      pending[buf] = 0;
-      if (!ok) break;
-    }
-    unsigned char* st = base + (size_t)buf * kVhsStage;
-    const int k0 = kt * kVK;
-    // 3 X slices then 3 L slices, each 128 rows x 64 k
-    for (int c = tid; c < 6 * 128 * 8; c += 128) {
-      const int which = c / (128 * 8), rem = c % (128 * 8), r = rem >> 3, g = rem & 7;
-      const uint16_t* src = which < 3 ? xq + which * xs_stride + (size_t)(m0 + r) * gpad
-                                      : lq + (which - 3) * ls_stride + (size_t)(n0 + r) * gpad;
-      *reinterpret_cast<uint4*>(st + (size_t)which * 128 * kVK * 2 + tc::tile_off(r, g * 8)) =
-          *reinterpret_cast<const uint4*>(src + k0 + g * 8);
-    }
-    tc::fence_proxy_async();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (tid == 0) {
-      const uint32_t su = tc::smem_u32(st);
-      bool first = kt == 0;
-      for (int t = 0; t < 3; ++t)
-        for (int u = 0; t + u <= 2; ++u) {
+  if (warp == 4) {
+    if (lane == 0) {
+      bool ok = true;
+      const uint32_t idesc = tc::idesc_bf16_f32(128, 128);
+      const uint32_t su = tc::smem_u32(base);
+      int chunk = 0;  // global K-chunk counter of this CTA (stage = chunk & 1)
+      int nt = 0;     // tiles of this CTA
+      for (int tl = blockIdx.x; tl < ntot && ok; tl += gridDim.x, ++nt) {
+        const int mt = tl / ntiles, ntl = tl % ntiles;
+        const int abuf = nt & 1;
+        if (nt >= 2) ok = tc::mbar_wait(&acc_empty[abuf], (uint32_t)(((nt - 2) / 2) & 1));
+        for (int kc = 0; kc < nkc && ok; ++kc, ++chunk) {
+          const int st = chunk & 1;
+          if (chunk >= 2) ok = tc::mbar_wait(&empty[st], (uint32_t)(((chunk - 2) / 2) & 1));
+          if (!ok) break;
+          unsigned char* dst = base + (size_t)st * kVStage;
+          tc::mbar_expect_tx(&full[st], kVStage);
+          tc::bulk_g2s(dst, xq + ((size_t)mt * nkc + kc) * 3 * (kVSlice / 2), 3 * kVSlice, &full[st]);
+          tc::bulk_g2s(dst + 3 * kVSlice, lq + ((size_t)ntl * nkc + kc) * 3 * (kVSlice / 2), 3 * kVSlice,
+                       &full[st]);
+          // MMAs of the previous chunk were issued already; now wait for this chunk's data
+          ok = tc::mbar_wait(&full[st], (uint32_t)((chunk / 2) & 1));
+          if (!ok) break;
+          tc::fence_after_sync();
+          const uint32_t s0 = su + (uint32_t)st * kVStage;
+          int first = kc == 0;
+          for (int t = 0; t < 3; ++t)
+            for (int u = 0; t + u <= 2; ++u) {
 #pragma unroll
-          for (int ks = 0; ks < kVK / 16; ++ks) {
-            const uint64_t ad = tc::smem_desc(su + (uint32_t)(t * 128 * kVK * 2 + ks * 256), 128, 1024);
-            const uint64_t bd = tc::smem_desc(su + (uint32_t)((3 + u) * 128 * kVK * 2 + ks * 256), 128, 1024);
-            tc::mma_bf16(taddr, ad, bd, idesc, first ? 0u : 1u);
-            first = false;
-          }
+              for (int ks = 0; ks < kVK / 16; ++ks) {
+                const uint64_t ad = tc::smem_desc(s0 + (uint32_t)(t * kVSlice + ks * 256), 128, 1024);
+                const uint64_t bd = tc::smem_desc(s0 + (uint32_t)((3 + u) * kVSlice + ks * 256), 128, 1024);
+                tc::mma_bf16(taddr + (uint32_t)(abuf * 128), ad, bd, idesc, first ? 0u : 1u);
+                first = 0;
+              }
+            }
+          tc::mma_commit(&empty[st]);
         }
-      tc::mma_commit(&mbar[buf]);
+        if (ok) tc::mma_commit(&acc_full[abuf]);
+      }
+      if (!ok) {
+        atomicExch(status, (int)TROT_ERR_DEVICE_TIMEOUT);
+        for (int k = 0; k < 2; ++k) tc::mbar_wait(&empty[k], 0u, 1000000u);
+      }
     }
-    pending[buf] = 1;
-  }
-  for (int bb = 0; bb < 2 && ok; ++bb)
-    if (pending[bb]) {
-      ok = tc::mbar_wait(&mbar[bb], phase[bb]);
-      phase[bb] ^= 1u;
+    __syncwarp();
+  } else {
+    // epilogue: warp q reads TMEM lanes 32q..32q+31 (rows of the tile)
+    int nt = 0;
+    for (int tl = blockIdx.x; tl < ntot; tl += gridDim.x, ++nt) {
+      const int mt = tl / ntiles, ntl = tl % ntiles;
+      const int abuf = nt & 1;
+      if (tid == 0) *flag = tc::mbar_wait(&acc_full[abuf], (uint32_t)((nt / 2) & 1)) ? 1 : 0;
+      tc::named_bar(1, 128);
+      if (!*flag) {
+        if (tid == 0) atomicExch(status, (int)TROT_ERR_DEVICE_TIMEOUT);
+        break;
+      }
+      tc::fence_after_sync();
+      const uint32_t trow = taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(abuf * 128);
+      float* drow = D + (size_t)(mt * 128 + warp * 32 + lane) * n2pad + (size_t)ntl * 128;
+      for (int c = 0; c < 8; ++c) {
+        float v[16];
+        tc::tmem_ld16(trow + c * 16, v);
+        float4* d4 = reinterpret_cast<float4*>(drow + c * 16);
+        d4[0] = make_float4(v[0], v[1], v[2], v[3]);
+        d4[1] = make_float4(v[4], v[5], v[6], v[7]);
+        d4[2] = make_float4(v[8], v[9], v[10], v[11]);
+        d4[3] = make_float4(v[12], v[13], v[14], v[15]);
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&acc_empty[abuf]);
+      tc::named_bar(1, 128);  // flag reuse
     }
-  if (ok) {
-    tc::fence_after_sync();
-    const uint32_t trow = taddr + ((uint32_t)(warp * 32) << 16);
-    float v[16];
-    for (int c = 0; c < 8; ++c) {
-      tc::tmem_ld16(trow + c * 16, v);
-      float4* d = reinterpret_cast<float4*>(D + (size_t)(m0 + warp * 32 + lane) * n2pad + n0 + c * 16);
-      d[0] = make_float4(v[0], v[1], v[2], v[3]);
-      d[1] = make_float4(v[4], v[5], v[6], v[7]);
-      d[2] = make_float4(v[8], v[9], v[10], v[11]);
-      d[3] = make_float4(v[12], v[13], v[14], v[15]);
-    }
-  } else if (tid == 0) {
-    atomicExch(status, (int)TROT_ERR_DEVICE_TIMEOUT);
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(taddr, 128);
+  if (warp == 4) tc::tmem_dealloc(taddr, 256);
 }
 
 // ------------------------------------------------------------------ FP32 Trotter propagation
 // Same algorithm as the FP64 trotter_kernel with float2 arithmetic: the walker's
 // VHS (complex N x N, from rows (2b, 2b+1) of D) is staged in shared memory.
+// Register-tiled products for the FP32 propagation: each thread owns a block
+// of RP rows x RJ columns of the N x nc output.
+static constexpr int kRP = 4, kRJ = 2;
+
+// out = E in   (E real N x N in global memory, in / out N x nc in shared memory)
 __device__ void real_mm32(int N, int nc, const float* __restrict__ E, const float2* in, float2* out) {
-  for (int e = threadIdx.x; e < N * nc; e += blockDim.x) {
-    const int p = e / nc, j = e % nc;
-    const float* Er = E + (size_t)p * N;
-    float2 acc = make_float2(0.f, 0.f);
+  const int pt = (N + kRP - 1) / kRP, jt = (nc + kRJ - 1) / kRJ;
+  for (int tt = threadIdx.x; tt < pt * jt; tt += blockDim.x) {
+    const int p0 = (tt / jt) * kRP, j0 = (tt % jt) * kRJ;
+    float2 acc[kRP][kRJ];
+#pragma unroll
+    for (int a = 0; a < kRP; ++a)
+#pragma unroll
+      for (int c = 0; c < kRJ; ++c) acc[a][c] = make_float2(0.f, 0.f);
     for (int q = 0; q < N; ++q) {
-      const float w = Er[q];
-      const float2 x = in[q * nc + j];
-      acc.x = fmaf(w, x.x, acc.x);
-      acc.y = fmaf(w, x.y, acc.y);
+      float e[kRP];
+      float2 x[kRJ];
+#pragma unroll
+      for (int a = 0; a < kRP; ++a) e[a] = p0 + a < N ? __ldg(E + (size_t)(p0 + a) * N + q) : 0.f;
+#pragma unroll
+      for (int c = 0; c < kRJ; ++c) x[c] = j0 + c < nc ? in[q * nc + j0 + c] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int a = 0; a < kRP; ++a)
+#pragma unroll
+        for (int c = 0; c < kRJ; ++c) {
+          acc[a][c].x = fmaf(e[a], x[c].x, acc[a][c].x);
+          acc[a][c].y = fmaf(e[a], x[c].y, acc[a][c].y);
+        }
     }
-    out[e] = acc;
+#pragma unroll
+    for (int a = 0; a < kRP; ++a)
+#pragma unroll
+      for (int c = 0; c < kRJ; ++c)
+        if (p0 + a < N && j0 + c < nc) out[(p0 + a) * nc + j0 + c] = acc[a][c];
+  }
+}
+
+// T2 = (i coef) V T ; O += T2   (V complex N x N, T / T2 / O N x nc, all in shared memory)
+__device__ void taylor_term32(int N, int nc, const float2* V, const float2* T, float coef, float2* T2, float2* O) {
+  const int pt = (N + kRP - 1) / kRP, jt = (nc + kRJ - 1) / kRJ;
+  for (int tt = threadIdx.x; tt < pt * jt; tt += blockDim.x) {
+    const int p0 = (tt / jt) * kRP, j0 = (tt % jt) * kRJ;
+    float2 acc[kRP][kRJ];
+#pragma unroll
+    for (int a = 0; a < kRP; ++a)
+#pragma unroll
+      for (int c = 0; c < kRJ; ++c) acc[a][c] = make_float2(0.f, 0.f);
+    for (int q = 0; q < N; ++q) {
+      float2 v[kRP], x[kRJ];
+#pragma unroll
+      for (int a = 0; a < kRP; ++a) v[a] = p0 + a < N ? V[(p0 + a) * N + q] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int c = 0; c < kRJ; ++c) x[c] = j0 + c < nc ? T[q * nc + j0 + c] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int a = 0; a < kRP; ++a)
+#pragma unroll
+        for (int c = 0; c < kRJ; ++c) {
+          acc[a][c].x = fmaf(v[a].x, x[c].x, acc[a][c].x);
+          acc[a][c].x = fmaf(-v[a].y, x[c].y, acc[a][c].x);
+          acc[a][c].y = fmaf(v[a].x, x[c].y, acc[a][c].y);
+          acc[a][c].y = fmaf(v[a].y, x[c].x, acc[a][c].y);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < kRP; ++a)
+#pragma unroll
+      for (int c = 0; c < kRJ; ++c)
+        if (p0 + a < N && j0 + c < nc) {
+          const int e = (p0 + a) * nc + j0 + c;
+          const float2 t = make_float2(-coef * acc[a][c].y, coef * acc[a][c].x);
+          T2[e] = t;
+          O[e] = make_float2(O[e].x + t.x, O[e].y + t.y);
+        }
   }
 }
 
@@ -578,22 +823,7 @@ __global__ void __launch_bounds__(256) trotter32_kernel(Spins sp, Trot32Args a32
   for (int e = tid; e < N * nc; e += nt) T[e] = O[e];
   __syncthreads();
   for (int k = 1; k <= a.nterms; ++k) {
-    const float c = (float)(a.sqrt_dt / (double)k);
-    for (int e = tid; e < N * nc; e += nt) {
-      const int p = e / nc, j = e % nc;
-      const float2* Vr = V + (size_t)p * N;
-      float2 acc = make_float2(0.f, 0.f);
-      for (int q = 0; q < N; ++q) {
-        const float2 v = Vr[q], x = T[q * nc + j];
-        acc.x = fmaf(v.x, x.x, acc.x);
-        acc.x = fmaf(-v.y, x.y, acc.x);
-        acc.y = fmaf(v.x, x.y, acc.y);
-        acc.y = fmaf(v.y, x.x, acc.y);
-      }
-      const float2 t = make_float2(-c * acc.y, c * acc.x);
-      T2[e] = t;
-      O[e] = make_float2(O[e].x + t.x, O[e].y + t.y);
-    }
+    taylor_term32(N, nc, V, T, (float)(a.sqrt_dt / (double)k), T2, O);
     __syncthreads();
     float2* tmp = T; T = T2; T2 = tmp;
   }
@@ -622,7 +852,7 @@ static int check_mixed_shapes(const trot_system* s, const Spins& sp) {
   if (!s->mixed) { set_error("mixed precision needs a trot_mixed context"); return TROT_ERR_NULL_PTR; }
   if (s->norb > kKP) { set_error("mixed path: norb %d > %d", s->norb, kKP); return TROT_ERR_UNSUPPORTED; }
   for (int q = 0; q < sp.nspin; ++q)
-    if (2 * (sp.n[q] + (sp.n[q] & 1)) > 32) { set_error("mixed path: nocc %d > 16", sp.n[q]); return TROT_ERR_UNSUPPORTED; }
+    if (sp.n[q] > kMaxOcc) { set_error("mixed path: nocc %d > %d", sp.n[q], kMaxOcc); return TROT_ERR_UNSUPPORTED; }
   if (s->mixed->kpad != kKP || s->mixed->slices != kSlices || s->mixed->max_order != kGroups - 1) {
     set_error("mixed context layout mismatch");
     return TROT_ERR_BAD_SHAPE;
@@ -635,7 +865,8 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
   for (int q = 0; q < sp.nspin; ++q) {
     SpinLayout L = spin_layout(s, sp, q);
     TROT_TIMED("green_slices", st, ([&]() -> int {
-      green_slices_kernel<<<W, 256, 0, st>>>(N, L.n, L.n_pad, W, sp.ntot, sp.off[q], m.green, m.gq[q], m.ge[q]);
+      green_slices_kernel<<<L.ntiles, 256, 0, st>>>(N, L.n, L.n_pad, L.WB, W, sp.ntot, sp.off[q], m.green, m.gq[q],
+                                                    m.ge[q]);
       TROT_CHECK_LAUNCH("green_slices_kernel");
       return TROT_OK;
     })());
@@ -651,15 +882,14 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
     ExArgs a{};
     a.L = L;
     a.G = G; a.W = W; a.mult = sp.mult[q];
-    // walker tiles per CTA: enough CTAs to fill the GPU a few times over
-    const int target = 152 * 4;
-    int chunks = (target + L.nblk - 1) / L.nblk;
-    if (chunks > L.nwb) chunks = L.nwb;
-    a.wb_per_cta = (L.nwb + chunks - 1) / chunks;
-    chunks = (L.nwb + a.wb_per_cta - 1) / a.wb_per_cta;
-    a.rot_q = s->mixed->rot_slices[mq];
+    // about two CTAs' worth of walker tiles per SM, one CTA per SM at a time
+    int chunks = (2 * 152 + L.nblk - 1) / L.nblk;
+    if (chunks > L.ntiles) chunks = L.ntiles;
+    a.tiles_per_cta = (L.ntiles + chunks - 1) / chunks;
+    chunks = (L.ntiles + a.tiles_per_cta - 1) / a.tiles_per_cta;
+    a.rot_img = s->mixed->rot_slices[mq];
     a.rot_e = s->mixed->rot_exp[mq];
-    a.green_q = m.gq[q];
+    a.green_img = m.gq[q];
     a.green_e = m.ge[q];
     a.cs = m.cs[q];
     a.xpart = m.xpart;
@@ -667,7 +897,7 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
     a.status = m.status;
     dim3 grid(L.nblk, chunks);
     TROT_TIMED("exchange_exact_tc", st, ([&]() -> int {
-      exchange_exact_kernel<<<grid, 128, kExSmem + 1024, st>>>(a);
+      exchange_exact_kernel<<<grid, kExThreads, kExSmem + 1024, st>>>(a);
       TROT_CHECK_LAUNCH("exchange_exact_kernel");
       return TROT_OK;
     })());
@@ -682,6 +912,10 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
 static int run_vhs(const trot_system* s, MixedBuffers& m, const double2* xs, cudaStream_t st) {
   const int W = s->n_walkers, G = s->nchol;
   const trot_mixed* mx = s->mixed;
+  if (mx->vhs_slices != 3 || mx->vhs_order != 2 || mx->gpad % kVK || mx->n2pad % 128) {
+    set_error("mixed context: VHS operand layout mismatch");
+    return TROT_ERR_BAD_SHAPE;
+  }
   TROT_TIMED("x_slices", st, ([&]() -> int {
     x_slices_kernel<<<152 * 8, 256, 0, st>>>(W, G, mx->gpad, m.mpad, xs, m.xq);
     TROT_CHECK_LAUNCH("x_slices_kernel");
@@ -692,10 +926,12 @@ static int run_vhs(const trot_system* s, MixedBuffers& m, const double2* xs, cud
     cudaFuncSetAttribute(vhs_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kVhsSmem);
     attr_set = true;
   }
-  dim3 grid(mx->n2pad / 128, m.mpad / 128);
+  const int mtiles = m.mpad / 128, ntiles = mx->n2pad / 128;
+  int grid = mtiles * ntiles;
+  if (grid > 152) grid = 152;
   TROT_TIMED("vhs_tc", st, ([&]() -> int {
-    vhs_gemm_kernel<<<grid, 128, kVhsSmem, st>>>(m.mpad, mx->n2pad, mx->gpad, m.xq, mx->chol_t_slices, m.vhs,
-                                                m.status);
+    vhs_gemm_kernel<<<grid, kVThreads, kVhsSmem, st>>>(mtiles, ntiles, mx->gpad, mx->n2pad, m.xq,
+                                                       mx->chol_t_slices, m.vhs, m.status);
     TROT_CHECK_LAUNCH("vhs_gemm_kernel");
     return TROT_OK;
   })());
@@ -742,7 +978,7 @@ int mixed_force_bias(const trot_system* s, const Spins& sp, const double2* wa, c
   Carver c(ws, ws_bytes);
   MixedBuffers m;
   TROT_TRY(begin(s, sp, c, m, TROT_OP_FORCE_BIAS, st));
-  TROT_TRY(launch_green(sp, s->n_walkers, s->norb, wa, wb, m.green, nullptr, nullptr, st));
+  TROT_TRY(launch_green_ff(sp, s->n_walkers, s->norb, wa, wb, m.green, nullptr, st));
   TROT_TRY(run_slices_and_exchange(s, sp, m, st));
   cudaMemcpyAsync(fb_out, m.fb, (size_t)s->n_walkers * s->nchol * sizeof(double2), cudaMemcpyDeviceToDevice, st);
   TROT_CHECK_LAUNCH("cudaMemcpyAsync");
@@ -754,7 +990,7 @@ int mixed_local_energy(const trot_system* s, const Spins& sp, const double2* wa,
   Carver c(ws, ws_bytes);
   MixedBuffers m;
   TROT_TRY(begin(s, sp, c, m, TROT_OP_LOCAL_ENERGY, st));
-  TROT_TRY(launch_green(sp, s->n_walkers, s->norb, wa, wb, m.green, nullptr, m.e1, st));
+  TROT_TRY(launch_green_ff(sp, s->n_walkers, s->norb, wa, wb, m.green, m.e1, st));
   TROT_TRY(run_slices_and_exchange(s, sp, m, st));
   return launch_energy_combine(s->n_walkers, s->nchol, m.nblk_total, s->h0, m.fb, m.e1, m.xpart, energy, st);
 }
@@ -780,7 +1016,7 @@ int mixed_prop_step(const trot_system* s, const Spins& sp, const trot_state* sta
   TROT_TRY(begin(s, sp, c, m, TROT_OP_PROP_STEP, st));
   double2* wa = (double2*)state->walkers_a;
   double2* wb = (double2*)state->walkers_b;
-  TROT_TIMED("green", st, launch_green(sp, W, N, wa, wb, m.green, nullptr, energy_out ? m.e1 : nullptr, st));
+  TROT_TIMED("green_ff", st, launch_green_ff(sp, W, N, wa, wb, m.green, energy_out ? m.e1 : nullptr, st));
   TROT_TRY(run_slices_and_exchange(s, sp, m, st));
   if (energy_out)
     TROT_TIMED("energy_combine", st,

@@ -7,7 +7,8 @@ Built once per (trial, Hamiltonian, dt) on the host and kept on the device:
   sum_t 2^(e - 8(t+1)) q_t (t < 5) with integer slices |q_t| <= 255 and one
   exponent per row, laid out as 128-row tiles of whole Cholesky vectors;
 * a 3-term BF16 split (hi + mid + lo) of the Cholesky vectors, transposed to
-  (N*N, G), for the VHS build;
+  (N*N, G) and stored as the VHS kernel's shared-memory image (128 x 64
+  tiles in core-matrix order);
 * exp(-dt/2 h1_eff) in FP32 for the one-body half steps.
 
 ``context(meas_ctx, prop_ctx, kind)`` returns the cached ``MixedCtx`` whose
@@ -64,10 +65,12 @@ def gammas_per_block(n: int) -> int:
 
 
 def rot_tiles(rot_chol: np.ndarray):
-    """(G, n, N) -> bf16 slices (SLICES, nblk, 128, KPAD) and exponents (nblk, 128)."""
+    """(G, n, N) -> bf16 slices in the kernel's shared-memory image layout
+    (nblk, SLICES, 128, KPAD) (each 128 x KPAD tile in 8 x 8 core-matrix order,
+    K fastest) and row exponents (nblk, 128)."""
     G, n, N = rot_chol.shape
-    if n > 64 or N > KPAD:
-        raise NotImplementedError(f"mixed path: n={n}, N={N} outside the tensor-core tile limits (n<=64, N<={KPAD})")
+    if n > 16 or N > KPAD:
+        raise NotImplementedError(f"mixed path: n={n}, N={N} outside the tensor-core tile limits (n<=16, N<={KPAD})")
     gb = gammas_per_block(n)
     nblk = (G + gb - 1) // gb
     rows = np.zeros((nblk, 128, KPAD), dtype=np.float64)
@@ -75,8 +78,11 @@ def rot_tiles(rot_chol: np.ndarray):
         g0, g1 = blk * gb, min(G, (blk + 1) * gb)
         r = rot_chol[g0:g1].reshape(-1, N)
         rows[blk, : r.shape[0], :N] = r
-    q, e = exact_slices(rows)
-    return torch.from_numpy(q).to(torch.bfloat16), torch.from_numpy(e.astype(np.int32)), gb, nblk
+    q, e = exact_slices(rows)  # (SLICES, nblk, 128, KPAD)
+    # shared-memory image of the exchange kernel's A operand: [nblk][slice][core-matrix order]
+    img = q.transpose(1, 0, 2, 3).reshape(nblk, SLICES, 16, 8, KPAD // 8, 8).transpose(0, 1, 2, 4, 3, 5)
+    img = np.ascontiguousarray(img).reshape(nblk, SLICES, 128, KPAD)
+    return torch.from_numpy(img).to(torch.bfloat16), torch.from_numpy(e.astype(np.int32)), gb, nblk
 
 
 class MixedCtx:
@@ -103,7 +109,11 @@ class MixedCtx:
         gpad = (G + 63) // 64 * 64
         lt = np.zeros((n2pad, gpad), dtype=np.float64)
         lt[:N2, :G] = chol_flat.T
-        sl = torch.stack(plain_split(lt)).to(dev).contiguous()
+        sl = torch.stack(plain_split(lt))  # (3, n2pad, gpad)
+        # shared-memory image: [ntile][kchunk][slice][128 rows][64] in core-matrix order
+        nt, nk = n2pad // 128, gpad // 64
+        sl = sl.reshape(3, nt, 16, 8, nk, 8, 8).permute(1, 4, 0, 2, 5, 3, 6).contiguous()
+        sl = sl.reshape(nt, nk, 3, 128, 64).to(dev).contiguous()
         self._keep.append(sl)
         s.vhs_slices, s.vhs_order, s.n2pad, s.gpad = VHS_SLICES, VHS_ORDER, n2pad, gpad
         s.chol_t_slices = sl.data_ptr()

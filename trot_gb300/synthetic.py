@@ -80,6 +80,57 @@ def scf(h1, chol, na: int, nb: int, iters: int = 30):
     return np.ascontiguousarray(ca), np.ascontiguousarray(cb)
 
 
+def scf_rhf_full(h1, chol, n: int, iters: int = 30):
+    """RHF SCF as ``scf`` with na == nb == n; returns all MOs (N, N) and orbital
+    energies of the final Fock matrix."""
+    _, c = np.linalg.eigh(h1)
+    co = c[:, :n]
+    for _ in range(iters):
+        d = co @ co.T
+        f = h1 + 2.0 * _coulomb(chol, d) - _exchange(chol, d)
+        eps, c = np.linalg.eigh(f)
+        co = c[:, :n]
+    return np.ascontiguousarray(c), eps
+
+
+@dataclass(frozen=True)
+class CisdSystem:
+    """Hamiltonian in the RHF MO basis (reference determinant = first nocc MOs)
+    plus CISD amplitudes in trot's (i, a, j, b) layout."""
+
+    h0: float
+    h1: np.ndarray  # (N, N) MO basis
+    chol: np.ndarray  # (G, N, N) MO basis
+    ci1: np.ndarray  # (n, v)
+    ci2: np.ndarray  # (n, v, n, v), symmetric under (i, a) <-> (j, b)
+
+    @property
+    def nocc(self) -> int:
+        return self.ci1.shape[0]
+
+
+def make_cisd_system(norb, nocc, nchol, decay=30.0, seed=0, h0=0.0, c1_sigma=0.02, c2_norm=0.2, scf_iters=30):
+    """CISD recipe: c1 ~ N(0, c1_sigma); c2_ijab = N(0, 1) / (e_a + e_b - e_i - e_j)
+    with e the RHF orbital energies, mapped to ci2[i, a, j, b] = c2_ijab,
+    symmetrised under (i, a) <-> (j, b) (the spatial-orbital convention of
+    trot/trial/cisd.py) and scaled to ||ci2|| = c2_norm."""
+    h0, h1, chol = hamiltonian(norb, nchol, decay, seed, h0)
+    c, eps = scf_rhf_full(h1, chol, nocc, scf_iters)
+    h1_mo = c.T @ h1 @ c
+    chol_mo = np.einsum("pi,gpq,qj->gij", c, chol, c, optimize=True)
+    nv = norb - nocc
+    rng = np.random.default_rng(seed + 17)
+    ci1 = rng.normal(0.0, c1_sigma, (nocc, nv))
+    eo, ev = eps[:nocc], eps[nocc:]
+    denom = ev[None, None, :, None] + ev[None, None, None, :] - eo[:, None, None, None] - eo[None, :, None, None]
+    c2 = rng.normal(size=(nocc, nocc, nv, nv)) / denom
+    ci2 = c2.transpose(0, 2, 1, 3)
+    ci2 = 0.5 * (ci2 + ci2.transpose(2, 3, 0, 1))
+    ci2 *= c2_norm / np.linalg.norm(ci2)
+    return CisdSystem(h0=float(h0), h1=np.ascontiguousarray(h1_mo), chol=np.ascontiguousarray(chol_mo),
+                      ci1=np.ascontiguousarray(ci1), ci2=np.ascontiguousarray(ci2))
+
+
 def make_system(norb, nelec, nchol, decay=30.0, seed=0, h0=0.0, scf_iters=30) -> SyntheticSystem:
     h0, h1, chol = hamiltonian(norb, nchol, decay, seed, h0)
     ca, cb = scf(h1, chol, nelec[0], nelec[1], scf_iters)
@@ -109,6 +160,8 @@ CONFIGS = {
     # the cfg2 system with fewer walkers: small case for profiler captures
     "cfg2_uhf_n120_w256": dict(norb=120, nelec=(12, 10), nchol=600, decay=150.0, n_walkers=256,
                                dt=0.005, n_steps=200, qr_every=10, kind="uhf_u"),
+    "cfg4_cisd_n60": dict(norb=60, nelec=(8, 8), nchol=300, decay=30.0, n_walkers=256,
+                          dt=0.005, n_steps=100, qr_every=10, kind="cisd"),
     "cfg3_rhf_n80": dict(norb=80, nelec=(10, 10), nchol=400, decay=30.0, n_walkers=512,
                          dt=0.01, n_steps=200, qr_every=20, kind="rhf_r"),
 }
