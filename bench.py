@@ -239,6 +239,9 @@ def main():
     ap.add_argument("--config", default="cfg2_uhf_n120")
     ap.add_argument("--cpu-sample", type=int, default=0, help="walkers in the CPU baseline sample (0 = auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-run", action="store_true",
+                    help="timed steps only (no e2e, FP64 comparison, precision check or CPU baseline): "
+                         "for profiler launch lists")
     args = ap.parse_args()
 
     from trot_gb300 import synthetic
@@ -317,6 +320,11 @@ def main():
         ms = float(t.item())
     value = W * args.steps * world / (ms / 1e3)
 
+    if args.profile_run:
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "ms_per_step": ms / args.steps,
+                              "kernels": {k: v for k, v in prof.items()}}), flush=True)
+        return
     # end to end through the public API: host fields in, energies out, every step
     k_e2e = max(4, args.steps // 2)
     fields_host = torch.from_numpy(synthetic.fields(W, G, 4, seed=77)).pin_memory()

@@ -38,6 +38,8 @@ TROT_D ff ff_mul(ff x, ff y) {
   return ff_fast(p, e);
 }
 TROT_D double ff_d(ff x) { return (double)x.hi + (double)x.lo; }
+// 2^e as a float for e in [-126, 127] (exact; the exponents here stay far inside)
+TROT_D float pow2f(int e) { return __int_as_float((e + 127) << 23); }
 TROT_D ff ff_shfl_xor(ff x, int o) {
   return ff{__shfl_xor_sync(0xffffffffu, x.hi, o), __shfl_xor_sync(0xffffffffu, x.lo, o)};
 }
@@ -319,6 +321,9 @@ static constexpr size_t kExOffRed = kExOffC + 128 * 2 * sizeof(ff);            /
 static constexpr size_t kExOffBar = kExOffRed + 8 * 2 * sizeof(ff);            // 11 mbarriers + flags
 static constexpr size_t kExSmem = kExOffBar + 16 * 8 + 64;
 
+// JH = n_pad / 2 columns j per epilogue warp (static so the per-row values stay
+// in registers); columns j >= n are exactly zero and contribute nothing.
+template <int JH>
 __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
@@ -423,7 +428,7 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
     const int q = warp & 3, h = warp >> 2;
     const int r = q * 32 + lane;
     const int i = r % L.n, gl = r / L.n;
-    const int jh = (L.n + 1) / 2, j0 = h * jh, j1 = min(L.n, j0 + jh), cnt = j1 - j0;
+    const int j0 = h * JH;
     const int etid = tid;  // 0..255
     for (int it = 0; it < ntl; ++it) {
       const int tile = t0 + it, abuf = it & 1;
@@ -438,26 +443,26 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
       const bool rvalid = r < rows_valid;
       const uint32_t tlane = taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(abuf * kGroups * kBN);
       const int32_t* eB = a.green_e + (size_t)tile * kBN;
+      const int ea = eA[r];
       for (int bl = 0; bl < L.WB; ++bl) {
         const int b = tile * L.WB + bl;
         if (b >= a.W) break;  // uniform across the epilogue warps
         // f values for my row and my j-half: re (column bl*S + j), im (column bl*S + n_pad + j)
-        ff fre[(kMaxOcc + 1) / 2], fim[(kMaxOcc + 1) / 2];
+        ff fre[JH], fim[JH];
         {
-          uint32_t raw[2][kGroups][(kMaxOcc + 1) / 2];
+          uint32_t raw[2][kGroups][JH];
 #pragma unroll
           for (int c = 0; c < 2; ++c)
 #pragma unroll
             for (int d = 0; d < kGroups; ++d)
 #pragma unroll
-              for (int jj = 0; jj < (kMaxOcc + 1) / 2; ++jj)
-                if (jj < cnt) raw[c][d][jj] = tc::tmem_ld1(tlane + (uint32_t)(d * kBN + bl * L.S + c * L.n_pad + j0 + jj));
+              for (int jj = 0; jj < JH; ++jj)
+                raw[c][d][jj] = tc::tmem_ld1(tlane + (uint32_t)(d * kBN + bl * L.S + c * L.n_pad + j0 + jj));
           tc::tmem_wait_ld();
 #pragma unroll
           for (int c = 0; c < 2; ++c)
 #pragma unroll
-            for (int jj = 0; jj < (kMaxOcc + 1) / 2; ++jj) {
-              if (jj >= cnt) continue;
+            for (int jj = 0; jj < JH; ++jj) {
               float g[kGroups];
 #pragma unroll
               for (int d = 0; d < kGroups; ++d) {
@@ -470,23 +475,26 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
               lo += g[3] * 5.9604644775390625e-08f;
               lo += g[4] * 2.3283064365386963e-10f;
               x = ff_fast(x.hi, lo);
-              const int e = eA[r] + eB[bl * L.S + c * L.n_pad + j0 + jj] - 16;
-              const ff y{ldexpf(x.hi, e), ldexpf(x.lo, e)};
+              const float sc = pow2f(ea + eB[bl * L.S + c * L.n_pad + j0 + jj] - 16);
+              const ff y{x.hi * sc, x.lo * sc};
               if (c == 0) fre[jj] = y; else fim[jj] = y;
             }
         }
         // exchange: sum_j f_ij f_ji, re parts of f_ji first, then im parts
         ff xr{0.f, 0.f}, xi{0.f, 0.f};
+        ff trv{0.f, 0.f}, tiv{0.f, 0.f};  // f_ii (re, im) of this row, read back from the full row in sF
         const int brow = gl * L.n;
+#pragma unroll
         for (int pass = 0; pass < 2; ++pass) {
 #pragma unroll
-          for (int jj = 0; jj < (kMaxOcc + 1) / 2; ++jj)
-            if (jj < cnt) sF[r * kMaxOcc + j0 + jj] = pass == 0 ? fre[jj] : fim[jj];
+          for (int jj = 0; jj < JH; ++jj) sF[r * kMaxOcc + j0 + jj] = pass == 0 ? fre[jj] : fim[jj];
           tc::named_bar(1, 256);
+          if (rvalid && h == 0) {
+            if (pass == 0) trv = sF[r * kMaxOcc + i]; else tiv = sF[r * kMaxOcc + i];
+          }
           if (rvalid) {
 #pragma unroll
-            for (int jj = 0; jj < (kMaxOcc + 1) / 2; ++jj) {
-              if (jj >= cnt) continue;
+            for (int jj = 0; jj < JH; ++jj) {
               const ff o = sF[(brow + j0 + jj) * kMaxOcc + i];  // re (pass 0) or im (pass 1) of f_ji
               if (pass == 0) {  // (a + ib)(c + id): += a c, += b c (imag)
                 xr = ff_add(xr, ff_mul(fre[jj], o));
@@ -499,9 +507,9 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
           }
           tc::named_bar(1, 256);
         }
-        if (rvalid && i >= j0 && i < j1) {
-          sC[2 * r] = fre[i - j0];
-          sC[2 * r + 1] = fim[i - j0];
+        if (rvalid && h == 0) {
+          sC[2 * r] = trv;
+          sC[2 * r + 1] = tiv;
         }
         if (!rvalid) { xr = ff{0.f, 0.f}; xi = ff{0.f, 0.f}; }
         for (int o = 16; o > 0; o >>= 1) {
@@ -860,6 +868,32 @@ static int check_mixed_shapes(const trot_system* s, const Spins& sp) {
   return TROT_OK;
 }
 
+template <int JH>
+static void exchange_exact_launch(dim3 grid, const ExArgs& a, cudaStream_t st) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(exchange_exact_kernel<JH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kExSmem + 1024);
+    attr_set = true;
+  }
+  exchange_exact_kernel<JH><<<grid, kExThreads, kExSmem + 1024, st>>>(a);
+}
+
+static int launch_exchange_exact(int jh, dim3 grid, const ExArgs& a, cudaStream_t st) {
+  switch (jh) {
+    case 1: exchange_exact_launch<1>(grid, a, st); break;
+    case 2: exchange_exact_launch<2>(grid, a, st); break;
+    case 3: exchange_exact_launch<3>(grid, a, st); break;
+    case 4: exchange_exact_launch<4>(grid, a, st); break;
+    case 5: exchange_exact_launch<5>(grid, a, st); break;
+    case 6: exchange_exact_launch<6>(grid, a, st); break;
+    case 7: exchange_exact_launch<7>(grid, a, st); break;
+    case 8: exchange_exact_launch<8>(grid, a, st); break;
+    default: set_error("exchange: n_pad/2 = %d unsupported", jh); return TROT_ERR_UNSUPPORTED;
+  }
+  TROT_CHECK_LAUNCH("exchange_exact_kernel");
+  return TROT_OK;
+}
+
 static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedBuffers& m, cudaStream_t st) {
   const int W = s->n_walkers, N = s->norb, G = s->nchol;
   for (int q = 0; q < sp.nspin; ++q) {
@@ -870,11 +904,6 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
       TROT_CHECK_LAUNCH("green_slices_kernel");
       return TROT_OK;
     })());
-  }
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(exchange_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kExSmem + 1024);
-    attr_set = true;
   }
   for (int q = 0; q < sp.nspin; ++q) {
     SpinLayout L = spin_layout(s, sp, q);
@@ -896,11 +925,7 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
     a.nblk_total = m.nblk_total;
     a.status = m.status;
     dim3 grid(L.nblk, chunks);
-    TROT_TIMED("exchange_exact_tc", st, ([&]() -> int {
-      exchange_exact_kernel<<<grid, kExThreads, kExSmem + 1024, st>>>(a);
-      TROT_CHECK_LAUNCH("exchange_exact_kernel");
-      return TROT_OK;
-    })());
+    TROT_TIMED("exchange_exact_tc", st, launch_exchange_exact(L.n_pad / 2, grid, a, st));
   }
   const int n = W * G;
   fb_combine_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, sp.nspin, sp.mult[0], sp.mult[1], m.cs[0],
