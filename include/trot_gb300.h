@@ -60,7 +60,8 @@ typedef enum {
   TROT_OP_APPLY_TROTTER = 2,
   TROT_OP_PROP_STEP = 3,
   TROT_OP_QR = 4,
-  TROT_OP_SR = 5
+  TROT_OP_SR = 5,
+  TROT_OP_OVERLAP = 6
 } trot_op;
 
 /* Operands of the mixed-precision path, prepared once per (trial,
@@ -235,6 +236,68 @@ int trot_split_key(int64_t* key, void* stream);
  * No counterpart in the reference. */
 int trot_local_energy_noalloc(const trot_system* sys, const double* walkers_a, const double* walkers_b,
                               double* energy_out, void* stream);
+
+/* ---------------------------------------------------------------- CISD trial
+ * Configuration-interaction singles+doubles trial with restricted walkers in
+ * the trial's MO basis (reference determinant = orbitals [0, nocc)), the
+ * whole space active: nocc + nvir == norb (no frozen core, no outer
+ * virtuals).  All arrays are device float64, row-major:
+ *   ci1      (nocc, nvir)                      c_ia
+ *   ci2      (nocc*nvir, nocc*nvir)            c_iajb, row (i,a), column (j,b)
+ *   ci2_perm (nocc*nvir, nocc*nvir)            ci2_perm[(i,b),(j,a)] = c_iajb
+ *   h1       (norb, norb), chol (nchol, norb, norb)
+ *   lci1     (nchol, norb, nocc)               lci1[g][i][p] = sum_a chol[g][i][nocc+a] c_pa
+ *   mo       (norb, nocc)                      the first nocc columns of I
+ * Replaces CisdTrial / the CISD meas context (trot/trial/cisd.py:14-88,
+ * trot/meas/cisd.py:772-836 build_meas_ctx). */
+typedef struct {
+  int norb, nocc, nvir, nchol;
+  double h0;
+  const double* ci1;
+  const double* ci2;
+  const double* ci2_perm;
+  const double* h1;
+  const double* chol;
+  const double* lci1;
+  const double* mo;
+} trot_cisd;
+
+/* Device workspace for trot_cisd_overlap (TROT_OP_OVERLAP), trot_cisd_force_bias
+ * (TROT_OP_FORCE_BIAS) or trot_cisd_local_energy (TROT_OP_LOCAL_ENERGY); 0 on bad
+ * sizes.  The local energy needs 3 W nchol nocc nvir complex values for the
+ * l2ci2 quadratic forms. */
+size_t trot_cisd_workspace_size(const trot_cisd* cisd, int n_walkers, int op);
+/* walkers: complex128 (W, norb, nocc); out complex128 (W).
+ * overlap_r_high (trot/trial/cisd.py:148-186). */
+int trot_cisd_overlap(const trot_cisd* cisd, int n_walkers, const double* walkers, double* overlap_out,
+                      void* workspace, size_t workspace_bytes, void* stream);
+/* out complex128 (W, nchol).  force_bias_kernel_rw_rh_high (trot/meas/cisd.py:548-572). */
+int trot_cisd_force_bias(const trot_cisd* cisd, int n_walkers, const double* walkers, double* fb_out,
+                         void* workspace, size_t workspace_bytes, void* stream);
+/* out complex128 (W).  energy_kernel_rw_rh, "high" memory mode, float64
+ * contractions (trot/meas/cisd.py:608-769). */
+int trot_cisd_local_energy(const trot_cisd* cisd, int n_walkers, const double* walkers, double* energy_out,
+                           void* workspace, size_t workspace_bytes, void* stream);
+
+/* out complex128 (W, norb, norb): the mixed-estimator 1-RDM of one spin,
+ * G0 - (ci1_green + ci2_green) / ov (rdm1_kernel_rw, trot/meas/cisd.py:772-820;
+ * both spins are equal for restricted walkers).  Workspace as for
+ * TROT_OP_FORCE_BIAS. */
+int trot_cisd_rdm1(const trot_cisd* cisd, int n_walkers, const double* walkers, double* rdm1_out, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/* One phaseless step with the CISD trial (trot/prop/afqmc.py:79-144 with
+ * make_cisd_meas_ops): force bias (and, if energy_out is not null, the local
+ * energy of the incoming walkers), shifted fields, VHS, Taylor propagation
+ * with one-body half steps, CISD overlaps of the new walkers, phaseless
+ * weights and population shift, all FP64.  `prop` carries the propagation
+ * context (kind TROT_RHF_R, precision TROT_FP64, n_walkers, n_exp_terms, dt,
+ * sqrt_dt, h0_prop, weight_floor/cap, pop_control_damping, exp_h1_half,
+ * chol_flat, mf_shifts_im); state->walkers_a (W, norb, nocc) is updated in
+ * place.  Workspace: trot_cisd_workspace_size(cisd, W, TROT_OP_PROP_STEP). */
+int trot_cisd_prop_step(const trot_cisd* cisd, const trot_system* prop, const trot_state* state,
+                        const double* fields, double* energy_out, void* workspace, size_t workspace_bytes,
+                        void* stream);
 
 /* Plain BF16 tensor-core GEMM (tcgen05, accumulator in tensor memory):
  * D (M x N, float32) = A (M x K, bf16) * B (N x K, bf16)^T, all row-major,

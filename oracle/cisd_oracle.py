@@ -162,3 +162,48 @@ def energy(w, tr: CisdTrial, h0, h1, chol):
     e2 = e2_0 + e2_1 + e2_2
     ov = 1.0 + 2.0 * ci1g + gci2g
     return (e1 + e2) / ov + h0
+
+
+def rdm1(w, tr: CisdTrial):
+    """``rdm1_kernel_rw`` (trot/meas/cisd.py:772-820), one spin: G0 - (ci1_green + ci2_green) / ov,
+    G0[:, :nocc_full] = G^T."""
+    g = green(w, tr.nocc_full)
+    g_act, g_occ, gp = _blocks(g, tr)
+    ci1g = np.einsum("pt,bpt->b", tr.ci1, g_occ)
+    ci1_green = (gp @ tr.ci1.T) @ g_act
+    c, e = _ci2g(tr.ci2, g_occ)
+    ci2_green = 2.0 * ((gp @ np.swapaxes(c, -1, -2)) @ g_act) - (gp @ np.swapaxes(e, -1, -2)) @ g_act
+    gci2g = np.einsum("bqu,bqu->b", 2.0 * c - e, g_occ)
+    ov = 1.0 + 2.0 * ci1g + gci2g
+    g0 = np.zeros((w.shape[0], tr.norb, tr.norb), dtype=g.dtype)
+    g0[:, :, : tr.nocc_full] = np.swapaxes(g, -1, -2)
+    return g0 - (ci1_green + ci2_green) / ov[:, None, None]
+
+
+@dataclass(frozen=True)
+class CisdModel:
+    """CISD trial with restricted walkers in the shape ``afqmc_oracle.afqmc_step`` /
+    ``afqmc_oracle.block`` expect (overlap, force_bias, energy, trotter, walker_kind):
+    trot/prop/afqmc.py:79-144 with the CISD meas ops."""
+
+    trial: CisdTrial
+    h0: float
+    h1: np.ndarray
+    chol: np.ndarray
+    prop: object  # afqmc_oracle.PropCtx
+
+    walker_kind = "restricted"
+
+    def overlap(self, w):
+        return overlap(w, self.trial)
+
+    def force_bias(self, w):
+        return force_bias(w, self.trial, self.chol)
+
+    def energy(self, w):
+        return energy(w, self.trial, self.h0, self.h1, self.chol)
+
+    def trotter(self, w, xs, n_terms):
+        from oracle import afqmc_oracle
+
+        return afqmc_oracle.apply_trotter_r(w, xs, self.prop, n_terms)

@@ -186,12 +186,18 @@ def cisd_case(name, norb, nocc, nchol, n_walkers, seed=0, h0=0.4, noise=0.1):
         w, ham, meas_ctx, trial))
     out["energy"] = np.asarray(vm(meas_ops.require_kernel("energy"), in_axes=(0, None, None, None))(
         w, ham, meas_ctx, trial))
+    out["rdm1"] = np.asarray(vm(meas_ops.require_observable("rdm1"), in_axes=(0, None, None, None))(
+        w, ham, meas_ctx, trial))
     path = os.path.join(HERE, f"{name}.npz")
     np.savez_compressed(path, **{k: np.asarray(v) for k, v in out.items()})
     print(f"wrote {path}: {os.path.getsize(path) / 1e3:.0f} kB")
 
 
 if __name__ == "__main__":
+    if len(sys.argv) > 2 and sys.argv[2] == "cisd":
+        cisd_case("cisd_small", norb=12, nocc=3, nchol=20, n_walkers=4)
+        cisd_case("cisd_n20", norb=20, nocc=5, nchol=50, n_walkers=3, seed=1)
+        sys.exit(0)
     cisd_case("cisd_small", norb=12, nocc=3, nchol=20, n_walkers=4)
     cisd_case("cisd_n20", norb=20, nocc=5, nchol=50, n_walkers=3, seed=1)
     case("rhf_r_small", norb=10, nelec=(3, 3), nchol=16, n_walkers=5, kind="rhf_r")

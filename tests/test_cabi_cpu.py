@@ -96,3 +96,44 @@ def test_workspace_size_monotone():
     big = _lib.load().trot_workspace_size(ctypes.byref(_sys(n_walkers=400)), _lib.OP_PROP_STEP)
     assert big > small > 0
     assert _lib.load().trot_workspace_size(ctypes.byref(_sys(n_walkers=0)), _lib.OP_PROP_STEP) == 0
+
+
+def _cisd(**kw):
+    c = _lib.TrotCisd()
+    c.norb, c.nocc, c.nvir, c.nchol, c.h0 = 10, 3, 7, 12, 0.5
+    c.ci1 = c.ci2 = c.ci2_perm = c.h1 = c.chol = c.lci1 = c.mo = 0x1000
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+def test_cisd_workspace_and_errors():
+    lib = _lib.load()
+    c = _cisd()
+    sizes = [lib.trot_cisd_workspace_size(ctypes.byref(c), 8, op)
+             for op in (_lib.OP_OVERLAP, _lib.OP_FORCE_BIAS, _lib.OP_LOCAL_ENERGY, _lib.OP_PROP_STEP)]
+    assert 0 < sizes[0] < sizes[1] < sizes[2] < sizes[3]
+    # the local energy keeps 3 W G nocc nvir complex values for the l2ci2 quadratic forms
+    assert sizes[2] - sizes[1] >= 3 * 8 * 12 * 21 * 16
+    assert lib.trot_cisd_workspace_size(ctypes.byref(c), 800, _lib.OP_LOCAL_ENERGY) > sizes[2]
+    assert lib.trot_cisd_workspace_size(ctypes.byref(c), 8, _lib.OP_QR) == 0
+    assert lib.trot_cisd_workspace_size(ctypes.byref(_cisd(nvir=6)), 8, _lib.OP_OVERLAP) == 0
+    assert b"nocc + nvir == norb" in lib.trot_last_error()
+    assert lib.trot_cisd_workspace_size(None, 8, _lib.OP_OVERLAP) == 0
+    # overlap needs no Hamiltonian; the energy does
+    nh = _cisd(h1=0, chol=0, lci1=0)
+    assert lib.trot_cisd_overlap(ctypes.byref(nh), 8, 0x1000, 0x1000, 0x1000, 16, None) == 4
+    assert lib.trot_cisd_local_energy(ctypes.byref(nh), 8, 0x1000, 0x1000, 0x1000, 1 << 40, None) == 3
+    assert lib.trot_cisd_force_bias(ctypes.byref(c), 8, None, 0x1000, 0x1000, 1 << 40, None) == 3
+    assert lib.trot_cisd_local_energy(ctypes.byref(c), 0, 0x1000, 0x1000, 0x1000, 1 << 40, None) == 1
+    # shared-memory tiles bound the orbital count
+    assert lib.trot_cisd_overlap(ctypes.byref(_cisd(norb=200, nvir=197)), 8, 0x1000, 0x1000, 0x1000, 1 << 40,
+                                 None) == 8
+    # the step's propagation context must match the CISD sizes and be restricted FP64
+    s = _sys(n_walkers=8, norb=10, nchol=12, nocc_a=3)
+    st = _lib.TrotState()
+    st.walkers_a = st.weights = st.overlaps = st.scalars = st.node_encounters = 0x1000
+    assert lib.trot_cisd_prop_step(ctypes.byref(c), ctypes.byref(_sys(n_walkers=8, norb=10, nchol=11, nocc_a=3)),
+                                   ctypes.byref(st), 0x1000, None, 0x1000, 1 << 40, None) == 1
+    assert lib.trot_cisd_prop_step(ctypes.byref(c), ctypes.byref(s), ctypes.byref(st), 0x1000, None, 0x1000, 16,
+                                   None) == 4

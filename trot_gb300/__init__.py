@@ -13,11 +13,13 @@ from .meas import (RhfMeasCtx, UhfMeasCtx, build_rhf_meas_ctx, build_uhf_meas_ct
 from .prop import CholAfqmcCtx, afqmc_step, init_prop_state, make_prop_ops, make_trotter_ops
 from .trial import RhfTrial, UhfTrial, get_rdm1, make_rhf_trial_ops, make_uhf_trial_ops
 from . import walkers
+from .cisd import CisdMeasCtx, CisdTrial, make_cisd_meas_ops, make_cisd_trial_ops
 
 __all__ = [
     "HamChol", "MeasOps", "PropOps", "PropState", "QmcParams", "QmcParamsBase", "System", "TrialOps",
     "k_energy", "k_force_bias", "RhfMeasCtx", "UhfMeasCtx", "build_rhf_meas_ctx", "build_uhf_meas_ctx",
     "make_rhf_meas_ops", "make_uhf_meas_ops", "CholAfqmcCtx", "afqmc_step", "init_prop_state", "make_prop_ops",
     "make_trotter_ops", "RhfTrial", "UhfTrial", "get_rdm1", "make_rhf_trial_ops", "make_uhf_trial_ops",
-    "walkers", "rng", "synthetic", "block", "BlockObs",
+    "walkers", "rng", "synthetic", "block", "BlockObs", "CisdTrial", "CisdMeasCtx", "make_cisd_meas_ops",
+    "make_cisd_trial_ops",
 ]

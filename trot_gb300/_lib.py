@@ -22,7 +22,7 @@ RHF_R, RHF_U, UHF_U = 0, 1, 2
 # trot_precision
 FP64, MIXED = 0, 1
 # trot_op
-OP_FORCE_BIAS, OP_LOCAL_ENERGY, OP_APPLY_TROTTER, OP_PROP_STEP, OP_QR, OP_SR = range(6)
+OP_FORCE_BIAS, OP_LOCAL_ENERGY, OP_APPLY_TROTTER, OP_PROP_STEP, OP_QR, OP_SR, OP_OVERLAP = range(7)
 
 _p = ctypes.c_void_p
 _d = ctypes.c_double
@@ -62,6 +62,15 @@ class TrotState(ctypes.Structure):
     ]
 
 
+class TrotCisd(ctypes.Structure):
+    """trot_cisd (include/trot_gb300.h)."""
+
+    _fields_ = [
+        ("norb", _i), ("nocc", _i), ("nvir", _i), ("nchol", _i), ("h0", _d),
+        ("ci1", _p), ("ci2", _p), ("ci2_perm", _p), ("h1", _p), ("chol", _p), ("lci1", _p), ("mo", _p),
+    ]
+
+
 class TrotError(RuntimeError):
     def __init__(self, status: int, msg: str):
         self.status = status
@@ -88,6 +97,13 @@ _SIGNATURES = {
     "trot_local_energy_noalloc": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p]),
     "trot_workspace_status": (_i, [_p, _p]),
     "trot_tc_gemm_bf16": (_i, [_p, _p, _p, _i, _i, _i, _p, _p]),
+    "trot_cisd_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(TrotCisd), _i, _i]),
+    "trot_cisd_overlap": (_i, [ctypes.POINTER(TrotCisd), _i, _p, _p, _p, ctypes.c_size_t, _p]),
+    "trot_cisd_force_bias": (_i, [ctypes.POINTER(TrotCisd), _i, _p, _p, _p, ctypes.c_size_t, _p]),
+    "trot_cisd_local_energy": (_i, [ctypes.POINTER(TrotCisd), _i, _p, _p, _p, ctypes.c_size_t, _p]),
+    "trot_cisd_rdm1": (_i, [ctypes.POINTER(TrotCisd), _i, _p, _p, _p, ctypes.c_size_t, _p]),
+    "trot_cisd_prop_step": (_i, [ctypes.POINTER(TrotCisd), ctypes.POINTER(TrotSystem), ctypes.POINTER(TrotState),
+                                 _p, _p, _p, ctypes.c_size_t, _p]),
     "trot_profile_enable": (_i, [_i]),
     "trot_profile_collect": (_i, [_i, ctypes.c_char_p, _p, _p]),
 }

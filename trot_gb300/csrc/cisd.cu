@@ -1,0 +1,606 @@
+// CISD-trial overlap, force bias and local energy (FP64), restricted walkers
+// in the trial's MO basis (reference determinant = orbitals [0, n)).
+//
+// Restated from trot/trial/cisd.py:148-186 and trot/meas/cisd.py:548-769
+// ("high" memory mode, float64 contractions).  With x = G[:, n:] (n x v),
+// C_c = x . ci2 and C_e = x . ci2_perm (ci2_perm[(p,u),(q,t)] = ci2[p,t,q,u]):
+//   ci2g = 2 C_c - C_e,  gci2g = sum ci2g o x,  ci1g = sum ci1 o x,
+//   ov = 1 + 2 ci1g + gci2g        (overlap = ov det(w_occ)^2)
+//   ci1_green = (gp ci1^T) G,  ci2_green = (gp ci2g^T) G   (N x N; gp rows < n: x, rows >= n: -I)
+//   force bias = (2 lg + 4 ci1g lg + 2 gci2g lg - 2 (lci1g + lci2g)) / ov
+//     with lg = rot_chol . G, lci{1,2}g = chol . ci{1,2}_green
+//   local energy: the terms of energy_kernel_rw_rh, see cisd_energy_combine.
+// The l2ci2 quadratic forms sum_g X_g^T ci2 X_g and X_g^T ci2_perm X_g
+// (X_g = vec(glgp_g)) are two GEMMs over all (walker, g) rows.
+#include "kernels.h"
+
+#include "profile.h"
+#include "step_tail.cuh"
+
+namespace trot {
+
+// ------------------------------------------------------------------ workspace
+struct CisdBuffers {
+  double2 *green, *det2, *hg2;  // G (W, n, N); det(w_occ)^2 (W); 2 hg (W)
+  double2* x;                   // (W, n v) contiguous x
+  double2 *cc, *ce;             // (W, n v)
+  double2* ci1g1;               // (W, n, n)
+  double2 *m1, *m2;             // ci1_green, ci2_green (W, N, N)
+  double2* wsc;                 // per-walker scalars (W, 8): ci1g, gci2g, e1_1_2, e1_2_2, ...
+  double2 *lg, *lci1g, *lci2g;  // (W, G)
+  double2* xg;                  // glgp rows (W G, n v)
+  double2 *y1, *y2;             // (W G, n v)
+  double2* gpart;               // per (walker, gamma chunk) partial sums (W, nchunk, 4)
+  // propagation step
+  double2 *fb, *xs, *shift_term, *fb_term, *vhs, *ov_new;
+  int* node_flag;
+};
+
+static constexpr int kCisdGChunk = 8;
+static int cisd_chunks(int G) { return (G + kCisdGChunk - 1) / kCisdGChunk; }
+
+static size_t carve_cisd(const trot_cisd* c, int W, int op, Carver& cv, CisdBuffers& b) {
+  const size_t N = c->norb, n = c->nocc, v = c->nvir, G = c->nchol, nv = n * v;
+  b = CisdBuffers{};
+  b.green = cv.take<double2>(W * n * N);
+  b.det2 = cv.take<double2>(W);
+  b.hg2 = cv.take<double2>(W);
+  b.x = cv.take<double2>(W * nv);
+  b.cc = cv.take<double2>(W * nv);
+  b.ce = cv.take<double2>(W * nv);
+  b.wsc = cv.take<double2>(W * 8);
+  if (op == TROT_OP_OVERLAP) return cv.used;
+  b.ci1g1 = cv.take<double2>(W * n * n);
+  b.m1 = cv.take<double2>(W * N * N);
+  b.m2 = cv.take<double2>(W * N * N);
+  b.lg = cv.take<double2>(W * G);
+  b.lci1g = cv.take<double2>(W * G);
+  b.lci2g = cv.take<double2>(W * G);
+  if (op == TROT_OP_FORCE_BIAS) return cv.used;
+  b.xg = cv.take<double2>((size_t)W * G * nv);
+  b.y1 = cv.take<double2>((size_t)W * G * nv);
+  b.y2 = cv.take<double2>((size_t)W * G * nv);
+  b.gpart = cv.take<double2>((size_t)W * cisd_chunks((int)G) * 4);
+  if (op != TROT_OP_PROP_STEP) return cv.used;
+  b.fb = cv.take<double2>((size_t)W * G);
+  b.xs = cv.take<double2>((size_t)W * G);
+  b.shift_term = cv.take<double2>(W);
+  b.fb_term = cv.take<double2>(W);
+  b.vhs = cv.take<double2>((size_t)W * N * N);
+  b.ov_new = cv.take<double2>(W);
+  b.node_flag = cv.take<int>(W);
+  return cv.used;
+}
+
+// ------------------------------------------------------------------ x, ci1g, ci1g1
+// x[b][p][t] = G[b][p][n + t];  ci1g = sum ci1 o x;  ci1g1[a][q] = sum_t ci1[a][t] G[q][n + t]
+__global__ void cisd_x_kernel(int N, int n, int v, const double2* __restrict__ green, const double* __restrict__ ci1,
+                              double2* __restrict__ x, double2* __restrict__ ci1g1, double2* __restrict__ wsc) {
+  __shared__ double2 red[32];
+  const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const double2* g = green + (size_t)b * n * N;
+  double2 acc = cmk(0.0, 0.0);
+  for (int e = tid; e < n * v; e += nt) {
+    const int p = e / v, t = e % v;
+    const double2 val = g[p * N + n + t];
+    x[(size_t)b * n * v + e] = val;
+    crfma(acc, ci1[e], val);
+  }
+  if (ci1g1) {
+    for (int e = tid; e < n * n; e += nt) {
+      const int a = e / n, q = e % n;
+      double2 s = cmk(0.0, 0.0);
+      for (int t = 0; t < v; ++t) crfma(s, ci1[a * v + t], g[q * N + n + t]);
+      ci1g1[(size_t)b * n * n + e] = s;
+    }
+  }
+  acc = block_sum2(acc, red);
+  if (tid == 0) wsc[(size_t)b * 8 + 0] = acc;  // ci1g
+}
+
+// ------------------------------------------------------------------ per-walker N x N matrices
+// ci2g = 2 cc - ce; gci2g = sum ci2g o x; P_Y = gp Y^T (N x n); M = P_Y G (N x N) for Y = ci1, ci2g;
+// e1_1_2 = -2 sum h1 o M1, e1_2_2 = -2 sum h1 o M2.
+__global__ void __launch_bounds__(256)
+cisd_mats_kernel(int N, int n, int v, const double2* __restrict__ green, const double* __restrict__ ci1,
+                 const double2* __restrict__ cc, const double2* __restrict__ ce, const double2* __restrict__ x,
+                 const double* __restrict__ h1, double2* __restrict__ m1, double2* __restrict__ m2,
+                 double2* __restrict__ wsc) {
+  extern __shared__ double2 sm[];
+  __shared__ double2 red[32];
+  const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  double2* Gs = sm;              // n x N
+  double2* Y2 = Gs + n * N;      // n x v  (ci2g)
+  double2* P1 = Y2 + n * v;      // N x n
+  double2* P2 = P1 + N * n;      // N x n
+  const double2* g = green + (size_t)b * n * N;
+  for (int e = tid; e < n * N; e += nt) Gs[e] = g[e];
+  double2 gs = cmk(0.0, 0.0);
+  for (int e = tid; e < n * v; e += nt) {
+    const double2 c = cc[(size_t)b * n * v + e], d = ce[(size_t)b * n * v + e];
+    const double2 y = cmk(2.0 * c.x - d.x, 2.0 * c.y - d.y);
+    Y2[e] = y;
+    cfma(gs, y, x[(size_t)b * n * v + e]);
+  }
+  __syncthreads();
+  // P[i][p] = sum_t gp[i][t] Y[p][t]: i < n -> sum_t x[i][t] Y[p][t]; i >= n -> -Y[p][i - n]
+  for (int e = tid; e < N * n; e += nt) {
+    const int i = e / n, p = e % n;
+    double2 a1 = cmk(0.0, 0.0), a2 = cmk(0.0, 0.0);
+    if (i < n) {
+      for (int t = 0; t < v; ++t) {
+        const double2 xv = Gs[i * N + n + t];
+        crfma(a1, ci1[p * v + t], xv);
+        cfma(a2, Y2[p * v + t], xv);
+      }
+    } else if (i - n < v) {
+      a1 = cmk(-ci1[p * v + (i - n)], 0.0);
+      const double2 y = Y2[p * v + (i - n)];
+      a2 = cmk(-y.x, -y.y);
+    }
+    P1[e] = a1;
+    P2[e] = a2;
+  }
+  __syncthreads();
+  double2 h1s = cmk(0.0, 0.0), h2s = cmk(0.0, 0.0);
+  for (int e = tid; e < N * N; e += nt) {
+    const int i = e / N, j = e % N;
+    double2 s1 = cmk(0.0, 0.0), s2 = cmk(0.0, 0.0);
+    for (int p = 0; p < n; ++p) {
+      const double2 gv = Gs[p * N + j];
+      cfma(s1, P1[i * n + p], gv);
+      cfma(s2, P2[i * n + p], gv);
+    }
+    m1[(size_t)b * N * N + e] = s1;
+    m2[(size_t)b * N * N + e] = s2;
+    const double hv = h1[e];
+    crfma(h1s, hv, s1);
+    crfma(h2s, hv, s2);
+  }
+  gs = block_sum2(gs, red);
+  h1s = block_sum2(h1s, red);
+  h2s = block_sum2(h2s, red);
+  if (tid == 0) {
+    wsc[(size_t)b * 8 + 1] = gs;                           // gci2g
+    wsc[(size_t)b * 8 + 2] = cmk(-2.0 * h1s.x, -2.0 * h1s.y);  // e1_1_2
+    wsc[(size_t)b * 8 + 3] = cmk(-2.0 * h2s.x, -2.0 * h2s.y);  // e1_2_2
+  }
+}
+
+// ------------------------------------------------------------------ per (walker, Cholesky chunk) terms
+// For each g in the chunk (L = chol_g, R = L[:n, :]):
+//   lg1 = R G^T (n x n), lci1g_mat B[q][a] = sum_i G[q][i] lci1_g[i][a]
+//   gl = G L (n x N), lci2_green[p][j] = sum_i R[p][i] M2[j][i], glgp = gl gp (n x v) -> xg
+//   partial sums: [0] sum lg1 o lg1^T, [1] tr(lg1 lg1 ci1g1), [2] sum B o lg1, [3] sum gl o lci2_green
+__global__ void __launch_bounds__(256)
+cisd_gamma_kernel(int N, int n, int v, int G, const double2* __restrict__ green, const double* __restrict__ chol,
+                  const double* __restrict__ lci1, const double2* __restrict__ m2, const double2* __restrict__ ci1g1,
+                  double2* __restrict__ xg, double2* __restrict__ gpart) {
+  extern __shared__ double2 sm[];
+  __shared__ double2 red[32];
+  const int chunk = blockIdx.x, b = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
+  const int nchunk = gridDim.x;
+  double2* Gs = sm;                 // n x N
+  double2* M2 = Gs + n * N;         // N x N
+  double2* C1 = M2 + N * N;         // n x n  (ci1g1)
+  double2* A = C1 + n * n;          // n x n  (lg1)
+  double2* GL = A + n * n;          // n x N  (gl)
+  double* Ls = reinterpret_cast<double*>(GL + n * N);  // N x N
+  for (int e = tid; e < n * N; e += nt) Gs[e] = green[(size_t)b * n * N + e];
+  for (int e = tid; e < N * N; e += nt) M2[e] = m2[(size_t)b * N * N + e];
+  for (int e = tid; e < n * n; e += nt) C1[e] = ci1g1[(size_t)b * n * n + e];
+  double2 s0 = cmk(0.0, 0.0), s1 = cmk(0.0, 0.0), s2 = cmk(0.0, 0.0), s3 = cmk(0.0, 0.0);
+  const int g0 = chunk * kCisdGChunk, g1 = min(G, g0 + kCisdGChunk);
+  for (int gg = g0; gg < g1; ++gg) {
+    __syncthreads();
+    const double* Lg = chol + (size_t)gg * N * N;
+    for (int e = tid; e < N * N; e += nt) Ls[e] = Lg[e];
+    __syncthreads();
+    // lg1[p][q] = sum_j L[p][j] G[q][j]
+    for (int e = tid; e < n * n; e += nt) {
+      const int p = e / n, q = e % n;
+      double2 a = cmk(0.0, 0.0);
+      for (int j = 0; j < N; ++j) crfma(a, Ls[p * N + j], Gs[q * N + j]);
+      A[e] = a;
+    }
+    // gl[p][i] = sum_j G[p][j] L[j][i]
+    for (int e = tid; e < n * N; e += nt) {
+      const int p = e / N, i = e % N;
+      double2 a = cmk(0.0, 0.0);
+      for (int j = 0; j < N; ++j) crfma(a, Ls[j * N + i], Gs[p * N + j]);
+      GL[e] = a;
+    }
+    __syncthreads();
+    const double* lc = lci1 + (size_t)gg * N * n;
+    for (int e = tid; e < n * n; e += nt) {
+      const int p = e / n, q = e % n;
+      // sum lg1 o lg1^T
+      cfma(s0, A[p * n + q], A[q * n + p]);
+      // tr(lg1 lg1 ci1g1): [lg1 lg1][p][a] ci1g1[a][p] -> sum over (p, q, a): A[p][q] A[q][a] C1[a][p]
+      double2 t = cmk(0.0, 0.0);
+      for (int a2 = 0; a2 < n; ++a2) cfma(t, A[q * n + a2], C1[a2 * n + p]);
+      cfma(s1, A[p * n + q], t);
+      // B[q][a] = sum_i G[q][i] lci1_g[i][a]  (here (p, q) -> (q_idx = p, a = q))
+      double2 bq = cmk(0.0, 0.0);
+      for (int i = 0; i < N; ++i) crfma(bq, lc[i * n + q], Gs[p * N + i]);
+      cfma(s2, bq, A[p * n + q]);
+    }
+    // sum gl o lci2_green, lci2_green[p][j] = sum_i R[p][i] M2[j][i]
+    for (int e = tid; e < n * N; e += nt) {
+      const int p = e / N, j = e % N;
+      double2 a = cmk(0.0, 0.0);
+      for (int i = 0; i < N; ++i) crfma(a, Ls[p * N + i], M2[j * N + i]);
+      cfma(s3, GL[e], a);
+    }
+    // glgp[p][t] = sum_{i<n} gl[p][i] x[i][t] - gl[p][n + t]
+    double2* xo = xg + ((size_t)b * G + gg) * n * v;
+    for (int e = tid; e < n * v; e += nt) {
+      const int p = e / v, t = e % v;
+      double2 a = cmk(-GL[p * N + n + t].x, -GL[p * N + n + t].y);
+      for (int i = 0; i < n; ++i) cfma(a, GL[p * N + i], Gs[i * N + n + t]);
+      xo[e] = a;
+    }
+  }
+  s0 = block_sum2(s0, red);
+  s1 = block_sum2(s1, red);
+  s2 = block_sum2(s2, red);
+  s3 = block_sum2(s3, red);
+  if (tid == 0) {
+    double2* o = gpart + ((size_t)b * nchunk + chunk) * 4;
+    o[0] = s0; o[1] = s1; o[2] = s2; o[3] = s3;
+  }
+}
+
+// l2ci2: per walker sum over g of X_g . (2 Y1_g - Y2_g)  -> wsc[b][6]
+__global__ void cisd_l2_reduce_kernel(int G, int nv, const double2* __restrict__ xg, const double2* __restrict__ y1,
+                                      const double2* __restrict__ y2, double2* __restrict__ wsc) {
+  __shared__ double2 red[32];
+  const int b = blockIdx.x;
+  double2 acc = cmk(0.0, 0.0);
+  const size_t base = (size_t)b * G * nv, cnt = (size_t)G * nv;
+  for (size_t e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const double2 xv = xg[base + e], a = y1[base + e], c = y2[base + e];
+    cfma(acc, xv, cmk(2.0 * a.x - c.x, 2.0 * a.y - c.y));
+  }
+  acc = block_sum2(acc, red);
+  if (threadIdx.x == 0) wsc[(size_t)b * 8 + 6] = acc;
+}
+
+// ------------------------------------------------------------------ combines
+__device__ __forceinline__ double2 cdot_row(const double2* a, const double2* b, int n) {
+  double2 s = cmk(0.0, 0.0);
+  for (int k = 0; k < n; ++k) cfma(s, a[k], b[k]);
+  return s;
+}
+
+// overlap = (1 + 2 ci1g + gci2g) det0^2, gci2g = sum (2 C_c - C_e) o x; one CTA per walker
+__global__ void cisd_overlap_kernel(int nv, const double2* __restrict__ x, const double2* __restrict__ cc,
+                                    const double2* __restrict__ ce, const double2* __restrict__ wsc,
+                                    const double2* __restrict__ det2, double2* __restrict__ out) {
+  __shared__ double2 red[32];
+  const int b = blockIdx.x;
+  double2 gs = cmk(0.0, 0.0);
+  for (int e = threadIdx.x; e < nv; e += blockDim.x) {
+    const size_t k = (size_t)b * nv + e;
+    const double2 c = cc[k], d = ce[k];
+    cfma(gs, cmk(2.0 * c.x - d.x, 2.0 * c.y - d.y), x[k]);
+  }
+  gs = block_sum2(gs, red);
+  if (threadIdx.x == 0) {
+    const double2 ci1g = wsc[(size_t)b * 8 + 0];
+    out[b] = cmul(cmk(1.0 + 2.0 * ci1g.x + gs.x, 2.0 * ci1g.y + gs.y), det2[b]);
+  }
+}
+
+// force bias: (2 lg (1 + 2 ci1g + gci2g) - 2 (lci1g + lci2g)) / ov
+__global__ void cisd_fb_kernel(int W, int G, const double2* __restrict__ wsc, const double2* __restrict__ lg,
+                               const double2* __restrict__ l1, const double2* __restrict__ l2, double2* __restrict__ fb) {
+  const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (k >= (size_t)W * G) return;
+  const int b = (int)(k / G);
+  const double2 ci1g = wsc[(size_t)b * 8 + 0], gci2g = wsc[(size_t)b * 8 + 1];
+  const double2 ov = cmk(1.0 + 2.0 * ci1g.x + gci2g.x, 2.0 * ci1g.y + gci2g.y);
+  const double2 f = cmk(2.0 * ci1g.x + gci2g.x, 2.0 * ci1g.y + gci2g.y);  // (ov - 1)
+  // 2 lg + 4 ci1g lg + 2 gci2g lg = 2 lg (1 + 2 ci1g + gci2g) = 2 lg ov
+  const double2 a = cmul(lg[k], cmk(2.0 * (1.0 + f.x), 2.0 * f.y));
+  const double2 c = cadd(l1[k], l2[k]);
+  fb[k] = cdiv(cmk(a.x - 2.0 * c.x, a.y - 2.0 * c.y), ov);
+}
+
+// mixed-estimator 1-RDM (trot/meas/cisd.py:772-820): gamma = G0 - (ci1_green + ci2_green) / ov,
+// G0[i][j] = G[j][i] for j < n, 0 otherwise
+__global__ void cisd_rdm1_kernel(int N, int n, const double2* __restrict__ green, const double2* __restrict__ m1,
+                                 const double2* __restrict__ m2, const double2* __restrict__ wsc,
+                                 double2* __restrict__ out) {
+  const int b = blockIdx.y;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= N * N) return;
+  const int i = e / N, j = e % N;
+  const double2 ci1g = wsc[(size_t)b * 8 + 0], gci2g = wsc[(size_t)b * 8 + 1];
+  const double2 ov = cmk(1.0 + 2.0 * ci1g.x + gci2g.x, 2.0 * ci1g.y + gci2g.y);
+  const size_t k = (size_t)b * N * N + e;
+  const double2 corr = cdiv(cadd(m1[k], m2[k]), ov);
+  const double2 g0 = j < n ? green[(size_t)b * n * N + (size_t)j * N + i] : cmk(0.0, 0.0);
+  out[k] = csub(g0, corr);
+}
+
+// phaseless weights from the CISD overlaps of the propagated walkers
+__global__ void cisd_weight_kernel(TrotterArgs a, const double2* __restrict__ ov_new) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < a.W) phaseless_update(a, b, ov_new[b]);
+}
+
+// local energy (trot/meas/cisd.py:608-769)
+__global__ void __launch_bounds__(256)
+cisd_energy_kernel(int G, int nchunk, double h0, const double2* __restrict__ wsc, const double2* __restrict__ hg2,
+                   const double2* __restrict__ lg, const double2* __restrict__ l1, const double2* __restrict__ l2,
+                   const double2* __restrict__ gpart, double2* __restrict__ energy) {
+  __shared__ double2 red[32];
+  const int b = blockIdx.x;
+  double2 lglg = cmk(0.0, 0.0), l1lg = cmk(0.0, 0.0), l2lg = cmk(0.0, 0.0);
+  for (int g = threadIdx.x; g < G; g += blockDim.x) {
+    const double2 x = lg[(size_t)b * G + g];
+    cfma(lglg, x, x);
+    cfma(l1lg, l1[(size_t)b * G + g], x);
+    cfma(l2lg, l2[(size_t)b * G + g], x);
+  }
+  double2 p[4] = {cmk(0.0, 0.0), cmk(0.0, 0.0), cmk(0.0, 0.0), cmk(0.0, 0.0)};
+  for (int c = threadIdx.x; c < nchunk; c += blockDim.x)
+    for (int k = 0; k < 4; ++k) p[k] = cadd(p[k], gpart[((size_t)b * nchunk + c) * 4 + k]);
+  lglg = block_sum2(lglg, red);
+  l1lg = block_sum2(l1lg, red);
+  l2lg = block_sum2(l2lg, red);
+  for (int k = 0; k < 4; ++k) p[k] = block_sum2(p[k], red);
+  if (threadIdx.x == 0) {
+    const double2 ci1g = wsc[(size_t)b * 8 + 0], gci2g = wsc[(size_t)b * 8 + 1];
+    const double2 e1_1_2 = wsc[(size_t)b * 8 + 2], e1_2_2 = wsc[(size_t)b * 8 + 3];
+    const double2 l2ci2 = wsc[(size_t)b * 8 + 6];
+    const double2 hg = hg2[b];  // 2 hg
+    // one body
+    const double2 e1 = cadd(cadd(cadd(hg, cmul(cscale(ci1g, 2.0), hg)), e1_1_2),
+                            cadd(cmul(hg, gci2g), e1_2_2));
+    // two body
+    const double2 e2_0 = csub(cscale(lglg, 2.0), p[0]);
+    const double2 e2_1 = cadd(cmul(cscale(e2_0, 2.0), ci1g),
+                              cscale(cadd(cadd(cscale(l1lg, -2.0), p[1]), cscale(p[2], -1.0)), 2.0));
+    const double2 e2_2 = cadd(cadd(cmul(e2_0, gci2g), cscale(cadd(cscale(l2lg, -1.0), cscale(p[3], 0.5)), 4.0)),
+                              l2ci2);
+    const double2 e2 = cadd(cadd(e2_0, e2_1), e2_2);
+    const double2 ov = cmk(1.0 + 2.0 * ci1g.x + gci2g.x, 2.0 * ci1g.y + gci2g.y);
+    const double2 e = cdiv(cadd(e1, e2), ov);
+    energy[b] = cmk(e.x + h0, e.y);
+  }
+}
+
+// ------------------------------------------------------------------ orchestration
+static size_t cisd_mats_smem(int N, int n, int v) { return (size_t)(n * N + n * v + 2 * N * n) * sizeof(double2); }
+static size_t cisd_gamma_smem(int N, int n) {
+  return (size_t)(2 * n * N + N * N + 2 * n * n) * sizeof(double2) + (size_t)N * N * sizeof(double);
+}
+
+// need_ham: the force bias / energy / step also read h1, chol and lci1
+static int check_cisd(const trot_cisd* c, int W, bool need_ham = true) {
+  if (!c) { set_error("null CISD context"); return TROT_ERR_NULL_PTR; }
+  if (W <= 0 || W > 65535 || c->norb <= 0 || c->nocc <= 0 || c->nvir <= 0 || c->nocc + c->nvir != c->norb ||
+      c->nchol <= 0) {
+    set_error("bad CISD sizes W=%d N=%d n=%d v=%d G=%d (need nocc + nvir == norb)", W, c->norb, c->nocc, c->nvir,
+              c->nchol);
+    return TROT_ERR_BAD_SHAPE;
+  }
+  if (!c->ci1 || !c->ci2 || !c->ci2_perm || !c->mo || (need_ham && (!c->h1 || !c->chol || !c->lci1))) {
+    set_error("null CISD context array");
+    return TROT_ERR_NULL_PTR;
+  }
+  if (c->nocc > 64 || cisd_mats_smem(c->norb, c->nocc, c->nvir) > 200 * 1024 ||
+      cisd_gamma_smem(c->norb, c->nocc) > 200 * 1024) {
+    set_error("CISD tile of N=%d, n=%d exceeds shared memory", c->norb, c->nocc);
+    return TROT_ERR_UNSUPPORTED;
+  }
+  return TROT_OK;
+}
+
+static Spins cisd_spins(const trot_cisd* c) {
+  Spins sp{};
+  sp.nspin = 1;
+  sp.n[0] = c->nocc;
+  sp.mult[0] = 2;
+  sp.off[0] = 0;
+  sp.off[1] = c->nocc;
+  sp.ntot = c->nocc;
+  sp.mo[0] = c->mo;
+  sp.rot_h1[0] = c->h1;  // rows [0, n) of h1: 2 sum G o h1[:n, :] = 2 hg
+  sp.rot_chol[0] = nullptr;
+  return sp;
+}
+
+// green, x, C_c / C_e, scalars; stage 0 = overlap only, 1 = + N x N matrices and chol contractions, 2 = + energy terms
+static int cisd_run(const trot_cisd* c, int W, const double2* w, CisdBuffers& b, int stage, cudaStream_t st) {
+  const int N = c->norb, n = c->nocc, v = c->nvir, G = c->nchol, nv = n * v;
+  Spins sp = cisd_spins(c);
+  TROT_TIMED("cisd_green", st, launch_green(sp, W, N, w, nullptr, b.green, b.det2, b.hg2, st));
+  cisd_x_kernel<<<W, 256, 0, st>>>(N, n, v, b.green, c->ci1, b.x, stage >= 1 ? b.ci1g1 : nullptr, b.wsc);
+  TROT_CHECK_LAUNCH("cisd_x_kernel");
+  TROT_TIMED("cisd_ci2g", st, launch_zgemm_cr(W, nv, nv, 1.0, b.x, nv, c->ci2, nv, false, b.cc, nv, false, st));
+  TROT_TRY(launch_zgemm_cr(W, nv, nv, 1.0, b.x, nv, c->ci2_perm, nv, false, b.ce, nv, false, st));
+  if (stage == 0) return TROT_OK;
+  const size_t smem = cisd_mats_smem(N, n, v);
+  if (smem > 48 * 1024) cudaFuncSetAttribute(cisd_mats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  TROT_TIMED("cisd_mats", st, ([&]() -> int {
+    cisd_mats_kernel<<<W, 256, smem, st>>>(N, n, v, b.green, c->ci1, b.cc, b.ce, b.x, c->h1, b.m1, b.m2, b.wsc);
+    TROT_CHECK_LAUNCH("cisd_mats_kernel");
+    return TROT_OK;
+  })());
+  // lg = rot_chol . G  (rot_chol rows g: chol[g][:n][:] = first n N entries of chol_flat row g)
+  TROT_TIMED("cisd_chol_gemm", st,
+             launch_zgemm_cr(W, G, n * N, 1.0, b.green, n * N, c->chol, N * N, true, b.lg, G, false, st));
+  TROT_TRY(launch_zgemm_cr(W, G, N * N, 1.0, b.m1, N * N, c->chol, N * N, true, b.lci1g, G, false, st));
+  TROT_TRY(launch_zgemm_cr(W, G, N * N, 1.0, b.m2, N * N, c->chol, N * N, true, b.lci2g, G, false, st));
+  if (stage == 1) return TROT_OK;
+  const int nch = cisd_chunks(G);
+  const size_t smem2 = cisd_gamma_smem(N, n);
+  cudaFuncSetAttribute(cisd_gamma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+  TROT_TIMED("cisd_gamma", st, ([&]() -> int {
+    cisd_gamma_kernel<<<dim3(nch, W), 256, smem2, st>>>(N, n, v, G, b.green, c->chol, c->lci1, b.m2, b.ci1g1, b.xg,
+                                                       b.gpart);
+    TROT_CHECK_LAUNCH("cisd_gamma_kernel");
+    return TROT_OK;
+  })());
+  if ((size_t)W * G > 65535u * 64u) { set_error("CISD: W*G too large"); return TROT_ERR_UNSUPPORTED; }
+  TROT_TIMED("cisd_l2ci2", st,
+             launch_zgemm_cr(W * G, nv, nv, 1.0, b.xg, nv, c->ci2, nv, false, b.y1, nv, false, st));
+  TROT_TRY(launch_zgemm_cr(W * G, nv, nv, 1.0, b.xg, nv, c->ci2_perm, nv, false, b.y2, nv, false, st));
+  cisd_l2_reduce_kernel<<<W, 256, 0, st>>>(G, nv, b.xg, b.y1, b.y2, b.wsc);
+  TROT_CHECK_LAUNCH("cisd_l2_reduce_kernel");
+  return TROT_OK;
+}
+
+}  // namespace trot
+
+using namespace trot;
+
+extern "C" {
+
+size_t trot_cisd_workspace_size(const trot_cisd* c, int n_walkers, int op) {
+  if (check_cisd(c, n_walkers, false) != TROT_OK) return 0;
+  if (op != TROT_OP_OVERLAP && op != TROT_OP_FORCE_BIAS && op != TROT_OP_LOCAL_ENERGY && op != TROT_OP_PROP_STEP) {
+    set_error("CISD workspace: unsupported op %d", op);
+    return 0;
+  }
+  Carver cv(nullptr, 0);
+  CisdBuffers b;
+  return carve_cisd(c, n_walkers, op, cv, b) + 256;
+}
+
+int trot_cisd_overlap(const trot_cisd* c, int W, const double* walkers, double* out, void* ws, size_t ws_bytes,
+                      void* stream) {
+  TROT_TRY(check_cisd(c, W, false));
+  if (!walkers || !out) { set_error("null walkers or output"); return TROT_ERR_NULL_PTR; }
+  Carver cv(ws, ws_bytes);
+  CisdBuffers b;
+  carve_cisd(c, W, TROT_OP_OVERLAP, cv, b);
+  if (!cv.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, cv.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
+  cudaStream_t st = (cudaStream_t)stream;
+  TROT_TRY(cisd_run(c, W, (const double2*)walkers, b, 0, st));
+  cisd_overlap_kernel<<<W, 256, 0, st>>>(c->nocc * c->nvir, b.x, b.cc, b.ce, b.wsc, b.det2, (double2*)out);
+  TROT_CHECK_LAUNCH("cisd_overlap_kernel");
+  return TROT_OK;
+}
+
+int trot_cisd_force_bias(const trot_cisd* c, int W, const double* walkers, double* out, void* ws, size_t ws_bytes,
+                         void* stream) {
+  TROT_TRY(check_cisd(c, W));
+  if (!walkers || !out) { set_error("null walkers or output"); return TROT_ERR_NULL_PTR; }
+  Carver cv(ws, ws_bytes);
+  CisdBuffers b;
+  carve_cisd(c, W, TROT_OP_FORCE_BIAS, cv, b);
+  if (!cv.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, cv.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
+  cudaStream_t st = (cudaStream_t)stream;
+  TROT_TRY(cisd_run(c, W, (const double2*)walkers, b, 1, st));
+  const size_t n = (size_t)W * c->nchol;
+  cisd_fb_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(W, c->nchol, b.wsc, b.lg, b.lci1g, b.lci2g,
+                                                             (double2*)out);
+  TROT_CHECK_LAUNCH("cisd_fb_kernel");
+  return TROT_OK;
+}
+
+int trot_cisd_local_energy(const trot_cisd* c, int W, const double* walkers, double* out, void* ws,
+                           size_t ws_bytes, void* stream) {
+  TROT_TRY(check_cisd(c, W));
+  if (!walkers || !out) { set_error("null walkers or output"); return TROT_ERR_NULL_PTR; }
+  Carver cv(ws, ws_bytes);
+  CisdBuffers b;
+  carve_cisd(c, W, TROT_OP_LOCAL_ENERGY, cv, b);
+  if (!cv.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, cv.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
+  cudaStream_t st = (cudaStream_t)stream;
+  TROT_TRY(cisd_run(c, W, (const double2*)walkers, b, 2, st));
+  cisd_energy_kernel<<<W, 256, 0, st>>>(c->nchol, cisd_chunks(c->nchol), c->h0, b.wsc, b.hg2, b.lg, b.lci1g,
+                                        b.lci2g, b.gpart, (double2*)out);
+  TROT_CHECK_LAUNCH("cisd_energy_kernel");
+  return TROT_OK;
+}
+
+int trot_cisd_rdm1(const trot_cisd* c, int W, const double* walkers, double* out, void* ws, size_t ws_bytes,
+                   void* stream) {
+  TROT_TRY(check_cisd(c, W));
+  if (!walkers || !out) { set_error("null walkers or output"); return TROT_ERR_NULL_PTR; }
+  Carver cv(ws, ws_bytes);
+  CisdBuffers b;
+  carve_cisd(c, W, TROT_OP_FORCE_BIAS, cv, b);
+  if (!cv.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, cv.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
+  cudaStream_t st = (cudaStream_t)stream;
+  TROT_TRY(cisd_run(c, W, (const double2*)walkers, b, 1, st));
+  const int N = c->norb;
+  cisd_rdm1_kernel<<<dim3((N * N + 255) / 256, W), 256, 0, st>>>(N, c->nocc, b.green, b.m1, b.m2, b.wsc,
+                                                                (double2*)out);
+  TROT_CHECK_LAUNCH("cisd_rdm1_kernel");
+  return TROT_OK;
+}
+
+/* One phaseless step with the CISD trial (trot/prop/afqmc.py:79-144 with the
+ * CISD meas ops): force bias and optional local energy of the incoming
+ * walkers, shifted fields, VHS, Taylor propagation with one-body half steps
+ * (FP64), CISD overlaps of the new walkers, phaseless weights, population
+ * shift.  `prop` supplies the propagation context (TROT_RHF_R, FP64). */
+int trot_cisd_prop_step(const trot_cisd* c, const trot_system* prop, const trot_state* state, const double* fields,
+                        double* energy_out, void* ws, size_t ws_bytes, void* stream) {
+  if (!prop || !state || !fields) { set_error("null system, state or fields"); return TROT_ERR_NULL_PTR; }
+  const int W = prop->n_walkers;
+  TROT_TRY(check_cisd(c, W));
+  if (prop->kind != TROT_RHF_R || prop->precision != TROT_FP64 || prop->norb != c->norb ||
+      prop->nchol != c->nchol || prop->nocc_a != c->nocc) {
+    set_error("CISD step: propagation context must be restricted FP64 with norb %d, nchol %d, nocc %d", c->norb,
+              c->nchol, c->nocc);
+    return TROT_ERR_BAD_SHAPE;
+  }
+  if (!prop->exp_h1_half || !prop->chol_flat || !prop->mf_shifts_im) {
+    set_error("CISD step: null propagation context array");
+    return TROT_ERR_NULL_PTR;
+  }
+  if (prop->n_exp_terms < 1 || prop->n_exp_terms > 16) { set_error("bad n_exp_terms"); return TROT_ERR_BAD_SHAPE; }
+  if (!state->walkers_a || !state->weights || !state->overlaps || !state->scalars || !state->node_encounters) {
+    set_error("null state buffer");
+    return TROT_ERR_NULL_PTR;
+  }
+  Carver cv(ws, ws_bytes);
+  CisdBuffers b;
+  carve_cisd(c, W, TROT_OP_PROP_STEP, cv, b);
+  if (!cv.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, cv.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N = c->norb, G = c->nchol;
+  double2* w = (double2*)state->walkers_a;
+  // 1. force bias (and local energy) of the incoming walkers
+  TROT_TRY(cisd_run(c, W, w, b, energy_out ? 2 : 1, st));
+  const size_t wg = (size_t)W * G;
+  cisd_fb_kernel<<<(unsigned)((wg + 255) / 256), 256, 0, st>>>(W, G, b.wsc, b.lg, b.lci1g, b.lci2g, b.fb);
+  TROT_CHECK_LAUNCH("cisd_fb_kernel");
+  if (energy_out) {
+    cisd_energy_kernel<<<W, 256, 0, st>>>(G, cisd_chunks(G), c->h0, b.wsc, b.hg2, b.lg, b.lci1g, b.lci2g, b.gpart,
+                                          (double2*)energy_out);
+    TROT_CHECK_LAUNCH("cisd_energy_kernel");
+  }
+  // 2. shifted fields, 3. VHS, 4. propagation in place
+  TROT_TIMED("fields", st,
+             launch_fields(W, G, prop->sqrt_dt, b.fb, prop->mf_shifts_im, fields, b.xs, b.shift_term, b.fb_term, st));
+  TROT_TIMED("vhs_fp64", st,
+             launch_zgemm_cr(W, N * N, G, 1.0, b.xs, G, prop->chol_flat, N * N, false, b.vhs, N * N, false, st));
+  Spins sp = make_spins(prop);
+  TrotterArgs a{};
+  a.W = W; a.N = N; a.G = G; a.nterms = prop->n_exp_terms; a.sqrt_dt = prop->sqrt_dt; a.expH = prop->exp_h1_half;
+  a.vhs = b.vhs; a.in_a = w; a.out_a = w;
+  TROT_TIMED("trotter_fp64", st, launch_trotter(sp, a, st));
+  // 5. CISD overlaps of the new walkers, weights, population shift
+  TROT_TRY(cisd_run(c, W, w, b, 0, st));
+  cisd_overlap_kernel<<<W, 256, 0, st>>>(c->nocc * c->nvir, b.x, b.cc, b.ce, b.wsc, b.det2, b.ov_new);
+  TROT_CHECK_LAUNCH("cisd_overlap_kernel");
+  a.overlaps = (double2*)state->overlaps; a.weights = state->weights; a.scalars = state->scalars;
+  a.shift_term = b.shift_term; a.fb_term = b.fb_term; a.node_flag = b.node_flag;
+  a.dt = prop->dt; a.h0_prop = prop->h0_prop; a.w_floor = prop->weight_floor; a.w_cap = prop->weight_cap;
+  cisd_weight_kernel<<<(W + 127) / 128, 128, 0, st>>>(a, b.ov_new);
+  TROT_CHECK_LAUNCH("cisd_weight_kernel");
+  TROT_TIMED("step_finalize", st,
+             launch_step_finalize(W, state->weights, state->scalars, (long long*)state->node_encounters, b.node_flag,
+                                  prop->pop_control_damping, prop->dt, st));
+  return TROT_OK;
+}
+
+}  // extern "C"

@@ -132,6 +132,13 @@ def afqmc_step(state: PropState, *, params, ham_data, trial_data, meas_ops: Meas
     None they are drawn on the device from ``state.rng_key`` (which is advanced).
     If ``energy_out`` (W,) complex128 is given it receives the local energy of
     the walkers entering the step."""
+    from .cisd import CisdTrial
+
+    if isinstance(trial_data, CisdTrial):
+        from . import cisd
+
+        return cisd.afqmc_step(state, params=params, ham_data=ham_data, trial_data=trial_data, meas_ctx=meas_ctx,
+                               prop_ctx=prop_ctx, fields=fields, energy_out=energy_out)
     kind = native.kind_of(trial_data, walker_kind)
     wa, wb = native.split_walkers(state.walkers, kind)
     W = wa.shape[0]
