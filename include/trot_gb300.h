@@ -90,6 +90,10 @@ typedef struct {
   int gpad;              /* G rounded up to 64 */
   const uint16_t* chol_t_slices; /* bf16 (vhs_slices, n2pad, gpad): row pq holds L[:, pq] */
   const float* exp_h1_half_f32;  /* (N, N) */
+  /* exp(-dt/2 h1_eff) as 3 BF16 slices in the tensor-core operand image
+   * (2 chunks x 3 slices x 128 rows x 64); when set, the Trotter action runs on
+   * the tensor cores (N <= 128, nocc_a + nocc_b <= 32), else in FP32. */
+  const uint16_t* exp_h1_half_img;
 } trot_mixed;
 
 /* Static description of one Hamiltonian + trial + propagation context.
@@ -243,8 +247,9 @@ int trot_local_energy_noalloc(const trot_system* sys, const double* walkers_a, c
  * whole space active: nocc + nvir == norb (no frozen core, no outer
  * virtuals).  All arrays are device float64, row-major:
  *   ci1      (nocc, nvir)                      c_ia
- *   ci2      (nocc*nvir, nocc*nvir)            c_iajb, row (i,a), column (j,b)
- *   ci2_perm (nocc*nvir, nocc*nvir)            ci2_perm[(i,b),(j,a)] = c_iajb
+ *   ci2m     (nocc*nvir, nocc*nvir)            2 c_iajb - c_ibja, row (i,a), column (j,b)
+ *            (every doubles contraction of the overlap, force bias and energy
+ *            uses c_iajb only in this combination)
  *   h1       (norb, norb), chol (nchol, norb, norb)
  *   lci1     (nchol, norb, nocc)               lci1[g][i][p] = sum_a chol[g][i][nocc+a] c_pa
  *   mo       (norb, nocc)                      the first nocc columns of I
@@ -254,17 +259,29 @@ typedef struct {
   int norb, nocc, nvir, nchol;
   double h0;
   const double* ci1;
-  const double* ci2;
-  const double* ci2_perm;
+  const double* ci2m;
   const double* h1;
   const double* chol;
   const double* lci1;
   const double* mo;
+  /* TROT_FP64, or TROT_MIXED: the l2ci2 quadratic forms on the tensor cores
+   * (3-term BF16 split, FP32 accumulation), as the reference computes them in
+   * float32 unless testing=True (trot/meas/cisd.py:838-839). */
+  int l2ci2_precision;
+  /* TROT_FP64, or TROT_MIXED: gl = G L_g and lci2_green in FP32 (the
+   * reference's mixed_precision=True float32 contractions). */
+  int gl_precision;
+  /* for l2ci2_precision == TROT_MIXED: ci2m (nocc nvir columns padded to
+   * ncpad, a multiple of 128; nocc nvir rows padded to nvpad, a multiple of
+   * 64) as 3 BF16 slices in the tensor-core operand image
+   * (trot_gb300.mixed.split3_image). */
+  int nvpad, ncpad;
+  const uint16_t* ci2_image;
 } trot_cisd;
 
 /* Device workspace for trot_cisd_overlap (TROT_OP_OVERLAP), trot_cisd_force_bias
  * (TROT_OP_FORCE_BIAS) or trot_cisd_local_energy (TROT_OP_LOCAL_ENERGY); 0 on bad
- * sizes.  The local energy needs 3 W nchol nocc nvir complex values for the
+ * sizes.  The local energy needs 2 W nchol nocc nvir complex values for the
  * l2ci2 quadratic forms. */
 size_t trot_cisd_workspace_size(const trot_cisd* cisd, int n_walkers, int op);
 /* walkers: complex128 (W, norb, nocc); out complex128 (W).

@@ -101,7 +101,7 @@ def test_workspace_size_monotone():
 def _cisd(**kw):
     c = _lib.TrotCisd()
     c.norb, c.nocc, c.nvir, c.nchol, c.h0 = 10, 3, 7, 12, 0.5
-    c.ci1 = c.ci2 = c.ci2_perm = c.h1 = c.chol = c.lci1 = c.mo = 0x1000
+    c.ci1 = c.ci2m = c.h1 = c.chol = c.lci1 = c.mo = 0x1000
     for k, v in kw.items():
         setattr(c, k, v)
     return c
@@ -113,8 +113,8 @@ def test_cisd_workspace_and_errors():
     sizes = [lib.trot_cisd_workspace_size(ctypes.byref(c), 8, op)
              for op in (_lib.OP_OVERLAP, _lib.OP_FORCE_BIAS, _lib.OP_LOCAL_ENERGY, _lib.OP_PROP_STEP)]
     assert 0 < sizes[0] < sizes[1] < sizes[2] < sizes[3]
-    # the local energy keeps 3 W G nocc nvir complex values for the l2ci2 quadratic forms
-    assert sizes[2] - sizes[1] >= 3 * 8 * 12 * 21 * 16
+    # the local energy keeps 2 W G nocc nvir complex values for the l2ci2 quadratic form
+    assert sizes[2] - sizes[1] >= 2 * 8 * 12 * 21 * 16
     assert lib.trot_cisd_workspace_size(ctypes.byref(c), 800, _lib.OP_LOCAL_ENERGY) > sizes[2]
     assert lib.trot_cisd_workspace_size(ctypes.byref(c), 8, _lib.OP_QR) == 0
     assert lib.trot_cisd_workspace_size(ctypes.byref(_cisd(nvir=6)), 8, _lib.OP_OVERLAP) == 0

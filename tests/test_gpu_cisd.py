@@ -22,7 +22,7 @@ def _cuda():
 
 
 class CisdSetup:
-    def __init__(self, h0, h1, chol, ci1, ci2, W, dt=0.005):
+    def __init__(self, h0, h1, chol, ci1, ci2, W, dt=0.005, mixed=False):
         import trot_gb300 as tg
 
         N, n = h1.shape[0], ci1.shape[0]
@@ -30,7 +30,10 @@ class CisdSetup:
         self.ham = tg.HamChol(h0=h0, h1=h1, chol=chol)
         self.trial = tg.CisdTrial(ci1, ci2)
         self.trial_ops = tg.make_cisd_trial_ops(self.sys)
-        self.meas_ops = tg.make_cisd_meas_ops(self.sys, memory_mode="high", mixed_precision=False, testing=True)
+        if mixed:  # the reference's defaults: float32 gl / l2ci2
+            self.meas_ops = tg.make_cisd_meas_ops(self.sys)
+        else:
+            self.meas_ops = tg.make_cisd_meas_ops(self.sys, memory_mode="high", mixed_precision=False, testing=True)
         self.meas_ctx = self.meas_ops.build_meas_ctx(self.ham, self.trial)
         self.params = tg.QmcParams(dt=dt, n_walkers=W, n_exp_terms=6, seed=3)
         self.prop_ops = tg.make_prop_ops("restricted", "restricted")
@@ -80,6 +83,26 @@ def test_cisd_vs_oracle(N, n, G, W, noise):
     assert rel(cpu(S.force_bias(wd)), co.force_bias(w, tr, cs.chol)) <= TOL
     assert rel(cpu(S.energy(wd)), co.energy(w, tr, cs.h0, cs.h1, cs.chol)) <= TOL
     assert rel(cpu(S.rdm1(wd))[:, 0], co.rdm1(w, tr)) <= TOL
+
+
+@pytest.mark.parametrize("N,n,G,W,noise", [(60, 8, 300, 6, 0.1), (31, 6, 70, 37, 0.3), (44, 11, 130, 5, 0.2),
+                                           (9, 2, 11, 3, 0.05), (31, 6, 70, 37, 0.1)])
+def test_cisd_mixed_energy(N, n, G, W, noise):
+    """Reference-default meas ops (tensor-core l2ci2 and FP32 gl, FP32-level like the
+    reference's float32 there).  Per walker against the FP64 path: |dE_L| <= 1e-5 Ha
+    for walkers near the trial (noise <= 0.1); for strongly perturbed walkers
+    |dE_L| <= 1e-5 max|E_L| (observed 2.3e-6 relative at noise 0.3).  Force bias and
+    overlaps are computed in FP64 either way."""
+    cs, w = _synthetic(N, n, G, W, noise)
+    F = CisdSetup(cs.h0, cs.h1, cs.chol, cs.ci1, cs.ci2, W)
+    M = CisdSetup(cs.h0, cs.h1, cs.chol, cs.ci1, cs.ci2, W, mixed=True)
+    wd = dev(w)
+    e64, emx = cpu(F.energy(wd)), cpu(M.energy(wd))
+    err = np.max(np.abs(emx - e64))
+    bound = 1e-5 if noise <= 0.1 else 1e-5 * np.max(np.abs(e64))
+    assert err <= bound, (err, bound)
+    assert rel(cpu(M.force_bias(wd)), cpu(F.force_bias(wd))) <= 1e-12
+    assert rel(cpu(M.overlap(wd)), cpu(F.overlap(wd))) <= 1e-14
 
 
 def test_cisd_step_and_block_vs_oracle():

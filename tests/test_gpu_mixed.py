@@ -106,3 +106,23 @@ def test_mixed_energy_many_walker_tiles(kind, N, nelec, G, W):
     emx = cpu(M.energy(w))
     assert np.max(np.abs(emx - e64)) <= 1e-5
     assert rel(cpu(M.force_bias(w)), cpu(F.force_bias(w))) <= 1e-9
+
+
+@pytest.mark.parametrize("kind,N,nelec,G,W", [("uhf_u", 64, (9, 7), 128, 300), ("rhf_r", 100, (16, 16), 200, 160),
+                                              ("rhf_u", 128, (16, 16), 150, 40)])
+def test_mixed_trotter_many_walkers(kind, N, nelec, G, W):
+    """Tensor-core Taylor action over several waves of CTAs and at the largest
+    supported tile (N = 128, 32 occupied columns)."""
+    import trot_gb300 as tg
+
+    ss, walkers, F, M = _setups(kind, N, nelec, G, W, 30.0, 0.1)
+    rng = np.random.default_rng(6)
+    xs = dev(rng.normal(size=(W, G)) + 0.3j * rng.normal(size=(W, G)))
+    w = F.walkers(walkers)
+    o64 = tg.make_trotter_ops("restricted", F.walker_kind).apply_trotter(w, xs, F.prop_ctx, 6)
+    omx = tg.make_trotter_ops("restricted", F.walker_kind, mixed_precision=True).apply_trotter(w, xs, M.prop_ctx, 6)
+    if kind == "rhf_r":
+        assert rel(cpu(omx), cpu(o64)) <= 2e-5
+    else:
+        assert rel(cpu(omx[0]), cpu(o64[0])) <= 2e-5
+        assert rel(cpu(omx[1]), cpu(o64[1])) <= 2e-5

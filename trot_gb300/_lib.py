@@ -36,6 +36,7 @@ class TrotMixed(ctypes.Structure):
         ("slices", _i), ("max_order", _i), ("kpad", _i), ("gammas_per_block", _i * 2), ("n_blocks", _i * 2),
         ("rot_slices", _p * 2), ("rot_exp", _p * 2), ("vhs_slices", _i), ("vhs_order", _i), ("n2pad", _i),
         ("gpad", _i), ("chol_t_slices", _p), ("exp_h1_half_f32", _p),
+        ("exp_h1_half_img", _p),
     ]
 
 
@@ -67,7 +68,8 @@ class TrotCisd(ctypes.Structure):
 
     _fields_ = [
         ("norb", _i), ("nocc", _i), ("nvir", _i), ("nchol", _i), ("h0", _d),
-        ("ci1", _p), ("ci2", _p), ("ci2_perm", _p), ("h1", _p), ("chol", _p), ("lci1", _p), ("mo", _p),
+        ("ci1", _p), ("ci2m", _p), ("h1", _p), ("chol", _p), ("lci1", _p), ("mo", _p),
+        ("l2ci2_precision", _i), ("gl_precision", _i), ("nvpad", _i), ("ncpad", _i), ("ci2_image", _p),
     ]
 
 

@@ -4,9 +4,15 @@ on the CUDA library.
 The trial, meas ops and trial ops keep the reference's names and call
 signatures; every kernel takes the whole walker batch and makes one call into
 the C ABI (``trot_cisd_*`` in include/trot_gb300.h).  The whole orbital
-space is active (``nocc_t_core == nvir_t_outer == 0``); the contractions run
-in float64 whatever ``mixed_precision`` asks for (the reference's float64
-``testing=True`` numbers).
+space is active (``nocc_t_core == nvir_t_outer == 0``).
+
+Precision follows the reference's two switches (trot/meas/cisd.py:823-839):
+``testing=True`` keeps every contraction in float64 (the reference's float64
+``*_testing`` dtypes); with ``testing=False`` the l2ci2 quadratic forms run on
+the tensor cores (3-term BF16 split, FP32 accumulation; the reference uses
+float32 there).  ``mixed_precision=True`` computes gl = G L_g and lci2_green
+in FP32 (the reference's float32 ``mixed_real_dtype``); overlaps, ci2g, the
+Cholesky contractions and every energy sum stay float64.
 """
 from __future__ import annotations
 
@@ -77,8 +83,8 @@ class CisdTrial:
 
 
 def _trial_dev(trial: CisdTrial) -> dict:
-    """Device operands derived once per trial: ci2 as an (nv, nv) matrix and its
-    exchange permutation ci2_perm[(i,b),(j,a)] = ci2[i,a,j,b]."""
+    """Device operands derived once per trial: ci2m[(i,a),(j,b)] = 2 c_iajb - c_ibja
+    as an (nv, nv) matrix, the only combination of the doubles the kernels use."""
     d = trial.__dict__.get("_dev")
     if d is None:
         if trial.nocc_t_core != 0 or trial.nvir_t_outer != 0:
@@ -86,8 +92,7 @@ def _trial_dev(trial: CisdTrial) -> dict:
         n, v = trial.nocc, trial.nvir
         d = {
             "ci1": trial.ci1.contiguous(),
-            "ci2": trial.ci2.reshape(n * v, n * v).contiguous(),
-            "ci2_perm": trial.ci2.permute(0, 3, 2, 1).reshape(n * v, n * v).contiguous(),
+            "ci2m": (2.0 * trial.ci2 - trial.ci2.permute(0, 3, 2, 1)).reshape(n * v, n * v).contiguous(),
             "mo": torch.eye(n + v, dtype=torch.float64, device=trial.ci1.device)[:, :n].contiguous(),
         }
         object.__setattr__(trial, "_dev", d)
@@ -122,6 +127,9 @@ class CisdMeasCtx:
     h1: torch.Tensor
     chol: torch.Tensor
     h0: float
+    ci2_image: torch.Tensor | None = None  # ci2m split-BF16 image (testing=False)
+    nvpad: int = 0
+    ncpad: int = 0
 
 
 def build_meas_ctx(ham_data: HamChol, trial_data: CisdTrial, cfg: CisdMeasCfg = CisdMeasCfg()) -> CisdMeasCtx:
@@ -135,20 +143,31 @@ def build_meas_ctx(ham_data: HamChol, trial_data: CisdTrial, cfg: CisdMeasCfg = 
     n = trial_data.nocc_full
     lci1 = torch.einsum("git,pt->gip", chol[:, :, trial_data.vir_act_slice], trial_data.ci1).contiguous()
     h0 = ham_data.h0.item() if isinstance(ham_data.h0, torch.Tensor) else ham_data.h0
+    img, ncpad, nvpad = None, 0, 0
+    if not cfg.testing:
+        from . import mixed
+
+        bt = _trial_dev(trial_data)["ci2m"].T.cpu().numpy()  # (nv columns, nv K)
+        img, ncpad, nvpad = mixed.split3_image(bt)
+        img = img.to(chol.device)
     return CisdMeasCtx(rot_chol=chol[:, :n, :], lci1=lci1, cfg=cfg, h1=h1, chol=chol,
-                       h0=float(np.real(np.asarray(h0))))
+                       h0=float(np.real(np.asarray(h0))), ci2_image=img, nvpad=nvpad, ncpad=ncpad)
 
 
 def _struct(trial: CisdTrial, meas_ctx: CisdMeasCtx | None) -> _lib.TrotCisd:
     d = _trial_dev(trial)
     c = _lib.TrotCisd()
     c.norb, c.nocc, c.nvir = trial.norb, trial.nocc, trial.nvir
-    c.ci1, c.ci2, c.ci2_perm, c.mo = (native.ptr(d[k]) for k in ("ci1", "ci2", "ci2_perm", "mo"))
+    c.ci1, c.ci2m, c.mo = (native.ptr(d[k]) for k in ("ci1", "ci2m", "mo"))
     c.nchol = 1
     if meas_ctx is not None:
         c.nchol = int(meas_ctx.chol.shape[0])
         c.h0 = meas_ctx.h0
         c.h1, c.chol, c.lci1 = native.ptr(meas_ctx.h1), native.ptr(meas_ctx.chol), native.ptr(meas_ctx.lci1)
+        c.gl_precision = _lib.MIXED if meas_ctx.cfg.mixed_precision else _lib.FP64
+        if meas_ctx.ci2_image is not None:
+            c.l2ci2_precision = _lib.MIXED
+            c.ci2_image, c.nvpad, c.ncpad = meas_ctx.ci2_image.data_ptr(), meas_ctx.nvpad, meas_ctx.ncpad
     return c
 
 

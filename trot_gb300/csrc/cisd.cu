@@ -2,17 +2,19 @@
 // in the trial's MO basis (reference determinant = orbitals [0, n)).
 //
 // Restated from trot/trial/cisd.py:148-186 and trot/meas/cisd.py:548-769
-// ("high" memory mode, float64 contractions).  With x = G[:, n:] (n x v),
-// C_c = x . ci2 and C_e = x . ci2_perm (ci2_perm[(p,u),(q,t)] = ci2[p,t,q,u]):
-//   ci2g = 2 C_c - C_e,  gci2g = sum ci2g o x,  ci1g = sum ci1 o x,
+// ("high" memory mode, float64 contractions).  With x = G[:, n:] (n x v) and
+// ci2m[(p,t),(q,u)] = 2 ci2[p,t,q,u] - ci2[p,u,q,t] (the reference's
+// 2 ci2g_c - ci2g_e, 2 l2ci2_1 - l2ci2_2 and direct - exchange combinations):
+//   ci2g = x . ci2m,  gci2g = sum ci2g o x,  ci1g = sum ci1 o x,
 //   ov = 1 + 2 ci1g + gci2g        (overlap = ov det(w_occ)^2)
 //   ci1_green = (gp ci1^T) G,  ci2_green = (gp ci2g^T) G   (N x N; gp rows < n: x, rows >= n: -I)
 //   force bias = (2 lg + 4 ci1g lg + 2 gci2g lg - 2 (lci1g + lci2g)) / ov
 //     with lg = rot_chol . G, lci{1,2}g = chol . ci{1,2}_green
 //   local energy: the terms of energy_kernel_rw_rh, see cisd_energy_combine.
-// The l2ci2 quadratic forms sum_g X_g^T ci2 X_g and X_g^T ci2_perm X_g
-// (X_g = vec(glgp_g)) are two GEMMs over all (walker, g) rows.
+// The l2ci2 quadratic forms 2 sum_g X_g^T ci2 X_g - X_g^T ci2_perm X_g (ci2_perm[(p,u),(q,t)] = ci2[p,t,q,u])
+// = sum_g X_g^T ci2m X_g (X_g = vec(glgp_g)) are one GEMM over all (walker, g) rows.
 #include "kernels.h"
+#include "mixed.h"
 
 #include "profile.h"
 #include "step_tail.cuh"
@@ -21,15 +23,18 @@ namespace trot {
 
 // ------------------------------------------------------------------ workspace
 struct CisdBuffers {
+  int* status;                  // device status word (offset 0 of the workspace)
   double2 *green, *det2, *hg2;  // G (W, n, N); det(w_occ)^2 (W); 2 hg (W)
   double2* x;                   // (W, n v) contiguous x
-  double2 *cc, *ce;             // (W, n v)
+  double2* cg;                  // ci2g = x ci2m (W, n v)
   double2* ci1g1;               // (W, n, n)
   double2 *m1, *m2;             // ci1_green, ci2_green (W, N, N)
   double2* wsc;                 // per-walker scalars (W, 8): ci1g, gci2g, e1_1_2, e1_2_2, ...
   double2 *lg, *lci1g, *lci2g;  // (W, G)
   double2* xg;                  // glgp rows (W G, n v)
-  double2 *y1, *y2;             // (W G, n v)
+  double2* y;                   // xg ci2m (W G, n v)    (FP64 l2ci2)
+  uint16_t* xq;                 // split3 image of xg    (mixed l2ci2)
+  float* yd;                    // xg ci2m, FP32         (mixed l2ci2)
   double2* gpart;               // per (walker, gamma chunk) partial sums (W, nchunk, 4)
   // propagation step
   double2 *fb, *xs, *shift_term, *fb_term, *vhs, *ov_new;
@@ -42,12 +47,12 @@ static int cisd_chunks(int G) { return (G + kCisdGChunk - 1) / kCisdGChunk; }
 static size_t carve_cisd(const trot_cisd* c, int W, int op, Carver& cv, CisdBuffers& b) {
   const size_t N = c->norb, n = c->nocc, v = c->nvir, G = c->nchol, nv = n * v;
   b = CisdBuffers{};
+  b.status = cv.take<int>(4);
   b.green = cv.take<double2>(W * n * N);
   b.det2 = cv.take<double2>(W);
   b.hg2 = cv.take<double2>(W);
   b.x = cv.take<double2>(W * nv);
-  b.cc = cv.take<double2>(W * nv);
-  b.ce = cv.take<double2>(W * nv);
+  b.cg = cv.take<double2>(W * nv);
   b.wsc = cv.take<double2>(W * 8);
   if (op == TROT_OP_OVERLAP) return cv.used;
   b.ci1g1 = cv.take<double2>(W * n * n);
@@ -58,8 +63,13 @@ static size_t carve_cisd(const trot_cisd* c, int W, int op, Carver& cv, CisdBuff
   b.lci2g = cv.take<double2>(W * G);
   if (op == TROT_OP_FORCE_BIAS) return cv.used;
   b.xg = cv.take<double2>((size_t)W * G * nv);
-  b.y1 = cv.take<double2>((size_t)W * G * nv);
-  b.y2 = cv.take<double2>((size_t)W * G * nv);
+  if (c->l2ci2_precision == TROT_MIXED) {
+    const size_t mpad = split3_mpad((int)(W * G));
+    b.xq = cv.take<uint16_t>(3 * mpad * (size_t)c->nvpad);
+    b.yd = cv.take<float>(mpad * (size_t)c->ncpad);
+  } else {
+    b.y = cv.take<double2>((size_t)W * G * nv);
+  }
   b.gpart = cv.take<double2>((size_t)W * cisd_chunks((int)G) * 4);
   if (op != TROT_OP_PROP_STEP) return cv.used;
   b.fb = cv.take<double2>((size_t)W * G);
@@ -99,11 +109,11 @@ __global__ void cisd_x_kernel(int N, int n, int v, const double2* __restrict__ g
 }
 
 // ------------------------------------------------------------------ per-walker N x N matrices
-// ci2g = 2 cc - ce; gci2g = sum ci2g o x; P_Y = gp Y^T (N x n); M = P_Y G (N x N) for Y = ci1, ci2g;
+// gci2g = sum ci2g o x; P_Y = gp Y^T (N x n); M = P_Y G (N x N) for Y = ci1, ci2g;
 // e1_1_2 = -2 sum h1 o M1, e1_2_2 = -2 sum h1 o M2.
 __global__ void __launch_bounds__(256)
 cisd_mats_kernel(int N, int n, int v, const double2* __restrict__ green, const double* __restrict__ ci1,
-                 const double2* __restrict__ cc, const double2* __restrict__ ce, const double2* __restrict__ x,
+                 const double2* __restrict__ cg, const double2* __restrict__ x,
                  const double* __restrict__ h1, double2* __restrict__ m1, double2* __restrict__ m2,
                  double2* __restrict__ wsc) {
   extern __shared__ double2 sm[];
@@ -117,8 +127,7 @@ cisd_mats_kernel(int N, int n, int v, const double2* __restrict__ green, const d
   for (int e = tid; e < n * N; e += nt) Gs[e] = g[e];
   double2 gs = cmk(0.0, 0.0);
   for (int e = tid; e < n * v; e += nt) {
-    const double2 c = cc[(size_t)b * n * v + e], d = ce[(size_t)b * n * v + e];
-    const double2 y = cmk(2.0 * c.x - d.x, 2.0 * c.y - d.y);
+    const double2 y = cg[(size_t)b * n * v + e];
     Y2[e] = y;
     cfma(gs, y, x[(size_t)b * n * v + e]);
   }
@@ -251,16 +260,139 @@ cisd_gamma_kernel(int N, int n, int v, int G, const double2* __restrict__ green,
   }
 }
 
-// l2ci2: per walker sum over g of X_g . (2 Y1_g - Y2_g)  -> wsc[b][6]
-__global__ void cisd_l2_reduce_kernel(int G, int nv, const double2* __restrict__ xg, const double2* __restrict__ y1,
-                                      const double2* __restrict__ y2, double2* __restrict__ wsc) {
+// Same sums as cisd_gamma_kernel with gl = G L and lci2_green = R M2^T in FP32
+// (float2 x float products, FP64 accumulation of the sums); lg1 and its terms stay FP64.
+__global__ void __launch_bounds__(256)
+cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ green, const double* __restrict__ chol,
+                      const double* __restrict__ lci1, const double2* __restrict__ m2,
+                      const double2* __restrict__ ci1g1, double2* __restrict__ xg, double2* __restrict__ gpart) {
+  extern __shared__ double2 sm[];
+  __shared__ double2 red[32];
+  const int chunk = blockIdx.x, b = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
+  const int nchunk = gridDim.x;
+  double2* Gs = sm;                                      // n x N (FP64)
+  double2* C1 = Gs + n * N;                              // n x n
+  double2* A = C1 + n * n;                               // n x n  (lg1)
+  double* Rd = reinterpret_cast<double*>(A + n * n);     // n x N  (rows < n of L_g)
+  float2* Gf = reinterpret_cast<float2*>(Rd + n * N);    // n x N
+  float2* M2f = Gf + n * N;                              // N x N
+  float2* GLf = M2f + N * N;                             // n x N
+  float* Lf = reinterpret_cast<float*>(GLf + n * N);     // N x N
+  for (int e = tid; e < n * N; e += nt) {
+    const double2 g = green[(size_t)b * n * N + e];
+    Gs[e] = g;
+    Gf[e] = make_float2((float)g.x, (float)g.y);
+  }
+  for (int e = tid; e < N * N; e += nt) {
+    const double2 m = m2[(size_t)b * N * N + e];
+    M2f[e] = make_float2((float)m.x, (float)m.y);
+  }
+  for (int e = tid; e < n * n; e += nt) C1[e] = ci1g1[(size_t)b * n * n + e];
+  double2 s0 = cmk(0.0, 0.0), s1 = cmk(0.0, 0.0), s2 = cmk(0.0, 0.0), s3 = cmk(0.0, 0.0);
+  const int g0 = chunk * kCisdGChunk, g1 = min(G, g0 + kCisdGChunk);
+  for (int gg = g0; gg < g1; ++gg) {
+    __syncthreads();
+    const double* Lg = chol + (size_t)gg * N * N;
+    for (int e = tid; e < N * N; e += nt) {
+      const double l = Lg[e];
+      Lf[e] = (float)l;
+      if (e < n * N) Rd[e] = l;
+    }
+    __syncthreads();
+    for (int e = tid; e < n * n; e += nt) {
+      const int p = e / n, q = e % n;
+      double2 a = cmk(0.0, 0.0);
+      for (int j = 0; j < N; ++j) crfma(a, Rd[p * N + j], Gs[q * N + j]);
+      A[e] = a;
+    }
+    for (int e = tid; e < n * N; e += nt) {
+      const int p = e / N, i = e % N;
+      float ar = 0.f, ai = 0.f;
+      for (int j = 0; j < N; ++j) {
+        const float l = Lf[j * N + i];
+        const float2 g = Gf[p * N + j];
+        ar = fmaf(l, g.x, ar);
+        ai = fmaf(l, g.y, ai);
+      }
+      GLf[e] = make_float2(ar, ai);
+    }
+    __syncthreads();
+    const double* lc = lci1 + (size_t)gg * N * n;
+    for (int e = tid; e < n * n; e += nt) {
+      const int p = e / n, q = e % n;
+      cfma(s0, A[p * n + q], A[q * n + p]);
+      double2 t = cmk(0.0, 0.0);
+      for (int a2 = 0; a2 < n; ++a2) cfma(t, A[q * n + a2], C1[a2 * n + p]);
+      cfma(s1, A[p * n + q], t);
+      double2 bq = cmk(0.0, 0.0);
+      for (int i = 0; i < N; ++i) crfma(bq, lc[i * n + q], Gs[p * N + i]);
+      cfma(s2, bq, A[p * n + q]);
+    }
+    for (int e = tid; e < n * N; e += nt) {
+      const int p = e / N, j = e % N;
+      float ar = 0.f, ai = 0.f;
+      for (int i = 0; i < N; ++i) {
+        const float l = Lf[p * N + i];
+        const float2 m = M2f[j * N + i];
+        ar = fmaf(l, m.x, ar);
+        ai = fmaf(l, m.y, ai);
+      }
+      const float2 gl = GLf[e];
+      s3.x += (double)gl.x * ar - (double)gl.y * ai;
+      s3.y += (double)gl.x * ai + (double)gl.y * ar;
+    }
+    double2* xo = xg + ((size_t)b * G + gg) * n * v;
+    for (int e = tid; e < n * v; e += nt) {
+      const int p = e / v, t = e % v;
+      const float2 gl = GLf[p * N + n + t];
+      float ar = -gl.x, ai = -gl.y;
+      for (int i = 0; i < n; ++i) {
+        const float2 a = GLf[p * N + i], x = Gf[i * N + n + t];
+        ar = fmaf(a.x, x.x, fmaf(-a.y, x.y, ar));
+        ai = fmaf(a.x, x.y, fmaf(a.y, x.x, ai));
+      }
+      xo[e] = cmk(ar, ai);
+    }
+  }
+  s0 = block_sum2(s0, red);
+  s1 = block_sum2(s1, red);
+  s2 = block_sum2(s2, red);
+  s3 = block_sum2(s3, red);
+  if (tid == 0) {
+    double2* o = gpart + ((size_t)b * nchunk + chunk) * 4;
+    o[0] = s0; o[1] = s1; o[2] = s2; o[3] = s3;
+  }
+}
+
+// l2ci2 from the tensor-core product: Y = xg ci2m in FP32, rows 2r (Re) / 2r+1 (Im) of yd
+// (row stride ldy); per walker sum over g of X_g . Y_g, FP64 accumulation.
+__global__ void cisd_l2_reduce_tc_kernel(int G, int nv, int ldy, const double2* __restrict__ xg,
+                                         const float* __restrict__ yd, double2* __restrict__ wsc) {
+  __shared__ double2 red[32];
+  const int b = blockIdx.x;
+  double2 acc = cmk(0.0, 0.0);
+  const size_t cnt = (size_t)G * nv;
+  for (size_t e = threadIdx.x; e < cnt; e += blockDim.x) {
+    const size_t r = (size_t)b * G + e / nv;
+    const int k = (int)(e % nv);
+    const double2 xv = xg[r * nv + k];
+    const float* yr = yd + 2 * r * (size_t)ldy;
+    const float* yi = yr + ldy;
+    cfma(acc, xv, cmk((double)yr[k], (double)yi[k]));
+  }
+  acc = block_sum2(acc, red);
+  if (threadIdx.x == 0) wsc[(size_t)b * 8 + 6] = acc;
+}
+
+// l2ci2: per walker sum over g of X_g . Y_g, Y = xg ci2m  -> wsc[b][6]
+__global__ void cisd_l2_reduce_kernel(int G, int nv, const double2* __restrict__ xg, const double2* __restrict__ y,
+                                      double2* __restrict__ wsc) {
   __shared__ double2 red[32];
   const int b = blockIdx.x;
   double2 acc = cmk(0.0, 0.0);
   const size_t base = (size_t)b * G * nv, cnt = (size_t)G * nv;
   for (size_t e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const double2 xv = xg[base + e], a = y1[base + e], c = y2[base + e];
-    cfma(acc, xv, cmk(2.0 * a.x - c.x, 2.0 * a.y - c.y));
+    cfma(acc, xg[base + e], y[base + e]);
   }
   acc = block_sum2(acc, red);
   if (threadIdx.x == 0) wsc[(size_t)b * 8 + 6] = acc;
@@ -273,17 +405,16 @@ __device__ __forceinline__ double2 cdot_row(const double2* a, const double2* b, 
   return s;
 }
 
-// overlap = (1 + 2 ci1g + gci2g) det0^2, gci2g = sum (2 C_c - C_e) o x; one CTA per walker
-__global__ void cisd_overlap_kernel(int nv, const double2* __restrict__ x, const double2* __restrict__ cc,
-                                    const double2* __restrict__ ce, const double2* __restrict__ wsc,
+// overlap = (1 + 2 ci1g + gci2g) det0^2, gci2g = sum ci2g o x; one CTA per walker
+__global__ void cisd_overlap_kernel(int nv, const double2* __restrict__ x, const double2* __restrict__ cg,
+                                    const double2* __restrict__ wsc,
                                     const double2* __restrict__ det2, double2* __restrict__ out) {
   __shared__ double2 red[32];
   const int b = blockIdx.x;
   double2 gs = cmk(0.0, 0.0);
   for (int e = threadIdx.x; e < nv; e += blockDim.x) {
     const size_t k = (size_t)b * nv + e;
-    const double2 c = cc[k], d = ce[k];
-    cfma(gs, cmk(2.0 * c.x - d.x, 2.0 * c.y - d.y), x[k]);
+    cfma(gs, cg[k], x[k]);
   }
   gs = block_sum2(gs, red);
   if (threadIdx.x == 0) {
@@ -378,6 +509,11 @@ static size_t cisd_gamma_smem(int N, int n) {
   return (size_t)(2 * n * N + N * N + 2 * n * n) * sizeof(double2) + (size_t)N * N * sizeof(double);
 }
 
+static size_t cisd_gamma_f32_smem(int N, int n) {
+  return (size_t)(n * N + 2 * n * n) * sizeof(double2) + (size_t)n * N * sizeof(double) +
+         (size_t)(2 * n * N + N * N) * sizeof(float2) + (size_t)N * N * sizeof(float);
+}
+
 // need_ham: the force bias / energy / step also read h1, chol and lci1
 static int check_cisd(const trot_cisd* c, int W, bool need_ham = true) {
   if (!c) { set_error("null CISD context"); return TROT_ERR_NULL_PTR; }
@@ -387,9 +523,22 @@ static int check_cisd(const trot_cisd* c, int W, bool need_ham = true) {
               c->nchol);
     return TROT_ERR_BAD_SHAPE;
   }
-  if (!c->ci1 || !c->ci2 || !c->ci2_perm || !c->mo || (need_ham && (!c->h1 || !c->chol || !c->lci1))) {
+  if (!c->ci1 || !c->ci2m || !c->mo || (need_ham && (!c->h1 || !c->chol || !c->lci1))) {
     set_error("null CISD context array");
     return TROT_ERR_NULL_PTR;
+  }
+  if ((c->l2ci2_precision != TROT_FP64 && c->l2ci2_precision != TROT_MIXED) ||
+      (c->gl_precision != TROT_FP64 && c->gl_precision != TROT_MIXED)) {
+    set_error("CISD: bad precision selector");
+    return TROT_ERR_BAD_DTYPE;
+  }
+  if (need_ham && c->l2ci2_precision == TROT_MIXED) {
+    const int nv = c->nocc * c->nvir;
+    if (!c->ci2_image) { set_error("CISD: mixed l2ci2 needs ci2_image"); return TROT_ERR_NULL_PTR; }
+    if (c->nvpad < nv || c->nvpad % 64 || c->ncpad < nv || c->ncpad % 128) {
+      set_error("CISD: ci2_image padding nvpad=%d ncpad=%d for nocc*nvir=%d", c->nvpad, c->ncpad, nv);
+      return TROT_ERR_BAD_SHAPE;
+    }
   }
   if (c->nocc > 64 || cisd_mats_smem(c->norb, c->nocc, c->nvir) > 200 * 1024 ||
       cisd_gamma_smem(c->norb, c->nocc) > 200 * 1024) {
@@ -417,16 +566,16 @@ static Spins cisd_spins(const trot_cisd* c) {
 static int cisd_run(const trot_cisd* c, int W, const double2* w, CisdBuffers& b, int stage, cudaStream_t st) {
   const int N = c->norb, n = c->nocc, v = c->nvir, G = c->nchol, nv = n * v;
   Spins sp = cisd_spins(c);
+  if (stage > 0) cudaMemsetAsync(b.status, 0, 4 * sizeof(int), st);
   TROT_TIMED("cisd_green", st, launch_green(sp, W, N, w, nullptr, b.green, b.det2, b.hg2, st));
   cisd_x_kernel<<<W, 256, 0, st>>>(N, n, v, b.green, c->ci1, b.x, stage >= 1 ? b.ci1g1 : nullptr, b.wsc);
   TROT_CHECK_LAUNCH("cisd_x_kernel");
-  TROT_TIMED("cisd_ci2g", st, launch_zgemm_cr(W, nv, nv, 1.0, b.x, nv, c->ci2, nv, false, b.cc, nv, false, st));
-  TROT_TRY(launch_zgemm_cr(W, nv, nv, 1.0, b.x, nv, c->ci2_perm, nv, false, b.ce, nv, false, st));
+  TROT_TIMED("cisd_ci2g", st, launch_zgemm_cr(W, nv, nv, 1.0, b.x, nv, c->ci2m, nv, false, b.cg, nv, false, st));
   if (stage == 0) return TROT_OK;
   const size_t smem = cisd_mats_smem(N, n, v);
   if (smem > 48 * 1024) cudaFuncSetAttribute(cisd_mats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   TROT_TIMED("cisd_mats", st, ([&]() -> int {
-    cisd_mats_kernel<<<W, 256, smem, st>>>(N, n, v, b.green, c->ci1, b.cc, b.ce, b.x, c->h1, b.m1, b.m2, b.wsc);
+    cisd_mats_kernel<<<W, 256, smem, st>>>(N, n, v, b.green, c->ci1, b.cg, b.x, c->h1, b.m1, b.m2, b.wsc);
     TROT_CHECK_LAUNCH("cisd_mats_kernel");
     return TROT_OK;
   })());
@@ -437,19 +586,36 @@ static int cisd_run(const trot_cisd* c, int W, const double2* w, CisdBuffers& b,
   TROT_TRY(launch_zgemm_cr(W, G, N * N, 1.0, b.m2, N * N, c->chol, N * N, true, b.lci2g, G, false, st));
   if (stage == 1) return TROT_OK;
   const int nch = cisd_chunks(G);
-  const size_t smem2 = cisd_gamma_smem(N, n);
-  cudaFuncSetAttribute(cisd_gamma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
-  TROT_TIMED("cisd_gamma", st, ([&]() -> int {
-    cisd_gamma_kernel<<<dim3(nch, W), 256, smem2, st>>>(N, n, v, G, b.green, c->chol, c->lci1, b.m2, b.ci1g1, b.xg,
-                                                       b.gpart);
-    TROT_CHECK_LAUNCH("cisd_gamma_kernel");
+  if (c->gl_precision == TROT_MIXED) {
+    const size_t smem2 = cisd_gamma_f32_smem(N, n);
+    cudaFuncSetAttribute(cisd_gamma_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+    TROT_TIMED("cisd_gamma_f32", st, ([&]() -> int {
+      cisd_gamma_f32_kernel<<<dim3(nch, W), 256, smem2, st>>>(N, n, v, G, b.green, c->chol, c->lci1, b.m2, b.ci1g1,
+                                                             b.xg, b.gpart);
+      TROT_CHECK_LAUNCH("cisd_gamma_f32_kernel");
+      return TROT_OK;
+    })());
+  } else {
+    const size_t smem2 = cisd_gamma_smem(N, n);
+    cudaFuncSetAttribute(cisd_gamma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+    TROT_TIMED("cisd_gamma", st, ([&]() -> int {
+      cisd_gamma_kernel<<<dim3(nch, W), 256, smem2, st>>>(N, n, v, G, b.green, c->chol, c->lci1, b.m2, b.ci1g1,
+                                                         b.xg, b.gpart);
+      TROT_CHECK_LAUNCH("cisd_gamma_kernel");
+      return TROT_OK;
+    })());
+  }
+  if (c->l2ci2_precision == TROT_MIXED) {
+    TROT_TIMED("cisd_l2ci2_tc", st,
+               launch_split3_gemm(W * G, nv, c->nvpad, c->ncpad, b.xg, c->ci2_image, b.xq, b.yd, b.status, st));
+    cisd_l2_reduce_tc_kernel<<<W, 256, 0, st>>>(G, nv, c->ncpad, b.xg, b.yd, b.wsc);
+    TROT_CHECK_LAUNCH("cisd_l2_reduce_tc_kernel");
     return TROT_OK;
-  })());
+  }
   if ((size_t)W * G > 65535u * 64u) { set_error("CISD: W*G too large"); return TROT_ERR_UNSUPPORTED; }
   TROT_TIMED("cisd_l2ci2", st,
-             launch_zgemm_cr(W * G, nv, nv, 1.0, b.xg, nv, c->ci2, nv, false, b.y1, nv, false, st));
-  TROT_TRY(launch_zgemm_cr(W * G, nv, nv, 1.0, b.xg, nv, c->ci2_perm, nv, false, b.y2, nv, false, st));
-  cisd_l2_reduce_kernel<<<W, 256, 0, st>>>(G, nv, b.xg, b.y1, b.y2, b.wsc);
+             launch_zgemm_cr(W * G, nv, nv, 1.0, b.xg, nv, c->ci2m, nv, false, b.y, nv, false, st));
+  cisd_l2_reduce_kernel<<<W, 256, 0, st>>>(G, nv, b.xg, b.y, b.wsc);
   TROT_CHECK_LAUNCH("cisd_l2_reduce_kernel");
   return TROT_OK;
 }
@@ -481,7 +647,7 @@ int trot_cisd_overlap(const trot_cisd* c, int W, const double* walkers, double* 
   if (!cv.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, cv.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
   cudaStream_t st = (cudaStream_t)stream;
   TROT_TRY(cisd_run(c, W, (const double2*)walkers, b, 0, st));
-  cisd_overlap_kernel<<<W, 256, 0, st>>>(c->nocc * c->nvir, b.x, b.cc, b.ce, b.wsc, b.det2, (double2*)out);
+  cisd_overlap_kernel<<<W, 256, 0, st>>>(c->nocc * c->nvir, b.x, b.cg, b.wsc, b.det2, (double2*)out);
   TROT_CHECK_LAUNCH("cisd_overlap_kernel");
   return TROT_OK;
 }
@@ -590,7 +756,7 @@ int trot_cisd_prop_step(const trot_cisd* c, const trot_system* prop, const trot_
   TROT_TIMED("trotter_fp64", st, launch_trotter(sp, a, st));
   // 5. CISD overlaps of the new walkers, weights, population shift
   TROT_TRY(cisd_run(c, W, w, b, 0, st));
-  cisd_overlap_kernel<<<W, 256, 0, st>>>(c->nocc * c->nvir, b.x, b.cc, b.ce, b.wsc, b.det2, b.ov_new);
+  cisd_overlap_kernel<<<W, 256, 0, st>>>(c->nocc * c->nvir, b.x, b.cg, b.wsc, b.det2, b.ov_new);
   TROT_CHECK_LAUNCH("cisd_overlap_kernel");
   a.overlaps = (double2*)state->overlaps; a.weights = state->weights; a.scalars = state->scalars;
   a.shift_term = b.shift_term; a.fb_term = b.fb_term; a.node_flag = b.node_flag;

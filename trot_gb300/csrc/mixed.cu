@@ -8,6 +8,8 @@
 //  * one-body half steps and the Taylor series: FP32 on the CUDA cores.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "mixed.h"
 #include "profile.h"
 #include "step_tail.cuh"
@@ -139,6 +141,7 @@ static int launch_green_ff(const Spins& sp, int W, int N, const double2* wa, con
 }
 
 // ------------------------------------------------------------------ layouts
+static constexpr size_t kTcChunkBytes = 3 * 128 * 64 * 2;  // one A chunk of the tensor-core Trotter kernel
 static constexpr int kKP = 128;       // padded orbital dimension of the exact product
 static constexpr int kBN = 48;        // MMA N of the exchange tile (columns = walker rows)
 static constexpr int kGroups = 5;     // accumulators for t + u = 0..4
@@ -185,6 +188,7 @@ struct MixedBuffers {
   double2 *shift_term, *fb_term;
   uint16_t* xq;
   float* vhs;
+  uint16_t* vimg;  // [Vr | Vi] operand images of the tensor-core Trotter kernel
   int* node_flag;
   int* status;
   int nblk_total, mpad;
@@ -215,6 +219,7 @@ static size_t carve_mixed(const trot_system* s, const Spins& sp, Carver& c, Mixe
     m.xs = c.take<double2>(W * G);
     m.xq = c.take<uint16_t>((size_t)s->mixed->vhs_slices * m.mpad * s->mixed->gpad);
     m.vhs = c.take<float>((size_t)m.mpad * s->mixed->n2pad);
+    if (s->mixed->exp_h1_half_img) m.vimg = c.take<uint16_t>(W * 4 * (size_t)(kTcChunkBytes / 2));
     m.shift_term = c.take<double2>(W);
     m.fb_term = c.take<double2>(W);
     m.node_flag = c.take<int>(W);
@@ -855,6 +860,260 @@ __global__ void __launch_bounds__(256) trotter32_kernel(Spins sp, Trot32Args a32
   overlap_and_weight(sp, a, N, nc, W2, Ms, &piv, red);
 }
 
+// ------------------------------------------------------------------ tensor-core Trotter propagation
+// Same algorithm as trotter32_kernel with every product on the tensor cores:
+//   term 0:        T0 = E w                      (E = exp(-dt/2 h1_eff), real)
+//   term k=1..K:   T_k = (i sqrt(dt)/k) V T_{k-1}, O = T0 + ... + T_K
+//   term K+1:      w' = E O
+// One CTA per walker.  The A operand (128 rows p x K) is streamed from global
+// memory in 64-wide K chunks of 3 BF16 slices (48 KB, 2-stage ring): E (K = 128,
+// 2 chunks, shared by all walkers) or this walker's [Vr | Vi] (K = 256, 4
+// chunks).  The B operand (NB rows x K, 3 slices) holds the previous term T in
+// shared memory, row 2j giving the real and row 2j + 1 the imaginary part of
+// output column j: for a V term row 2j = [Tr_j ; -Ti_j] and row 2j + 1 =
+// [Ti_j ; Tr_j] over K = [Re rows 0..127 ; Im rows 128..255], for an E term
+// rows 2j / 2j + 1 = Tr_j / Ti_j over K = 128.  3-term BF16 splits of
+// both operands, products t + u <= 2 (6 MMAs per K step), FP32 accumulation in
+// TMEM (~2^-24 relative, the FP32 path's accuracy).  Warps 0-3 (thread = row p
+// = TMEM lane) turn each accumulator into the next B operand and accumulate O
+// in registers; warp 4 lane 0 streams A and issues the MMAs.  The tail (FP64
+// overlap, phaseless weight) is shared with the other Trotter kernels.
+static constexpr int kTcThreads = 160;
+static constexpr uint32_t kTcChunk = 3 * kVSlice;  // 48 KB: 3 slices x 128 rows x 64 K
+
+struct TrotTcArgs {
+  TrotterArgs t;
+  const uint16_t* vimg;  // (W, 4 chunks, 3, 128, 64) bf16 image of [Vr | Vi]
+  const uint16_t* eimg;  // (2 chunks, 3, 128, 64) bf16 image of E
+  int* status;
+};
+
+__device__ __forceinline__ void split3_bf16(float x, uint16_t& h, uint16_t& m, uint16_t& l) {
+  const __nv_bfloat16 bh = __float2bfloat16_rn(x);
+  const float r1 = x - __bfloat162float(bh);
+  const __nv_bfloat16 bm = __float2bfloat16_rn(r1);
+  const __nv_bfloat16 bl = __float2bfloat16_rn(r1 - __bfloat162float(bm));
+  h = *reinterpret_cast<const uint16_t*>(&bh);
+  m = *reinterpret_cast<const uint16_t*>(&bm);
+  l = *reinterpret_cast<const uint16_t*>(&bl);
+}
+
+// B element (row j, k) = x as 3 slices; B image = [kchunk][slice][NB rows][64]
+__device__ __forceinline__ void put_b(unsigned char* B, int NB, int j, int k, float x) {
+  uint16_t h, m, l;
+  split3_bf16(x, h, m, l);
+  const uint32_t sl = (uint32_t)NB * 128;  // bytes of one slice of one chunk
+  unsigned char* c = B + (size_t)(k >> 6) * 3 * sl + tc::tile_off(j, k & 63);
+  *reinterpret_cast<uint16_t*>(c) = h;
+  *reinterpret_cast<uint16_t*>(c + sl) = m;
+  *reinterpret_cast<uint16_t*>(c + 2 * sl) = l;
+}
+
+template <int NBT>
+__global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, TrotTcArgs g) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ double2 red[32];
+  __shared__ int piv;
+  __shared__ __align__(8) uint64_t bars[6];
+  __shared__ uint32_t tslot;
+  __shared__ int okflag;
+  unsigned char* base = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
+  unsigned char* Abuf = base;                    // 2 x 48 KB
+  unsigned char* Bbuf = base + 2 * kTcChunk;     // 4 chunks x 3 slices x NB x 128 B
+  uint64_t* full = bars;       // [2]
+  uint64_t* empty = bars + 2;  // [2]
+  uint64_t* acc_full = bars + 4;
+  uint64_t* b_ready = bars + 5;
+  const TrotterArgs& a = g.t;
+  const int b = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int N = a.N, nc = sp.ntot, nterms = a.nterms;
+  constexpr int NB = NBT, NJ = NBT / 2;
+  const int nsteps = nterms + 2;  // E, V x nterms, E
+  if (warp == 4) tc::tmem_alloc(&tslot, 64);
+  if (tid == 128) {
+    for (int k = 0; k < 2; ++k) {
+      tc::mbar_init(&full[k], 1);
+      tc::mbar_init(&empty[k], 1);
+    }
+    tc::mbar_init(acc_full, 1);
+    tc::mbar_init(b_ready, 128);
+    okflag = 1;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  // zero the B image once: padding rows (j >= 2 nc) and columns (k >= N) stay zero
+  {
+    const int words = 4 * 3 * NB * 128 / 16;
+    uint4* bz = reinterpret_cast<uint4*>(Bbuf);
+    for (int e = tid; e < words; e += kTcThreads) bz[e] = make_uint4(0u, 0u, 0u, 0u);
+    tc::fence_proxy_async();  // visible to the tensor core (async proxy)
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = tslot;
+  if (warp == 4) {
+    if (lane == 0) {
+      bool ok = true;
+      const uint32_t idesc = tc::idesc_bf16_f32(128, NB);
+      const uint32_t sa = tc::smem_u32(Abuf), sb = tc::smem_u32(Bbuf);
+      const uint32_t bsl = (uint32_t)NB * 128;
+      const uint16_t* vimg = g.vimg + (size_t)b * 4 * (kTcChunk / 2);
+      int chunk = 0;
+      for (int step = 0; step < nsteps && ok; ++step) {
+        const bool vterm = step > 0 && step <= nterms;
+        const int nk = vterm ? 4 : 2;
+        for (int kc = 0; kc < nk && ok; ++kc, ++chunk) {
+          const int st = chunk & 1;
+          if (chunk >= 2) ok = tc::mbar_wait(&empty[st], (uint32_t)(((chunk - 2) >> 1) & 1));
+          if (!ok) break;
+          const uint16_t* src = (vterm ? vimg : g.eimg) + (size_t)kc * (kTcChunk / 2);
+          tc::mbar_expect_tx(&full[st], kTcChunk);
+          tc::bulk_g2s(Abuf + (size_t)st * kTcChunk, src, kTcChunk, &full[st]);
+          if (kc == 0) {  // the B operand of this step is written by the epilogue warps
+            ok = tc::mbar_wait(b_ready, (uint32_t)(step & 1));
+            if (!ok) break;
+          }
+          ok = tc::mbar_wait(&full[st], (uint32_t)((chunk >> 1) & 1));
+          if (!ok) break;
+          tc::fence_after_sync();
+          const uint32_t a0 = sa + (uint32_t)st * kTcChunk;
+          const uint32_t b0 = sb + (uint32_t)kc * 3 * bsl;
+          for (int t = 0; t < 3; ++t)
+            for (int u = 0; t + u <= 2; ++u) {
+#pragma unroll
+              for (int ks = 0; ks < 4; ++ks) {
+                const uint64_t ad = tc::smem_desc(a0 + (uint32_t)t * kVSlice + ks * 256, 128, 1024);
+                const uint64_t bd = tc::smem_desc(b0 + (uint32_t)u * bsl + ks * 256, 128, 1024);
+                tc::mma_bf16(taddr, ad, bd, idesc, (kc | t | u | ks) ? 1u : 0u);
+              }
+            }
+          tc::mma_commit(&empty[st]);
+        }
+        if (ok) tc::mma_commit(acc_full);
+      }
+      if (!ok) {
+        atomicExch(g.status, (int)TROT_ERR_DEVICE_TIMEOUT);
+        okflag = 0;
+        // let copies / MMAs already issued land before the tensor memory is released
+        for (int k = 0; k < 2; ++k) tc::mbar_wait(&empty[k], 0u, 1000000u);
+        tc::mbar_wait(&full[0], 0u, 1000000u);
+      }
+    }
+    __syncwarp();
+  } else {
+    // thread r: row p = r of every accumulator (TMEM lane r); output column j of
+    // the complex product is B row 2j (real part) and 2j + 1 (imaginary part)
+    const int p = tid;
+    const bool prow = p < N;
+    float orr[NJ], oi[NJ];
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) { orr[j] = 0.f; oi[j] = 0.f; }
+    // term 0 operand: B[2j][p] = Re w[p][j], B[2j+1][p] = Im w[p][j]
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+      if (j < nc) {
+        const int s = j < sp.n[0] ? 0 : 1, n = sp.n[s], col = j - sp.off[s];
+        const double2* w = (s == 0 ? a.in_a : a.in_b) + (size_t)b * N * n;
+        const double2 x = prow ? w[(size_t)p * n + col] : make_double2(0.0, 0.0);
+        put_b(Bbuf, NB, 2 * j, p, (float)x.x);
+        put_b(Bbuf, NB, 2 * j + 1, p, (float)x.y);
+      }
+    }
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    tc::mbar_arrive(b_ready);
+    const uint32_t trow = taddr + ((uint32_t)(warp * 32) << 16);
+    for (int step = 0; step < nsteps; ++step) {
+      if (!tc::mbar_wait(acc_full, (uint32_t)(step & 1))) {
+        atomicExch(g.status, (int)TROT_ERR_DEVICE_TIMEOUT);
+        okflag = 0;
+        break;
+      }
+      tc::fence_after_sync();
+      float d[NB];
+#pragma unroll
+      for (int c = 0; c < NB; c += 16) tc::tmem_ld16(trow + c, d + c);
+      if (step == nsteps - 1) {
+        // w' = E O: write the walker (FP64) to global memory and to shared memory for the tail
+        double2* W2 = reinterpret_cast<double2*>(Abuf);
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+          if (j < nc && prow) {
+            const double2 x = make_double2((double)d[2 * j], (double)d[2 * j + 1]);
+            W2[p * nc + j] = x;
+            const int s = j < sp.n[0] ? 0 : 1, n = sp.n[s], col = j - sp.off[s];
+            (s == 0 ? a.out_a : a.out_b)[((size_t)b * N + p) * n + col] = x;
+          }
+        }
+        break;
+      }
+      const bool next_is_v = step < nterms;  // the operand built now feeds a V term
+      const float coef = step == 0 ? 1.f : (float)(a.sqrt_dt / (double)step);
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        if (j < nc) {
+          float tr, ti;
+          if (step == 0) { tr = d[2 * j]; ti = d[2 * j + 1]; }
+          else { tr = -coef * d[2 * j + 1]; ti = coef * d[2 * j]; }
+          orr[j] += tr;
+          oi[j] += ti;
+          if (next_is_v) {
+            put_b(Bbuf, NB, 2 * j, p, tr);
+            put_b(Bbuf, NB, 2 * j, 128 + p, -ti);
+            put_b(Bbuf, NB, 2 * j + 1, p, ti);
+            put_b(Bbuf, NB, 2 * j + 1, 128 + p, tr);
+          } else {
+            put_b(Bbuf, NB, 2 * j, p, orr[j]);
+            put_b(Bbuf, NB, 2 * j + 1, p, oi[j]);
+          }
+        }
+      }
+      tc::fence_proxy_async();
+      tc::fence_before_sync();
+      tc::mbar_arrive(b_ready);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 4) tc::tmem_dealloc(taddr, 64);
+  if (!okflag) return;
+  if (a.overlaps == nullptr) return;
+  double2* W2 = reinterpret_cast<double2*>(Abuf);
+  double2* Ms = reinterpret_cast<double2*>(Bbuf);
+  overlap_and_weight(sp, a, N, nc, W2, Ms, &piv, red);
+}
+
+// [Vr | Vi] of every walker as the A image of trotter_tc_kernel: (W, 4 chunks, 3 slices, 128 rows, 64)
+// from the VHS GEMM output (rows 2b / 2b+1 = Re / Im of walker b, n2pad columns pq).
+// One thread per (walker, chunk, row, 8 consecutive k): three 16-byte stores.
+__global__ void vhs_image_kernel(int W, int N, int n2pad, const float* __restrict__ D, uint16_t* __restrict__ img) {
+  const size_t total = (size_t)W * 4 * 128 * 8;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int kg = (int)(e & 7), p = (int)((e >> 3) & 127), kc = (int)((e >> 10) & 3);
+    const size_t b = e >> 12;
+    const int k0 = kc * 64 + kg * 8;                 // 0..255
+    const int im = k0 >= 128 ? 1 : 0, q0 = k0 & 127;
+    const float* src = D + (2 * b + im) * (size_t)n2pad + (size_t)p * N;
+    uint32_t hw[4], mw[4], lw[4];
+#pragma unroll
+    for (int i = 0; i < 8; i += 2) {
+      const float x0 = (p < N && q0 + i < N) ? src[q0 + i] : 0.f;
+      const float x1 = (p < N && q0 + i + 1 < N) ? src[q0 + i + 1] : 0.f;
+      uint16_t h0, m0, l0, h1, m1, l1;
+      split3_bf16(x0, h0, m0, l0);
+      split3_bf16(x1, h1, m1, l1);
+      hw[i / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+      mw[i / 2] = (uint32_t)m0 | ((uint32_t)m1 << 16);
+      lw[i / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+    }
+    unsigned char* dst = reinterpret_cast<unsigned char*>(img) + (b * 4 + kc) * (size_t)kTcChunk + tc::tile_off(p, kg * 8);
+    *reinterpret_cast<uint4*>(dst) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *reinterpret_cast<uint4*>(dst + kVSlice) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+    *reinterpret_cast<uint4*>(dst + 2 * kVSlice) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+  }
+}
+
 // ------------------------------------------------------------------ host orchestration
 static int check_mixed_shapes(const trot_system* s, const Spins& sp) {
   if (!s->mixed) { set_error("mixed precision needs a trot_mixed context"); return TROT_ERR_NULL_PTR; }
@@ -934,6 +1193,31 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
   return TROT_OK;
 }
 
+static void vhs_gemm_attr() {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(vhs_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kVhsSmem);
+    attr_set = true;
+  }
+}
+
+int launch_split3_gemm(int rows, int K, int kpad, int npad, const double2* x, const uint16_t* b_image,
+                       uint16_t* xq, float* D, int* status, cudaStream_t st) {
+  if (kpad % kVK || npad % 128 || K > kpad || rows <= 0) {
+    set_error("split3 GEMM: bad layout rows=%d K=%d kpad=%d npad=%d", rows, K, kpad, npad);
+    return TROT_ERR_BAD_SHAPE;
+  }
+  const int mpad = split3_mpad(rows);
+  x_slices_kernel<<<152 * 8, 256, 0, st>>>(rows, K, kpad, mpad, x, xq);
+  TROT_CHECK_LAUNCH("x_slices_kernel");
+  vhs_gemm_attr();
+  const int mtiles = mpad / 128, ntiles = npad / 128;
+  const int grid = mtiles * ntiles > 152 ? 152 : mtiles * ntiles;
+  vhs_gemm_kernel<<<grid, kVThreads, kVhsSmem, st>>>(mtiles, ntiles, kpad, npad, xq, b_image, D, status);
+  TROT_CHECK_LAUNCH("vhs_gemm_kernel");
+  return TROT_OK;
+}
+
 static int run_vhs(const trot_system* s, MixedBuffers& m, const double2* xs, cudaStream_t st) {
   const int W = s->n_walkers, G = s->nchol;
   const trot_mixed* mx = s->mixed;
@@ -946,11 +1230,7 @@ static int run_vhs(const trot_system* s, MixedBuffers& m, const double2* xs, cud
     TROT_CHECK_LAUNCH("x_slices_kernel");
     return TROT_OK;
   })());
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(vhs_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kVhsSmem);
-    attr_set = true;
-  }
+  vhs_gemm_attr();
   const int mtiles = m.mpad / 128, ntiles = mx->n2pad / 128;
   int grid = mtiles * ntiles;
   if (grid > 152) grid = 152;
@@ -983,6 +1263,54 @@ static int run_trotter32(const trot_system* s, const Spins& sp, const TrotterArg
   a.expH32 = s->mixed->exp_h1_half_f32;
   trotter32_kernel<<<s->n_walkers, 256, smem, st>>>(sp, a);
   TROT_CHECK_LAUNCH("trotter32_kernel");
+  return TROT_OK;
+}
+
+template <int NBT>
+static void trotter_tc_launch(const Spins& sp, const TrotTcArgs& g, int W, size_t smem, cudaStream_t st) {
+  cudaFuncSetAttribute(trotter_tc_kernel<NBT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  trotter_tc_kernel<NBT><<<W, kTcThreads, smem, st>>>(sp, g);
+}
+
+static int run_trotter_tc(const trot_system* s, const Spins& sp, const TrotterArgs& t, const MixedBuffers& m,
+                          cudaStream_t st) {
+  const int W = s->n_walkers, N = s->norb, nc = sp.ntot;
+  const int NB = (2 * nc + 15) / 16 * 16;
+  if (N > 128 || NB > 64 || t.nterms < 1 || t.nterms > 16 || !m.vimg) {
+    set_error("tensor-core Trotter: N=%d nc=%d nterms=%d unsupported", N, nc, t.nterms);
+    return TROT_ERR_UNSUPPORTED;
+  }
+  static_assert(kTcChunkBytes == kTcChunk, "A chunk size");
+  TROT_TIMED("vhs_image", st, ([&]() -> int {
+    const size_t threads = (size_t)W * 4 * 128 * 8;
+    const int blocks = (int)std::min<size_t>((threads + 255) / 256, 152 * 32);
+    vhs_image_kernel<<<blocks, 256, 0, st>>>(W, N, s->mixed->n2pad, m.vhs, m.vimg);
+    TROT_CHECK_LAUNCH("vhs_image_kernel");
+    return TROT_OK;
+  })());
+  TrotTcArgs g{};
+  g.t = t;
+  g.vimg = m.vimg;
+  g.eimg = s->mixed->exp_h1_half_img;
+  g.status = m.status;
+  const size_t smem = 1024 + 2 * (size_t)kTcChunk + 4 * 3 * (size_t)NB * 128;
+  TROT_TIMED("trotter_tc", st, ([&]() -> int {
+    switch (NB) {
+      case 16: trotter_tc_launch<16>(sp, g, W, smem, st); break;
+      case 32: trotter_tc_launch<32>(sp, g, W, smem, st); break;
+      case 48: trotter_tc_launch<48>(sp, g, W, smem, st); break;
+      default: trotter_tc_launch<64>(sp, g, W, smem, st); break;
+    }
+    TROT_CHECK_LAUNCH("trotter_tc_kernel");
+    return TROT_OK;
+  })());
+  return TROT_OK;
+}
+
+static int run_trotter(const trot_system* s, const Spins& sp, const TrotterArgs& t, const MixedBuffers& m,
+                       cudaStream_t st) {
+  if (s->mixed->exp_h1_half_img && m.vimg) return run_trotter_tc(s, sp, t, m, st);
+  TROT_TIMED("trotter_fp32", st, run_trotter32(s, sp, t, m, st));
   return TROT_OK;
 }
 
@@ -1030,7 +1358,7 @@ int mixed_apply_trotter(const trot_system* s, const Spins& sp, const double2* xs
   if (!c.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, c.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
   cudaMemsetAsync(m.status, 0, 4 * sizeof(int), st);
   TROT_TRY(run_vhs(s, m, xs, st));
-  return run_trotter32(s, sp, a, m, st);
+  return run_trotter(s, sp, a, m, st);
 }
 
 int mixed_prop_step(const trot_system* s, const Spins& sp, const trot_state* state, const double* fields,
@@ -1055,7 +1383,7 @@ int mixed_prop_step(const trot_system* s, const Spins& sp, const trot_state* sta
   a.overlaps = (double2*)state->overlaps; a.weights = state->weights; a.scalars = state->scalars;
   a.shift_term = m.shift_term; a.fb_term = m.fb_term; a.node_flag = m.node_flag;
   a.dt = s->dt; a.h0_prop = s->h0_prop; a.w_floor = s->weight_floor; a.w_cap = s->weight_cap;
-  TROT_TIMED("trotter_fp32", st, run_trotter32(s, sp, a, m, st));
+  TROT_TRY(run_trotter(s, sp, a, m, st));
   TROT_TIMED("step_finalize", st, launch_step_finalize(W, state->weights, state->scalars,
                                                        (long long*)state->node_encounters, m.node_flag,
                                                        s->pop_control_damping, s->dt, st));

@@ -60,6 +60,23 @@ def plain_split(x: np.ndarray, slices: int = VHS_SLICES) -> list[torch.Tensor]:
     return out
 
 
+def split3_image(bt: np.ndarray):
+    """Operand image of a real matrix B (K, ncols) for the split-BF16 GEMM
+    kernel, given its transpose bt (ncols, K): rows padded to a multiple of
+    128, K to a multiple of 64, split into 3 BF16 terms and laid out as
+    [ncols/128][K/64][3][128][64] tiles in core-matrix order (8 x 8 blocks).
+    Returns (image (bf16, host), ncols_pad, k_pad)."""
+    bt = np.asarray(bt, dtype=np.float64)
+    nc, K = bt.shape
+    npad, kpad = (nc + 127) // 128 * 128, (K + 63) // 64 * 64
+    lt = np.zeros((npad, kpad), dtype=np.float64)
+    lt[:nc, :K] = bt
+    sl = torch.stack(plain_split(lt))  # (3, npad, kpad)
+    nt, nk = npad // 128, kpad // 64
+    sl = sl.reshape(3, nt, 16, 8, nk, 8, 8).permute(1, 4, 0, 2, 5, 3, 6).contiguous()
+    return sl.reshape(nt, nk, 3, 128, 64).contiguous(), npad, kpad
+
+
 def gammas_per_block(n: int) -> int:
     return max(1, 128 // n)
 
@@ -104,22 +121,23 @@ class MixedCtx:
         self.struct = s
         if chol_flat is None:
             return
-        G, N2 = chol_flat.shape
-        n2pad = (N2 + 127) // 128 * 128
-        gpad = (G + 63) // 64 * 64
-        lt = np.zeros((n2pad, gpad), dtype=np.float64)
-        lt[:N2, :G] = chol_flat.T
-        sl = torch.stack(plain_split(lt))  # (3, n2pad, gpad)
-        # shared-memory image: [ntile][kchunk][slice][128 rows][64] in core-matrix order
-        nt, nk = n2pad // 128, gpad // 64
-        sl = sl.reshape(3, nt, 16, 8, nk, 8, 8).permute(1, 4, 0, 2, 5, 3, 6).contiguous()
-        sl = sl.reshape(nt, nk, 3, 128, 64).to(dev).contiguous()
+        sl, n2pad, gpad = split3_image(np.asarray(chol_flat).T)
+        sl = sl.to(dev)
         self._keep.append(sl)
         s.vhs_slices, s.vhs_order, s.n2pad, s.gpad = VHS_SLICES, VHS_ORDER, n2pad, gpad
         s.chol_t_slices = sl.data_ptr()
         eh = torch.as_tensor(np.asarray(exp_h1_half, dtype=np.float32)).to(dev).contiguous()
         self._keep.append(eh)
         s.exp_h1_half_f32 = eh.data_ptr()
+        E = np.asarray(exp_h1_half, dtype=np.float64)
+        if E.shape[0] <= 128:
+            E128 = np.zeros((128, 128))  # the kernel reads K = 128 (two 64-wide chunks) for every N
+            E128[: E.shape[0], : E.shape[1]] = E
+            ei, _, kp = split3_image(E128)  # A operand rows p, K = q: (1, 2, 3, 128, 64)
+            assert tuple(ei.shape) == (1, 2, 3, 128, 64) and kp == 128
+            ei = ei.to(dev)
+            self._keep.append(ei)
+            s.exp_h1_half_img = ei.data_ptr()
         self.struct = s
 
     def data_ptr(self) -> int:
