@@ -90,9 +90,10 @@ typedef struct {
   int gpad;              /* G rounded up to 64 */
   const uint16_t* chol_t_slices; /* bf16 (vhs_slices, n2pad, gpad): row pq holds L[:, pq] */
   const float* exp_h1_half_f32;  /* (N, N) */
-  /* exp(-dt/2 h1_eff) as 3 BF16 slices in the tensor-core operand image
-   * (2 chunks x 3 slices x 128 rows x 64); when set, the Trotter action runs on
-   * the tensor cores (N <= 128, nocc_a + nocc_b <= 32), else in FP32. */
+  /* exp(-dt/2 h1_eff), zero-padded to 128 x 128, as 3 BF16 slices in the
+   * tensor-core operand image (4 chunks x 3 slices x 128 rows x 32); when set,
+   * the Trotter action runs on the tensor cores (N <= 128, nocc_a + nocc_b <=
+   * 32), else in FP32. */
   const uint16_t* exp_h1_half_img;
 } trot_mixed;
 
@@ -315,6 +316,21 @@ int trot_cisd_rdm1(const trot_cisd* cisd, int n_walkers, const double* walkers, 
 int trot_cisd_prop_step(const trot_cisd* cisd, const trot_system* prop, const trot_state* state,
                         const double* fields, double* energy_out, void* workspace, size_t workspace_bytes,
                         void* stream);
+
+/* ---------------------------------------------------------------- free projection
+ * One free-projection step (trot/prop/afqmc_fp.py:18-72): unshifted fields
+ * (W, nchol) float64, the Trotter action with sys->n_exp_terms terms (10 in
+ * the reference) at sys->precision, walker columns times
+ * exp(-sqrt(dt) sum_g x_g mf_g + dt h0_prop)^(1/n_total), QR norms
+ * prod_j |R_jj| (qr_norm, trot/walkers.py:182-207), weights times the norms,
+ * comb resampling with the device scalar *zeta_dev, and the resampled weights
+ * divided by the selected walkers' norms.  sys->h0_prop includes ene0
+ * (_build_prop_ctx_fp, trot/prop/chol_afqmc_ops_fp.py:49-72).  Walkers and
+ * weights are updated in place; overlaps, scalars and node count are not read.
+ * Workspace: trot_fp_workspace_size(sys) bytes. */
+size_t trot_fp_workspace_size(const trot_system* sys);
+int trot_fp_step(const trot_system* sys, const trot_state* state, const double* fields, const double* zeta_dev,
+                 void* workspace, size_t workspace_bytes, void* stream);
 
 /* Plain BF16 tensor-core GEMM (tcgen05, accumulator in tensor memory):
  * D (M x N, float32) = A (M x K, bf16) * B (N x K, bf16)^T, all row-major,

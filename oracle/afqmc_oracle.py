@@ -462,6 +462,53 @@ def block(state: State, model: Model, params: Params, fields_seq, zeta):
     return st, e_block, w_sum
 
 
+def qr_norm(w, walker_kind):
+    """``qr_norm`` (trot/walkers.py:182-207): det of the phase-fixed R only
+    (R = phase * R, det = prod diag), squared for restricted walkers."""
+
+    def det_r(mat):
+        r = np.linalg.qr(mat, mode="r")
+        d = np.diagonal(r, axis1=-2, axis2=-1)
+        ad = np.abs(d)
+        phase = d / np.where(ad == 0, 1.0, ad)
+        return np.prod(phase * d, axis=-1)
+
+    if walker_kind == "unrestricted":
+        return det_r(w[0]) * det_r(w[1])
+    d = det_r(w)
+    return d * d if walker_kind == "restricted" else d
+
+
+def multiply_constants(w, constants, walker_kind):
+    """``multiply_constants`` (trot/walkers.py:210-227): c^(1/n_total) on every column."""
+    constants = np.asarray(constants)
+    if walker_kind == "unrestricted":
+        n_total = w[0].shape[-1] + w[1].shape[-1]
+        c = (constants ** (1.0 / n_total))[:, None, None]
+        return (w[0] * c, w[1] * c)
+    n_total = 2 * w.shape[-1]
+    c = (constants ** (1.0 / n_total))[:, None, None]
+    return w * c
+
+
+def afqmc_step_fp(state: State, model: Model, fields, zeta, n_terms=10):
+    """``afqmc_step_fp`` (trot/prop/afqmc_fp.py:18-72) with injected fields (W, G) and zeta;
+    ``model.prop`` is the free-projection context (h0_prop includes ene0)."""
+    ctx = model.prop
+    shift_term = fields @ ctx.mf_shifts
+    constants = np.exp(-ctx.sqrt_dt * shift_term + ctx.dt * ctx.h0_prop)
+    wn = model.trotter(state.walkers, fields.astype(np.complex128), n_terms)
+    wn = multiply_constants(wn, constants, model.walker_kind)
+    norms = qr_norm(wn, model.walker_kind)
+    weights = state.weights * norms.real
+    n = weights.shape[0]
+    idx = sr_indices(weights, zeta, n)
+    w_sr, weights_sr, _ = stochastic_reconfiguration(wn, weights, zeta, model.walker_kind)
+    weights_sr = weights_sr / norms[idx].real
+    return State(w_sr, weights_sr, state.overlaps, state.pop_control_ene_shift, state.e_estimate,
+                 state.node_encounters)
+
+
 def natorbs(dm, n_occ):
     """``_natorbs`` (trot/walkers.py:14-17)."""
     dm = 0.5 * (dm + np.conj(dm.T))

@@ -168,6 +168,60 @@ def _save_state(out, prefix, st, kind):
     out[prefix + "nodes"] = int(st.node_encounters)
 
 
+def fp_case(name, norb, nelec, nchol, n_walkers, kind, dt=0.02, ene0=-1.3, seed=3, h0=0.5):
+    """One free-projection step (trot/prop/afqmc_fp.py) with injected fields and zeta."""
+    from trot.prop.afqmc_fp import make_prop_ops_fp
+    from trot.prop.types import QmcParamsFp
+
+    ss = synthetic.make_system(norb, nelec, nchol, decay=30.0, seed=seed, h0=h0)
+    ham = HamChol(h0=np.asarray(h0), h1=ss.h1, chol=ss.chol, basis="restricted")
+    walker_kind = "restricted" if kind == "rhf_r" else "unrestricted"
+    sysm = System(norb=norb, nelec=nelec, walker_kind=walker_kind)
+    if kind == "uhf_u":
+        trial, trial_ops = tuhf.UhfTrial(ss.mo_a, ss.mo_b), tuhf.make_uhf_trial_ops(sysm)
+    else:
+        trial, trial_ops = trhf.RhfTrial(ss.mo_a), trhf.make_rhf_trial_ops(sysm)
+    params = QmcParamsFp(dt=dt, n_walkers=n_walkers, ene0=ene0, n_exp_terms=6, seed=0)
+    prop_ops = make_prop_ops_fp("restricted", walker_kind, sysm)
+    rdm1 = trial_ops.get_rdm1(trial)
+    ctx = prop_ops.build_prop_ctx(ham, rdm1, params)
+    rng = np.random.default_rng(seed + 7)
+    wu = synthetic.perturbed_walkers(ss.mo_a, n_walkers, 0.2, seed + 1)
+    wd = synthetic.perturbed_walkers(ss.mo_b, n_walkers, 0.2, seed + 2)
+    walkers = wu if kind == "rhf_r" else (wu, wd)
+    weights = 0.5 + rng.uniform(size=n_walkers)
+    fields = rng.standard_normal((n_walkers, nchol))
+    zeta = float(rng.uniform())
+    state = PropState(walkers=walkers, weights=weights, overlaps=np.ones(n_walkers, np.complex128),
+                      rng_key=np.array([0, 0], np.uint32), pop_control_ene_shift=np.asarray(0.0),
+                      e_estimate=np.asarray(0.0), node_encounters=np.asarray(0))
+    INJ.clear()
+    INJ.append(fields)
+    INJ.append(np.asarray(zeta))
+    out_state = prop_ops.step(state, params=params, ham_data=ham, trial_data=trial, trial_ops=trial_ops,
+                              meas_ops=None, meas_ctx=None, prop_ctx=ctx)
+    assert not INJ
+    out = dict(h0=h0, h1=ss.h1, chol=ss.chol, mo_a=ss.mo_a, mo_b=ss.mo_b, dt=dt, ene0=ene0, kind=np.array(kind),
+               fields=fields, zeta=zeta, weights=weights, h0_prop=np.asarray(ctx.h0_prop),
+               out_weights=np.asarray(out_state.weights))
+    if kind == "rhf_r":
+        out.update(walkers=wu, out_walkers=np.asarray(out_state.walkers))
+    else:
+        out.update(walkers_u=wu, walkers_d=wd, out_walkers_u=np.asarray(out_state.walkers[0]),
+                   out_walkers_d=np.asarray(out_state.walkers[1]))
+    out["qr_norm"] = np.asarray(wk.qr_norm(walkers, walker_kind))
+    consts = np.exp(0.3j * rng.standard_normal(n_walkers) + 0.1 * rng.standard_normal(n_walkers))
+    mc = wk.multiply_constants(walkers, consts, walker_kind)
+    out["mc_constants"] = consts
+    if kind == "rhf_r":
+        out["mc_out"] = np.asarray(mc)
+    else:
+        out["mc_out_u"], out["mc_out_d"] = np.asarray(mc[0]), np.asarray(mc[1])
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **{k: np.asarray(v) for k, v in out.items()})
+    print(f"wrote {path}: {os.path.getsize(path) / 1e3:.0f} kB")
+
+
 def cisd_case(name, norb, nocc, nchol, n_walkers, seed=0, h0=0.4, noise=0.1):
     cs = synthetic.make_cisd_system(norb, nocc, nchol, decay=30.0, seed=seed, h0=h0)
     ham = HamChol(h0=np.asarray(h0), h1=cs.h1, chol=cs.chol, basis="restricted")
@@ -194,12 +248,18 @@ def cisd_case(name, norb, nocc, nchol, n_walkers, seed=0, h0=0.4, noise=0.1):
 
 
 if __name__ == "__main__":
+    if len(sys.argv) > 2 and sys.argv[2] == "fp":
+        fp_case("fp_rhf_r", norb=10, nelec=(3, 3), nchol=16, n_walkers=6, kind="rhf_r")
+        fp_case("fp_uhf_u", norb=11, nelec=(4, 2), nchol=18, n_walkers=5, kind="uhf_u")
+        sys.exit(0)
     if len(sys.argv) > 2 and sys.argv[2] == "cisd":
         cisd_case("cisd_small", norb=12, nocc=3, nchol=20, n_walkers=4)
         cisd_case("cisd_n20", norb=20, nocc=5, nchol=50, n_walkers=3, seed=1)
         sys.exit(0)
     cisd_case("cisd_small", norb=12, nocc=3, nchol=20, n_walkers=4)
     cisd_case("cisd_n20", norb=20, nocc=5, nchol=50, n_walkers=3, seed=1)
+    fp_case("fp_rhf_r", norb=10, nelec=(3, 3), nchol=16, n_walkers=6, kind="rhf_r")
+    fp_case("fp_uhf_u", norb=11, nelec=(4, 2), nchol=18, n_walkers=5, kind="uhf_u")
     case("rhf_r_small", norb=10, nelec=(3, 3), nchol=16, n_walkers=5, kind="rhf_r")
     case("rhf_u_small", norb=9, nelec=(3, 3), nchol=14, n_walkers=4, kind="rhf_u")
     case("uhf_u_small", norb=11, nelec=(4, 2), nchol=18, n_walkers=5, kind="uhf_u")

@@ -4,6 +4,8 @@ import numpy as np
 import pytest
 
 from oracle import afqmc_oracle as orc
+from oracle import afqmc_oracle as ao
+from tests.conftest import load_golden
 from tests.golden_model import model_from_golden, rel_err, state_from_golden, walkers_from_golden
 
 TOL = 1e-11
@@ -100,3 +102,37 @@ def test_init_walkers(golden):
         pa = a @ np.conj(np.swapaxes(a, -1, -2))
         pb = b @ np.conj(np.swapaxes(b, -1, -2))
         assert rel_err(pa, pb) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["fp_rhf_r", "fp_uhf_u"])
+def test_oracle_free_projection_step(name):
+    _rel = rel_err
+    """afqmc_step_fp, qr_norm and multiply_constants vs the reference's own
+    free-projection modules (trot/prop/afqmc_fp.py, trot/walkers.py:182-227)."""
+    g = load_golden(name)
+    kind = str(g["kind"])
+    wk = "restricted" if kind == "rhf_r" else "unrestricted"
+    w = g["walkers"] if kind == "rhf_r" else (g["walkers_u"], g["walkers_d"])
+    mo = g["mo_a"] if kind != "uhf_u" else (g["mo_a"], g["mo_b"])
+    tmo = g["mo_a"] if kind == "rhf_r" else mo
+    if kind == "uhf_u":
+        dm = np.stack([g["mo_a"] @ g["mo_a"].T, g["mo_b"] @ g["mo_b"].T])
+    else:
+        dm = np.stack([g["mo_a"] @ g["mo_a"].T] * 2)
+    prop = ao.build_prop_ctx(float(g["h0"]), g["h1"], g["chol"], dm, float(g["dt"]))
+    prop = ao.PropCtx(prop.dt, prop.sqrt_dt, prop.exp_h1_half, prop.mf_shifts, prop.h0_prop + float(g["ene0"]),
+                      prop.chol_flat, prop.norb)
+    assert abs(prop.h0_prop - float(np.real(g["h0_prop"]))) <= 1e-12 * abs(prop.h0_prop)
+    model = ao.Model(kind, float(g["h0"]), tmo, None, prop)
+    st = ao.State(w, g["weights"], np.ones(len(g["weights"]), complex), 0.0, 0.0)
+    out = ao.afqmc_step_fp(st, model, g["fields"], float(g["zeta"]))
+    assert _rel(out.weights, g["out_weights"]) < 1e-11
+    if kind == "rhf_r":
+        assert _rel(out.walkers, g["out_walkers"]) < 1e-11
+        assert _rel(ao.multiply_constants(w, g["mc_constants"], wk), g["mc_out"]) < 1e-14
+    else:
+        assert _rel(out.walkers[0], g["out_walkers_u"]) < 1e-11
+        assert _rel(out.walkers[1], g["out_walkers_d"]) < 1e-11
+        mc = ao.multiply_constants(w, g["mc_constants"], wk)
+        assert _rel(mc[0], g["mc_out_u"]) < 1e-14 and _rel(mc[1], g["mc_out_d"]) < 1e-14
+    assert _rel(ao.qr_norm(w, wk), g["qr_norm"]) < 1e-12

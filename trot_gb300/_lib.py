@@ -106,6 +106,8 @@ _SIGNATURES = {
     "trot_cisd_rdm1": (_i, [ctypes.POINTER(TrotCisd), _i, _p, _p, _p, ctypes.c_size_t, _p]),
     "trot_cisd_prop_step": (_i, [ctypes.POINTER(TrotCisd), ctypes.POINTER(TrotSystem), ctypes.POINTER(TrotState),
                                  _p, _p, _p, ctypes.c_size_t, _p]),
+    "trot_fp_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(TrotSystem)]),
+    "trot_fp_step": (_i, [ctypes.POINTER(TrotSystem), ctypes.POINTER(TrotState), _p, _p, _p, ctypes.c_size_t, _p]),
     "trot_profile_enable": (_i, [_i]),
     "trot_profile_collect": (_i, [_i, ctypes.c_char_p, _p, _p]),
 }

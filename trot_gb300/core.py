@@ -163,6 +163,18 @@ class QmcParams(QmcParamsBase):
     n_eql_blocks: int = 20
 
 
+@dataclass(frozen=True)
+class QmcParamsFp(QmcParamsBase):
+    """Free-projection parameters (trot/prop/types.py:55-62)."""
+
+    dt: float = 0.05
+    n_prop_steps: int = 20
+    n_qr_blocks: int = 10
+    n_blocks: int = 5
+    ene0: float | None = None
+    n_traj: int = 10
+
+
 @dataclass
 class PropState:
     """Walker population and running scalars.

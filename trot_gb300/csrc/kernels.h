@@ -71,7 +71,9 @@ int launch_energy_combine(int W, int G, int nchunks, double h0, const double2* f
                           const double2* partial, double2* energy, cudaStream_t st);
 
 // walkers.cu
-int launch_qr(const Spins& sp, int W, int N, double2* wa, double2* wb, double2* norm_out, cudaStream_t st);
+// write_q = false: only the norms prod_j |R_jj| (free-projection qr_norm); the walkers are left unchanged
+int launch_qr(const Spins& sp, int W, int N, double2* wa, double2* wb, double2* norm_out, cudaStream_t st,
+              bool write_q = true);
 int launch_sr(const Spins& sp, int W, int N, const double* weights, const double* zeta_dev, double zeta,
               const double2* ina,
               const double2* inb, double2* outa, double2* outb, double* weights_out, long long* idx,

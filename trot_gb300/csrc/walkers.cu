@@ -13,7 +13,7 @@ namespace trot {
 static constexpr int kQrThreads = 256;
 
 __global__ void __launch_bounds__(kQrThreads)
-qr_kernel(int N, int n, double2* __restrict__ w, double2* __restrict__ norm, int norm_mode) {
+qr_kernel(int N, int n, double2* __restrict__ w, double2* __restrict__ norm, int norm_mode, int write_q) {
   extern __shared__ double2 smem[];
   __shared__ double2 red[32];
   __shared__ double2 coef[64];
@@ -54,7 +54,8 @@ qr_kernel(int N, int n, double2* __restrict__ w, double2* __restrict__ norm, int
     for (int p = tid; p < N; p += nt) Q[p * n + j] = cscale(Q[p * n + j], inv);
     __syncthreads();
   }
-  for (int e = tid; e < N * n; e += nt) gw[e] = Q[e];
+  if (write_q)
+    for (int e = tid; e < N * n; e += nt) gw[e] = Q[e];
   // norm_mode: 0 set det_r, 1 set det_r^2 (restricted), 2 multiply into the
   // alpha launch's value (unrestricted: det_a det_b; stream order keeps it safe)
   if (tid == 0 && norm) {
@@ -64,7 +65,8 @@ qr_kernel(int N, int n, double2* __restrict__ w, double2* __restrict__ norm, int
   }
 }
 
-int launch_qr(const Spins& sp, int W, int N, double2* wa, double2* wb, double2* norm_out, cudaStream_t st) {
+int launch_qr(const Spins& sp, int W, int N, double2* wa, double2* wb, double2* norm_out, cudaStream_t st,
+              bool write_q) {
   int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
   if (nmax > 64) {
     set_error("qr: nocc %d > 64 unsupported", nmax);
@@ -76,10 +78,10 @@ int launch_qr(const Spins& sp, int W, int N, double2* wa, double2* wb, double2* 
     return TROT_ERR_UNSUPPORTED;
   }
   if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  qr_kernel<<<W, kQrThreads, smem, st>>>(N, sp.n[0], wa, norm_out, sp.mult[0] == 2 ? 1 : 0);
+  qr_kernel<<<W, kQrThreads, smem, st>>>(N, sp.n[0], wa, norm_out, sp.mult[0] == 2 ? 1 : 0, write_q ? 1 : 0);
   TROT_CHECK_LAUNCH("qr_kernel");
   if (sp.nspin == 2) {
-    qr_kernel<<<W, kQrThreads, smem, st>>>(N, sp.n[1], wb, norm_out, 2);
+    qr_kernel<<<W, kQrThreads, smem, st>>>(N, sp.n[1], wb, norm_out, 2, write_q ? 1 : 0);
     TROT_CHECK_LAUNCH("qr_kernel");
   }
   return TROT_OK;
