@@ -48,6 +48,27 @@ def flops_per_walker_step(N, na, nb, G, nterms=6):
     return d
 
 
+def flops_per_walker_step_cisd(N, n, G, nterms=6):
+    """Algorithmic flops of one CISD walker-step (trot/meas/cisd.py:608-769 contraction
+    order: the two l2ci2 quadratic forms, glgp, gl, lci2_green, ... plus the propagation)."""
+    v = N - n
+    nv = n * v
+    d = {
+        "l2ci2": 2 * 4 * G * nv * nv,
+        "glgp": 8 * G * n * N * v,
+        "gl": 4 * G * n * N * N,
+        "lci2_green": 4 * G * n * N * N,
+        "lg1": 4 * G * n * n * N,
+        "chol_contract": 3 * 4 * G * N * N,
+        "ci2g": 2 * 4 * nv * nv,
+        "mats": 2 * 8 * N * N * n,
+        "vhs": 4 * G * N * N,
+        "taylor": nterms * 8 * N * N * n,
+        "onebody": 2 * 4 * N * N * n,
+    }
+    return d
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -120,8 +141,10 @@ def build_workload(cfg, precision):
     from trot_gb300 import synthetic
 
     N, (na, nb), G, W = cfg["norb"], cfg["nelec"], cfg["nchol"], cfg["n_walkers"]
-    ss = synthetic.make_system(N, (na, nb), G, decay=cfg["decay"], seed=0, h0=0.0)
     kind = cfg["kind"]
+    if kind == "cisd":
+        return build_workload_cisd(cfg, precision)
+    ss = synthetic.make_system(N, (na, nb), G, decay=cfg["decay"], seed=0, h0=0.0)
     wk = "restricted" if kind == "rhf_r" else "unrestricted"
     sysm = tg.System(norb=N, nelec=(na, nb), walker_kind=wk)
     ham = tg.HamChol(h0=ss.h0, h1=ss.h1, chol=ss.chol)
@@ -143,6 +166,36 @@ def build_workload(cfg, precision):
     return dict(tg=tg, ss=ss, sys=sysm, ham=ham, params=params, trial=trial, trial_ops=trial_ops,
                 meas_ops=meas_ops, meas_ctx=meas_ctx, prop_ops=prop_ops, prop_ctx=prop_ctx, state=state, e=e,
                 W=W, N=N, na=na, nb=nb, G=G, qr_every=cfg["qr_every"], kind=kind)
+
+
+def build_workload_cisd(cfg, precision):
+    """CISD trial (N, nocc, G) with restricted walkers; "mixed" = the reference's
+    default CISD dtypes (tensor-core l2ci2, FP32 gl), "fp64" = testing=True."""
+    import torch
+
+    import trot_gb300 as tg
+    from trot_gb300 import synthetic
+
+    N, (n, _), G, W = cfg["norb"], cfg["nelec"], cfg["nchol"], cfg["n_walkers"]
+    cs = synthetic.make_cisd_system(N, n, G, decay=cfg["decay"], seed=0, h0=0.0)
+    sysm = tg.System(norb=N, nelec=(n, n), walker_kind="restricted")
+    ham = tg.HamChol(h0=cs.h0, h1=cs.h1, chol=cs.chol)
+    params = tg.QmcParams(dt=cfg["dt"], n_walkers=W, n_prop_steps=cfg["qr_every"], seed=1234)
+    trial = tg.CisdTrial(cs.ci1, cs.ci2)
+    trial_ops = tg.make_cisd_trial_ops(sysm)
+    if precision == "mixed":
+        meas_ops = tg.make_cisd_meas_ops(sysm)
+    else:
+        meas_ops = tg.make_cisd_meas_ops(sysm, mixed_precision=False, testing=True)
+    meas_ctx = meas_ops.build_meas_ctx(ham, trial)
+    prop_ops = tg.make_prop_ops("restricted", "restricted")
+    prop_ctx = prop_ops.build_prop_ctx(ham, trial_ops.get_rdm1(trial), params)
+    state = prop_ops.init_prop_state(sys=sysm, ham_data=ham, trial_ops=trial_ops, trial_data=trial,
+                                     meas_ops=meas_ops, params=params)
+    e = torch.empty(W, dtype=torch.complex128, device="cuda")
+    return dict(tg=tg, ss=cs, sys=sysm, ham=ham, params=params, trial=trial, trial_ops=trial_ops,
+                meas_ops=meas_ops, meas_ctx=meas_ctx, prop_ops=prop_ops, prop_ctx=prop_ctx, state=state, e=e,
+                W=W, N=N, na=n, nb=n, G=G, qr_every=cfg["qr_every"], kind="cisd")
 
 
 def run_steps(wl, nsteps, k0=0, fields_host=None, pinned_e=None):
@@ -185,6 +238,38 @@ def block_tail(wl, st):
     return st._replace(walkers=w_sr, weights=weights_sr, overlaps=ov_sr)
 
 
+def perturbed_trial_walkers(wl, noise, seed=21):
+    """W walkers = trial orbitals + complex Gaussian noise (the parity tests' recipe)."""
+    import torch
+
+    from trot_gb300 import synthetic
+
+    W, N = wl["W"], wl["N"]
+    if wl["kind"] == "cisd":
+        return torch.as_tensor(synthetic.perturbed_walkers(np.eye(N)[:, :wl["na"]], W, noise, seed)).cuda()
+    wa = torch.as_tensor(synthetic.perturbed_walkers(wl["ss"].mo_a, W, noise, seed)).cuda()
+    if wl["kind"] == "rhf_r":
+        return wa
+    return wa, torch.as_tensor(synthetic.perturbed_walkers(wl["ss"].mo_b, W, noise, seed + 1)).cuda()
+
+
+def max_over_ranks(x: float, world: int, device="cuda") -> float:
+    """Largest value of ``x`` over the ranks of the process group (the job's
+    time is its slowest replica's); ``x`` itself when running alone."""
+    if world <= 1:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Whole-job throughput: the units all replicas processed over the slowest time."""
+    return units_per_rank * world / seconds
+
+
 def flush_l2(buf):
     buf.add_(1.0)
 
@@ -197,13 +282,23 @@ def cpu_port_rate(cfg, W_sample, steps, threads=None, min_seconds=0.0, max_steps
     from trot_gb300 import synthetic
 
     N, (na, nb), G = cfg["norb"], cfg["nelec"], cfg["nchol"]
-    ss = synthetic.make_system(N, (na, nb), G, decay=cfg["decay"], seed=0, h0=0.0)
     kind = cfg["kind"]
-    prop = orc.build_prop_ctx(ss.h0, ss.h1, ss.chol, ss.rdm1(), cfg["dt"])
-    if kind == "uhf_u":
+    if kind == "cisd":
+        from oracle import cisd_oracle as co
+
+        ss = synthetic.make_cisd_system(N, na, G, decay=cfg["decay"], seed=0, h0=0.0)
+        mo = np.eye(N)[:, :na]
+        prop = orc.build_prop_ctx(ss.h0, ss.h1, ss.chol, np.stack([mo @ mo.T] * 2), cfg["dt"])
+        m = co.CisdModel(co.CisdTrial(ss.ci1, ss.ci2), ss.h0, ss.h1, ss.chol, prop)
+        w = synthetic.perturbed_walkers(mo, W_sample, 0.0)
+    elif kind == "uhf_u":
+        ss = synthetic.make_system(N, (na, nb), G, decay=cfg["decay"], seed=0, h0=0.0)
+        prop = orc.build_prop_ctx(ss.h0, ss.h1, ss.chol, ss.rdm1(), cfg["dt"])
         m = orc.Model(kind, ss.h0, (ss.mo_a, ss.mo_b), orc.build_uhf_meas_ctx(ss.h1, ss.chol, ss.mo_a, ss.mo_b), prop)
         w = (synthetic.perturbed_walkers(ss.mo_a, W_sample, 0.0), synthetic.perturbed_walkers(ss.mo_b, W_sample, 0.0))
     else:
+        ss = synthetic.make_system(N, (na, nb), G, decay=cfg["decay"], seed=0, h0=0.0)
+        prop = orc.build_prop_ctx(ss.h0, ss.h1, ss.chol, ss.rdm1(), cfg["dt"])
         m = orc.Model(kind, ss.h0, ss.mo_a, orc.build_rhf_meas_ctx(ss.h1, ss.chol, ss.mo_a), prop)
         w = synthetic.perturbed_walkers(ss.mo_a, W_sample, 0.0)
     fields = synthetic.fields(W_sample, G, 2, seed=9)
@@ -250,7 +345,8 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     N, (na, nb), G, W = cfg["norb"], cfg["nelec"], cfg["nchol"], cfg["n_walkers"]
-    fl = flops_per_walker_step(N, na, nb, G)
+    fl = flops_per_walker_step_cisd(N, na, G) if cfg["kind"] == "cisd" else flops_per_walker_step(N, na, nb, G)
+    nspin = 1 if cfg["kind"] in ("rhf_r", "cisd") else 2
     config = {"workload": f"{cfg['kind']} N={N} nelec=({na},{nb}) G={G} W={W} dt={cfg['dt']} "
                           f"qr/sr every {cfg['qr_every']}", "walkers": W, "norb": N, "nelec": [na, nb],
               "nchol": G, "trial": cfg["kind"], "seed": 0}
@@ -316,11 +412,8 @@ def main():
     ms = ev0.elapsed_time(ev1)
     prof = _lib.profile_collect()
     _lib.profile_enable(0)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = W * args.steps * world / (ms / 1e3)
+    ms = max_over_ranks(ms, world)
+    value = job_rate(W * args.steps, world, ms / 1e3)
 
     if args.profile_run:
         if rank == 0:
@@ -338,11 +431,8 @@ def main():
     torch.cuda.synchronize()
     barrier()
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": W * k_e2e * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": W * G * 8,
+    e2e_s = max_over_ranks(e2e_s, world)
+    e2e = {"value": job_rate(W * k_e2e, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": W * G * 8,
            "d2h_bytes_per_step": W * 16, "steps": k_e2e}
     # precision: mixed vs FP64 local energy on the run's own (identical) walkers
     precision_info = None
@@ -351,16 +441,31 @@ def main():
         import trot_gb300 as tg
 
         st = wl["state"]
+        mc64 = wl["meas_ctx"]
         if wl["kind"] == "uhf_u":
             m64 = tg.make_uhf_meas_ops(wl["sys"])
+        elif wl["kind"] == "cisd":
+            m64 = tg.make_cisd_meas_ops(wl["sys"], mixed_precision=False, testing=True)
+            mc64 = m64.build_meas_ctx(wl["ham"], wl["trial"])
         else:
             m64 = tg.make_rhf_meas_ops(wl["sys"])
-        e64 = m64.kernels["energy"](st.walkers, wl["ham"], wl["meas_ctx"], wl["trial"])
+        e64 = m64.kernels["energy"](st.walkers, wl["ham"], mc64, wl["trial"])
         emx = wl["meas_ops"].kernels["energy"](st.walkers, wl["ham"], wl["meas_ctx"], wl["trial"])
         d = (emx - e64).abs()
         precision_info = {"max_abs_dE_L_Ha": float(d.max()), "median_abs_dE_L_Ha": float(d.median()),
                           "max_abs_E_L_Ha": float(e64.abs().max()), "walkers": W,
                           "on": "the benchmark's walkers after warm-up + timed + e2e steps (identical walkers)"}
+        # the seeded recipe's population decays within a few steps (|E_L| up to ~1e6 Ha), so the
+        # same comparison is also made on walkers near the trial, where E_L is physical
+        near = {}
+        for noise in (0.05, 0.3):
+            wn = perturbed_trial_walkers(wl, noise)
+            a64 = m64.kernels["energy"](wn, wl["ham"], mc64, wl["trial"])
+            amx = wl["meas_ops"].kernels["energy"](wn, wl["ham"], wl["meas_ctx"], wl["trial"])
+            dd = (amx - a64).abs()
+            near[f"noise_{noise}"] = {"max_abs_dE_L_Ha": float(dd.max()), "median_abs_dE_L_Ha": float(dd.median()),
+                                      "max_abs_E_L_Ha": float(a64.abs().max())}
+        precision_info["near_trial_walkers"] = near
         # FP64 path on the same workload, same device, a few steps
         wl64 = build_workload(cfg, "fp64")
         run_steps(wl64, 1)
@@ -383,9 +488,17 @@ def main():
     # roofline of the dominant kernel
     top = max(prof.items(), key=lambda kv: kv[1][0]) if prof else ("none", (0.0, 1))
     tname, (tms, tcnt) = top
-    fl_map = {"vhs": fl["vhs"], "exchange_exact": fl["exchange"] + fl["force_bias"], "exchange": fl["exchange"],
-              "trotter": fl["taylor"] + fl["onebody"] + fl["overlap"], "force_bias": fl["force_bias"],
-              "green": fl["green"]}
+    # algorithmic flops per walker of one launch: the exchange kernel runs once per spin
+    if cfg["kind"] == "cisd":
+        v_ = N - na
+        fl_map = {"cisd_gamma": fl["gl"] + fl["lci2_green"] + fl["glgp"] + fl["lg1"],
+                  "cisd_l2ci2": 4 * G * (na * v_) ** 2,  # one quadratic form with the combined ci2m
+                  "cisd_chol_gemm": 4 * G * na * N, "cisd_ci2g": 4 * (na * v_) ** 2, "vhs": fl["vhs"],
+                  "trotter": fl["taylor"] + fl["onebody"]}
+    else:
+        fl_map = {"vhs": fl["vhs"], "exchange_exact": (fl["exchange"] + fl["force_bias"]) / nspin,
+                  "exchange": fl["exchange"], "trotter": fl["taylor"] + fl["onebody"] + fl["overlap"],
+                  "force_bias": fl["force_bias"], "green": fl["green"]}
     kfl = next((v for k, v in fl_map.items() if tname.startswith(k)), sum(fl.values()))
     per_launch_s = tms / max(tcnt, 1) / 1e3
     achieved_tflops = kfl * W / per_launch_s / 1e12 if per_launch_s > 0 else 0.0

@@ -1,5 +1,6 @@
 """Host-side operand preparation of the mixed-precision path (no GPU)."""
 import numpy as np
+import pytest
 import torch
 
 from trot_gb300 import mixed
@@ -46,3 +47,23 @@ def test_rot_tiles_layout():
     np.testing.assert_allclose(rec, rc[13, 4], rtol=0, atol=2.0 ** -40 * np.max(np.abs(rc[13, 4])))
     assert np.all(qd[:, :, :, N:] == 0)
     assert np.all(qd[:, 2, 5 * n:, :] == 0)  # last block holds 5 vectors
+
+
+@pytest.mark.parametrize("kchunk", [32, 64])
+def test_split3_image_layout(kchunk):
+    """Tensor-core operand image of B^T: [ncols/128][K/kchunk][3][128][kchunk] in
+    8 x 8 core-matrix order; the three BF16 terms add up to the FP64 value to ~2^-24."""
+    rng = np.random.default_rng(3)
+    bt = rng.normal(size=(150, 70))
+    img, npad, kpad = mixed.split3_image(bt, kchunk=kchunk)
+    assert npad == 256 and kpad == (70 + kchunk - 1) // kchunk * kchunk
+    assert tuple(img.shape) == (2, kpad // kchunk, 3, 128, kchunk)
+    a = img.to(torch.float64).numpy().reshape(2, kpad // kchunk, 3, 16, kchunk // 8, 8, 8)
+    # (nt, nk, slice, rg, kg, r, k) -> (slice, nt, rg, r, nk, kg, k)
+    m = a.transpose(2, 0, 3, 5, 1, 4, 6).reshape(3, npad, kpad)
+    rec = m.sum(axis=0)
+    np.testing.assert_allclose(rec[:150, :70], bt, rtol=2.0 ** -23, atol=0)
+    assert np.all(rec[150:] == 0) and np.all(rec[:, 70:] == 0)
+    # the image's first row of the first chunk is contiguous in 8-element core-matrix rows
+    flat = img.to(torch.float64).numpy().reshape(2, kpad // kchunk, 3, -1)
+    assert flat[0, 0, 0, 1] == m[0, 0, 1]

@@ -19,21 +19,23 @@ namespace trot {
 
 // ------------------------------------------------------------------ float-float
 struct ff { float hi, lo; };
+// The error-free transformations below rely on the rounded value of every sum and
+// product, so they use the _rn intrinsics, which the compiler never contracts into FMAs.
 TROT_D ff ff_two_sum(float a, float b) {
-  const float s = a + b, bb = s - a;
-  return ff{s, (a - (s - bb)) + (b - bb)};
+  const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+  return ff{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
 }
 TROT_D ff ff_fast(float a, float b) {
-  const float s = a + b;
-  return ff{s, b - (s - a)};
+  const float s = __fadd_rn(a, b);
+  return ff{s, __fsub_rn(b, __fsub_rn(s, a))};
 }
 TROT_D ff ff_add(ff x, ff y) {
   ff s = ff_two_sum(x.hi, y.hi);
-  return ff_fast(s.hi, s.lo + x.lo + y.lo);
+  return ff_fast(s.hi, __fadd_rn(__fadd_rn(s.lo, x.lo), y.lo));
 }
 TROT_D ff ff_sub(ff x, ff y) { return ff_add(x, ff{-y.hi, -y.lo}); }
 TROT_D ff ff_mul(ff x, ff y) {
-  const float p = x.hi * y.hi;
+  const float p = __fmul_rn(x.hi, y.hi);
   float e = fmaf(x.hi, y.hi, -p);
   e = fmaf(x.hi, y.lo, e);
   e = fmaf(x.lo, y.hi, e);
@@ -44,6 +46,18 @@ TROT_D double ff_d(ff x) { return (double)x.hi + (double)x.lo; }
 TROT_D float pow2f(int e) { return __int_as_float((e + 127) << 23); }
 TROT_D ff ff_shfl_xor(ff x, int o) {
   return ff{__shfl_xor_sync(0xffffffffu, x.hi, o), __shfl_xor_sync(0xffffffffu, x.lo, o)};
+}
+// acc += a b (float-float operands): exact product of the high parts (TwoProd) plus
+// the cross terms; the high parts are summed with TwoSum and the low parts in plain
+// FP32, renormalised once by the caller (ff_fast) after at most a few dozen terms.
+TROT_D void ff_mad(ff& acc, ff a, ff b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const ff t = ff_two_sum(acc.hi, p);
+  acc.hi = t.hi;
+  acc.lo = __fadd_rn(acc.lo, __fadd_rn(t.lo, e));
 }
 
 // ------------------------------------------------------------------ Green's functions in float-float
@@ -84,15 +98,35 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
     }
     __syncthreads();
     for (int e = tid; e < n * n; e += nt) {
+      // four independent accumulator pairs over p (mod 4): the N-long dot products are
+      // latency-bound chains otherwise
       const int i = e / n, j = e % n;
-      ff ar{0.f, 0.f}, ai{0.f, 0.f};
-      for (int p = 0; p < N; ++p) {
+      ff ar[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      ff ai[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      int p = 0;
+      for (; p + 4 <= N; p += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const ff c = Cf[(p + u) * n + i];
+          const ffc x = Wf[(p + u) * n + j];
+          ff_mad(ar[u], c, x.re);
+          ff_mad(ai[u], c, x.im);
+        }
+      }
+      for (; p < N; ++p) {
         const ff c = Cf[p * n + i];
         const ffc x = Wf[p * n + j];
-        ar = ff_fma(ar, c, x.re);
-        ai = ff_fma(ai, c, x.im);
+        ff_mad(ar[0], c, x.re);
+        ff_mad(ai[0], c, x.im);
       }
-      Md[e] = make_double2(ff_d(ar), ff_d(ai));
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        ar[u] = ff_fast(ar[u].hi, ar[u].lo);
+        ai[u] = ff_fast(ai[u].hi, ai[u].lo);
+      }
+      const ff sr = ff_add(ff_add(ar[0], ar[1]), ff_add(ar[2], ar[3]));
+      const ff si = ff_add(ff_add(ai[0], ai[1]), ff_add(ai[2], ai[3]));
+      Md[e] = make_double2(ff_d(sr), ff_d(si));
     }
     __syncthreads();
     block_gauss_jordan(Md, n, n, Mi, &piv, red);
@@ -106,11 +140,13 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
       ff gr{0.f, 0.f}, gi{0.f, 0.f};
       for (int j = 0; j < n; ++j) {
         const ffc x = Wf[p * n + j], y = Mif[j * n + i];
-        gr = ff_fma(gr, x.re, y.re);
-        gr = ff_sub(gr, ff_mul(x.im, y.im));
-        gi = ff_fma(gi, x.re, y.im);
-        gi = ff_fma(gi, x.im, y.re);
+        ff_mad(gr, x.re, y.re);
+        ff_mad(gr, ff{-x.im.hi, -x.im.lo}, y.im);
+        ff_mad(gi, x.re, y.im);
+        ff_mad(gi, x.im, y.re);
       }
+      gr = ff_fast(gr.hi, gr.lo);
+      gi = ff_fast(gi.hi, gi.lo);
       gout[e] = make_double2(ff_d(gr), ff_d(gi));
       if (H) {
         const ff h = ff_from_d(H[e]);
@@ -141,12 +177,12 @@ static int launch_green_ff(const Spins& sp, int W, int N, const double2* wa, con
 }
 
 // ------------------------------------------------------------------ layouts
-static constexpr size_t kTcChunkBytes = 3 * 128 * 64 * 2;  // one A chunk of the tensor-core Trotter kernel
+static constexpr size_t kTcImgBytes = 3 * 128 * 256 * 2;  // [Vr | Vi] operand image of one walker (192 KB)
 static constexpr int kKP = 128;       // padded orbital dimension of the exact product
 static constexpr int kBN = 48;        // MMA N of the exchange tile (columns = walker rows)
 static constexpr int kGroups = 5;     // accumulators for t + u = 0..4
 static constexpr int kSlices = 5;
-static constexpr int kSlots = 3;      // ring of Green's-function slice buffers
+static constexpr int kSlots = 2;      // ring of Green's-function slice buffers
 static constexpr int kMaxOcc = 16;    // largest n the epilogue handles (2 * n_pad <= 32 columns per walker)
 static constexpr uint32_t kAImg = (uint32_t)kSlices * 128 * kKP * 2;  // 163840 B: 5 rot slices of a tile
 static constexpr uint32_t kBImg = (uint32_t)kBN * kKP * 2;            // 12288 B: one green slice of a tile
@@ -165,7 +201,7 @@ struct SpinLayout {
 static SpinLayout spin_layout(const trot_system* s, const Spins& sp, int q) {
   SpinLayout L{};
   L.n = sp.n[q];
-  L.n_pad = L.n + (L.n & 1);
+  L.n_pad = (L.n + 3) & ~3;  // 4 column quarters per walker in the exchange epilogue
   L.S = 2 * L.n_pad;
   L.WB = kBN / L.S;
   L.ntiles = (s->n_walkers + L.WB - 1) / L.WB;
@@ -189,6 +225,7 @@ struct MixedBuffers {
   uint16_t* xq;
   float* vhs;
   uint16_t* vimg;  // [Vr | Vi] operand images of the tensor-core Trotter kernel
+  double2* ov_new; // overlaps of the propagated walkers (tensor-core Trotter, step mode)
   int* node_flag;
   int* status;
   int nblk_total, mpad;
@@ -219,7 +256,10 @@ static size_t carve_mixed(const trot_system* s, const Spins& sp, Carver& c, Mixe
     m.xs = c.take<double2>(W * G);
     m.xq = c.take<uint16_t>((size_t)s->mixed->vhs_slices * m.mpad * s->mixed->gpad);
     m.vhs = c.take<float>((size_t)m.mpad * s->mixed->n2pad);
-    if (s->mixed->exp_h1_half_img) m.vimg = c.take<uint16_t>(W * 4 * (size_t)(kTcChunkBytes / 2));
+    if (s->mixed->exp_h1_half_img) {
+      m.vimg = c.take<uint16_t>(W * (kTcImgBytes / 2));
+      m.ov_new = c.take<double2>(W);
+    }
     m.shift_term = c.take<double2>(W);
     m.fb_term = c.take<double2>(W);
     m.node_flag = c.take<int>(W);
@@ -306,7 +346,8 @@ green_slices_kernel(int N, int n, int n_pad, int WB, int W, int ntot, int off, c
 // traces c_g = sum_i f_gii (Coulomb / force bias, trot/meas/rhf.py:119-125).
 struct ExArgs {
   SpinLayout L;
-  int G, W, mult, tiles_per_cta;
+  int G, W, mult;
+  int tiles_per_item, chunks, n_items;  // work item = (Cholesky block, run of walker tiles)
   const uint16_t* rot_img;   // [nblk][slices][128][kKP] core-matrix order
   const int32_t* rot_e;      // [nblk][128]
   const uint16_t* green_img; // [ntiles][slices][kBN][kKP]
@@ -317,16 +358,18 @@ struct ExArgs {
   int* status;
 };
 
-static constexpr int kExThreads = 288;  // 8 epilogue warps + 1 producer warp
+static constexpr int kExThreads = 544;  // 16 epilogue warps + 1 producer warp
+static constexpr int kExEpi = 512;      // epilogue threads
 static constexpr size_t kExOffRing = kAImg;
-static constexpr size_t kExOffF = kExOffRing + (size_t)kSlots * kBImg;        // [128][16] ff
-static constexpr size_t kExOffEA = kExOffF + (size_t)128 * kMaxOcc * sizeof(ff);
+static constexpr int kFS = kMaxOcc + 1;  // row stride of the f staging arrays (padded against bank conflicts)
+static constexpr size_t kExOffF = kExOffRing + (size_t)kSlots * kBImg;        // re, im: [128][kFS] ff each
+static constexpr size_t kExOffEA = kExOffF + (size_t)2 * 128 * kFS * sizeof(ff);
 static constexpr size_t kExOffC = kExOffEA + 128 * 4;                          // [128][2] ff traces
-static constexpr size_t kExOffRed = kExOffC + 128 * 2 * sizeof(ff);            // [8 warps][2] ff
-static constexpr size_t kExOffBar = kExOffRed + 8 * 2 * sizeof(ff);            // 11 mbarriers + flags
+static constexpr size_t kExOffRed = kExOffC + 128 * 2 * sizeof(ff);            // [16 warps][2] ff
+static constexpr size_t kExOffBar = kExOffRed + 16 * 2 * sizeof(ff);           // 11 mbarriers + flags
 static constexpr size_t kExSmem = kExOffBar + 16 * 8 + 64;
 
-// JH = n_pad / 2 columns j per epilogue warp (static so the per-row values stay
+// JH = n_pad / 4 columns j per epilogue warp (static so the per-row values stay
 // in registers); columns j >= n are exactly zero and contribute nothing.
 template <int JH>
 __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a) {
@@ -335,91 +378,98 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
   unsigned char* sA = base;
   unsigned char* ring = base + kExOffRing;
   ff* sF = reinterpret_cast<ff*>(base + kExOffF);
-  int* eA = reinterpret_cast<int*>(base + kExOffEA);
   ff* sC = reinterpret_cast<ff*>(base + kExOffC);
   ff* sRed = reinterpret_cast<ff*>(base + kExOffRed);
   uint64_t* bars = reinterpret_cast<uint64_t*>(base + kExOffBar);
   uint64_t* a_full = bars;
-  uint64_t* full = bars + 1;        // [kSlots]
-  uint64_t* empty = bars + 4;       // [kSlots]
+  uint64_t* full = bars + 1;        // [kSlots <= 3]
+  uint64_t* empty = bars + 4;       // [kSlots <= 3]
   uint64_t* acc_full = bars + 7;    // [2]
   uint64_t* acc_empty = bars + 9;   // [2]
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 11);
   int* flag = reinterpret_cast<int*>(bars + 12);  // epilogue go/stop broadcast
+  uint64_t* a_free = bars + 13;     // the MMAs of the previous work item are done with sA
 
   const SpinLayout& L = a.L;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int blk = blockIdx.x;
-  const int t0 = blockIdx.y * a.tiles_per_cta, t1 = min(L.ntiles, t0 + a.tiles_per_cta);
-  if (t0 >= t1) return;
-  const int ntl = t1 - t0;
+  if ((int)blockIdx.x >= a.n_items) return;
 
-  if (warp == 8) tc::tmem_alloc(tslot, 512);
-  if (tid == 256) {
+  if (warp == 16) tc::tmem_alloc(tslot, 512);
+  if (tid == kExEpi) {
     tc::mbar_init(a_full, 1);
+    tc::mbar_init(a_free, 1);
     for (int k = 0; k < kSlots; ++k) {
       tc::mbar_init(&full[k], 1);
       tc::mbar_init(&empty[k], 1);
     }
     for (int k = 0; k < 2; ++k) {
       tc::mbar_init(&acc_full[k], 1);
-      tc::mbar_init(&acc_empty[k], 8);
+      tc::mbar_init(&acc_empty[k], 16);
     }
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  if (tid < 128) eA[tid] = a.rot_e[(size_t)blk * 128 + tid];
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = *tslot;
 
-  if (warp == 8) {
+  if (warp == 16) {
     // ------------------------------------------------ producer: loads + MMAs (one lane)
     if (lane == 0) {
       bool ok = true;
       const uint32_t idesc = tc::idesc_bf16_f32(128, kBN);
       const uint32_t sA_u = tc::smem_u32(sA), ring_u = tc::smem_u32(ring);
-      tc::mbar_expect_tx(a_full, kAImg);
-      tc::bulk_g2s(sA, a.rot_img + (size_t)blk * (kAImg / 2), kAImg, a_full);
-      const int total = ntl * kSlices;
-      int nl = 0;  // slices issued
-      for (int sidx = 0; sidx < total && ok; ++sidx) {
-        const int i = sidx / kSlices, u = sidx % kSlices;
-        // keep up to kSlots slice copies in flight ahead of the MMAs
-        while (nl < total && nl < sidx + kSlots && ok) {
-          const int slot = nl % kSlots;
-          if (nl >= kSlots) ok = tc::mbar_wait(&empty[slot], (uint32_t)((nl / kSlots - 1) & 1));
-          if (!ok) break;
-          const int ti = t0 + nl / kSlices, tu = nl % kSlices;
-          tc::mbar_expect_tx(&full[slot], kBImg);
-          tc::bulk_g2s(ring + (size_t)slot * kBImg, a.green_img + ((size_t)ti * kSlices + tu) * (kBImg / 2), kBImg,
-                       &full[slot]);
-          ++nl;
-        }
+      int g_issue = 0, g_base = 0, tg = 0, kitem = 0;  // CTA-wide slice / tile / item counters
+      for (int item = blockIdx.x; item < a.n_items && ok; item += gridDim.x, ++kitem) {
+        const int blk = item / a.chunks;
+        const int t0 = (item % a.chunks) * a.tiles_per_item, t1 = min(L.ntiles, t0 + a.tiles_per_item);
+        const int ntl = t1 - t0, total = ntl * kSlices;
+        if (kitem > 0) ok = tc::mbar_wait(a_free, (uint32_t)((kitem - 1) & 1));
         if (!ok) break;
-        const int abuf = i & 1;
-        if (u == 0) {
-          if (i == 0) ok = tc::mbar_wait(a_full, 0u);
-          if (ok && i >= 2) ok = tc::mbar_wait(&acc_empty[abuf], (uint32_t)(((i - 2) / 2) & 1));
-          if (!ok) break;
-        }
-        const int slot = sidx % kSlots;
-        ok = tc::mbar_wait(&full[slot], (uint32_t)((sidx / kSlots) & 1));
-        if (!ok) break;
-        tc::fence_after_sync();
-        const int tmax = min(kSlices - 1, (kGroups - 1) - u);
-        for (int t = 0; t <= tmax; ++t) {
-          const int d = t + u;
-#pragma unroll
-          for (int ks = 0; ks < kKP / 16; ++ks) {
-            const uint64_t ad = tc::smem_desc(sA_u + (uint32_t)(t * 128 * kKP * 2 + ks * 256), 128, kKP * 16);
-            const uint64_t bd = tc::smem_desc(ring_u + (uint32_t)(slot * kBImg + ks * 256), 128, kKP * 16);
-            tc::mma_bf16(taddr + (uint32_t)(abuf * kGroups * kBN + d * kBN), ad, bd, idesc,
-                         (u == 0 && ks == 0) ? 0u : 1u);
+        tc::mbar_expect_tx(a_full, kAImg);
+        tc::bulk_g2s(sA, a.rot_img + (size_t)blk * (kAImg / 2), kAImg, a_full);
+        for (int sidx = 0; sidx < total && ok; ++sidx) {
+          const int i = sidx / kSlices, u = sidx % kSlices;
+          // keep up to kSlots slice copies of this item in flight ahead of the MMAs
+          while (g_issue < g_base + total && g_issue < g_base + sidx + kSlots && ok) {
+            const int slot = g_issue % kSlots;
+            if (g_issue >= kSlots) ok = tc::mbar_wait(&empty[slot], (uint32_t)((g_issue / kSlots - 1) & 1));
+            if (!ok) break;
+            const int li = g_issue - g_base;
+            const int ti = t0 + li / kSlices, tu = li % kSlices;
+            tc::mbar_expect_tx(&full[slot], kBImg);
+            tc::bulk_g2s(ring + (size_t)slot * kBImg, a.green_img + ((size_t)ti * kSlices + tu) * (kBImg / 2), kBImg,
+                         &full[slot]);
+            ++g_issue;
           }
+          if (!ok) break;
+          const int tgi = tg + i, abuf = tgi & 1;
+          if (u == 0) {
+            if (i == 0) ok = tc::mbar_wait(a_full, (uint32_t)(kitem & 1));
+            if (ok && tgi >= 2) ok = tc::mbar_wait(&acc_empty[abuf], (uint32_t)(((tgi - 2) / 2) & 1));
+            if (!ok) break;
+          }
+          const int gs = g_base + sidx, slot = gs % kSlots;
+          ok = tc::mbar_wait(&full[slot], (uint32_t)((gs / kSlots) & 1));
+          if (!ok) break;
+          tc::fence_after_sync();
+          const int tmax = min(kSlices - 1, (kGroups - 1) - u);
+          for (int t = 0; t <= tmax; ++t) {
+            const int d = t + u;
+#pragma unroll
+            for (int ks = 0; ks < kKP / 16; ++ks) {
+              const uint64_t ad = tc::smem_desc(sA_u + (uint32_t)(t * 128 * kKP * 2 + ks * 256), 128, kKP * 16);
+              const uint64_t bd = tc::smem_desc(ring_u + (uint32_t)(slot * kBImg + ks * 256), 128, kKP * 16);
+              tc::mma_bf16(taddr + (uint32_t)(abuf * kGroups * kBN + d * kBN), ad, bd, idesc,
+                           (u == 0 && ks == 0) ? 0u : 1u);
+            }
+          }
+          tc::mma_commit(&empty[slot]);
+          if (u == kSlices - 1) tc::mma_commit(&acc_full[abuf]);
         }
-        tc::mma_commit(&empty[slot]);
-        if (u == kSlices - 1) tc::mma_commit(&acc_full[abuf]);
+        if (ok) tc::mma_commit(a_free);
+        g_base += total;
+        tg += ntl;
       }
       if (!ok) {
         atomicExch(a.status, (int)TROT_ERR_DEVICE_TIMEOUT);
@@ -429,26 +479,33 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
     }
     __syncwarp();
   } else {
-    // ------------------------------------------------ epilogue: 8 warps
+    // ------------------------------------------------ epilogue: 16 warps (lane quarter q, column quarter h)
     const int q = warp & 3, h = warp >> 2;
     const int r = q * 32 + lane;
     const int i = r % L.n, gl = r / L.n;
     const int j0 = h * JH;
-    const int etid = tid;  // 0..255
-    for (int it = 0; it < ntl; ++it) {
-      const int tile = t0 + it, abuf = it & 1;
-      if (etid == 0) *flag = tc::mbar_wait(&acc_full[abuf], (uint32_t)((it / 2) & 1)) ? 1 : 0;
-      tc::named_bar(1, 256);
+    const int etid = tid;  // 0..511
+    bool stop = false;
+    int tgl = 0;  // CTA-wide tile counter (TMEM buffer and phase)
+    for (int item = blockIdx.x; item < a.n_items && !stop; item += gridDim.x) {
+    const int blk = item / a.chunks;
+    const int t0 = (item % a.chunks) * a.tiles_per_item, t1 = min(L.ntiles, t0 + a.tiles_per_item);
+    const int ntl = t1 - t0;
+    const int rows_valid = min(L.gb, a.G - blk * L.gb) * L.n;
+    const bool rvalid = r < rows_valid;
+    const int ea = a.rot_e[(size_t)blk * 128 + r];
+    for (int it = 0; it < ntl; ++it, ++tgl) {
+      const int tile = t0 + it, abuf = tgl & 1;
+      if (etid == 0) *flag = tc::mbar_wait(&acc_full[abuf], (uint32_t)((tgl / 2) & 1)) ? 1 : 0;
+      tc::named_bar(1, kExEpi);
       if (!*flag) {
         if (etid == 0) atomicExch(a.status, (int)TROT_ERR_DEVICE_TIMEOUT);
+        stop = true;
         break;
       }
       tc::fence_after_sync();
-      const int rows_valid = min(L.gb, a.G - blk * L.gb) * L.n;
-      const bool rvalid = r < rows_valid;
       const uint32_t tlane = taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(abuf * kGroups * kBN);
       const int32_t* eB = a.green_e + (size_t)tile * kBN;
-      const int ea = eA[r];
       for (int bl = 0; bl < L.WB; ++bl) {
         const int b = tile * L.WB + bl;
         if (b >= a.W) break;  // uniform across the epilogue warps
@@ -485,38 +542,37 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
               if (c == 0) fre[jj] = y; else fim[jj] = y;
             }
         }
-        // exchange: sum_j f_ij f_ji, re parts of f_ji first, then im parts
-        ff xr{0.f, 0.f}, xi{0.f, 0.f};
-        ff trv{0.f, 0.f}, tiv{0.f, 0.f};  // f_ii (re, im) of this row, read back from the full row in sF
+        // exchange sum_j f_ij f_ji: stage re and im of this row's f values, one barrier
         const int brow = gl * L.n;
+        ff* sFr = sF;
+        ff* sFi = sF + 128 * kFS;
 #pragma unroll
-        for (int pass = 0; pass < 2; ++pass) {
-#pragma unroll
-          for (int jj = 0; jj < JH; ++jj) sF[r * kMaxOcc + j0 + jj] = pass == 0 ? fre[jj] : fim[jj];
-          tc::named_bar(1, 256);
-          if (rvalid && h == 0) {
-            if (pass == 0) trv = sF[r * kMaxOcc + i]; else tiv = sF[r * kMaxOcc + i];
-          }
-          if (rvalid) {
-#pragma unroll
-            for (int jj = 0; jj < JH; ++jj) {
-              const ff o = sF[(brow + j0 + jj) * kMaxOcc + i];  // re (pass 0) or im (pass 1) of f_ji
-              if (pass == 0) {  // (a + ib)(c + id): += a c, += b c (imag)
-                xr = ff_add(xr, ff_mul(fre[jj], o));
-                xi = ff_add(xi, ff_mul(fim[jj], o));
-              } else {          // -= b d, += a d (imag)
-                xr = ff_sub(xr, ff_mul(fim[jj], o));
-                xi = ff_add(xi, ff_mul(fre[jj], o));
-              }
-            }
-          }
-          tc::named_bar(1, 256);
+        for (int jj = 0; jj < JH; ++jj) {
+          sFr[r * kFS + j0 + jj] = fre[jj];
+          sFi[r * kFS + j0 + jj] = fim[jj];
         }
-        if (rvalid && h == 0) {
-          sC[2 * r] = trv;
-          sC[2 * r + 1] = tiv;
+        tc::named_bar(1, kExEpi);
+        ff xr{0.f, 0.f}, xi{0.f, 0.f};
+        if (rvalid) {
+#pragma unroll
+          for (int jj = 0; jj < JH; ++jj) {
+            // padding columns j >= n contribute nothing; their row brow + j may lie past this
+            // Cholesky vector (or past row 127), so they are skipped rather than multiplied by 0
+            if (j0 + jj >= L.n) break;
+            const ff orr = sFr[(brow + j0 + jj) * kFS + i], oi = sFi[(brow + j0 + jj) * kFS + i];
+            // (a + ib)(c + id) = (ac - bd) + i(ad + bc)
+            ff_mad(xr, fre[jj], orr);
+            ff_mad(xr, ff{-fim[jj].hi, -fim[jj].lo}, oi);
+            ff_mad(xi, fre[jj], oi);
+            ff_mad(xi, fim[jj], orr);
+          }
+          if (h == 0) {  // f_ii of this row for the trace (force bias)
+            sC[2 * r] = sFr[r * kFS + i];
+            sC[2 * r + 1] = sFi[r * kFS + i];
+          }
         }
-        if (!rvalid) { xr = ff{0.f, 0.f}; xi = ff{0.f, 0.f}; }
+        xr = ff_fast(xr.hi, xr.lo);
+        xi = ff_fast(xi.hi, xi.lo);
         for (int o = 16; o > 0; o >>= 1) {
           xr = ff_add(xr, ff_shfl_xor(xr, o));
           xi = ff_add(xi, ff_shfl_xor(xi, o));
@@ -525,38 +581,44 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
           sRed[2 * warp] = xr;
           sRed[2 * warp + 1] = xi;
         }
-        tc::named_bar(1, 256);
-        if (etid == 0) {
-          ff tr = sRed[0], ti = sRed[1];
-          for (int w = 1; w < 8; ++w) {
-            tr = ff_add(tr, sRed[2 * w]);
-            ti = ff_add(ti, sRed[2 * w + 1]);
+        tc::named_bar(1, kExEpi);
+        // per-walker results; the next walker's staging writes come after its own barrier
+        if (warp == 0) {
+          ff tr = lane < 16 ? sRed[2 * lane] : ff{0.f, 0.f};
+          ff ti = lane < 16 ? sRed[2 * lane + 1] : ff{0.f, 0.f};
+          for (int o = 8; o > 0; o >>= 1) {
+            tr = ff_add(tr, ff_shfl_xor(tr, o));
+            ti = ff_add(ti, ff_shfl_xor(ti, o));
           }
-          a.xpart[(size_t)b * a.nblk_total + L.blk_off + blk] =
-              make_double2((double)a.mult * ff_d(tr), (double)a.mult * ff_d(ti));
+          if (lane == 0)
+            a.xpart[(size_t)b * a.nblk_total + L.blk_off + blk] =
+                make_double2((double)a.mult * ff_d(tr), (double)a.mult * ff_d(ti));
         }
-        if (etid < L.gb) {
-          const int g = blk * L.gb + etid;
-          if (g < a.G) {
-            ff tr{0.f, 0.f}, ti{0.f, 0.f};
-            for (int ii = 0; ii < L.n; ++ii) {
-              tr = ff_add(tr, sC[2 * (etid * L.n + ii)]);
-              ti = ff_add(ti, sC[2 * (etid * L.n + ii) + 1]);
-            }
-            a.cs[(size_t)b * a.G + g] = make_double2(ff_d(tr), ff_d(ti));
+        // traces: 16 lanes per Cholesky vector of the block, 32 vectors per pass
+        for (int gbase = 0; gbase < L.gb; gbase += kExEpi / 16) {
+          if (gbase + 2 * warp >= L.gb) continue;  // warp-uniform: no vector of this pass in this warp
+          const int gv = gbase + (etid >> 4), ii = etid & 15;
+          const int g = blk * L.gb + gv;
+          const bool ok = gv < L.gb && ii < L.n && g < a.G;
+          ff tr = ok ? sC[2 * (gv * L.n + ii)] : ff{0.f, 0.f};
+          ff ti = ok ? sC[2 * (gv * L.n + ii) + 1] : ff{0.f, 0.f};
+          for (int o = 8; o > 0; o >>= 1) {
+            tr = ff_add(tr, ff_shfl_xor(tr, o));
+            ti = ff_add(ti, ff_shfl_xor(ti, o));
           }
+          if (ii == 0 && gv < L.gb && g < a.G) a.cs[(size_t)b * a.G + g] = make_double2(ff_d(tr), ff_d(ti));
         }
-        tc::named_bar(1, 256);
       }
       // this accumulator buffer is free again
       tc::fence_before_sync();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&acc_empty[abuf]);
     }
+    }
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 8) tc::tmem_dealloc(taddr, 512);
+  if (warp == 16) tc::tmem_dealloc(taddr, 512);
 }
 
 // fb = sum_s mult_s c_s   (complex, W x G)
@@ -862,29 +924,36 @@ __global__ void __launch_bounds__(256) trotter32_kernel(Spins sp, Trot32Args a32
 
 // ------------------------------------------------------------------ tensor-core Trotter propagation
 // Same algorithm as trotter32_kernel with every product on the tensor cores:
-//   term 0:        T0 = E w                      (E = exp(-dt/2 h1_eff), real)
-//   term k=1..K:   T_k = (i sqrt(dt)/k) V T_{k-1}, O = T0 + ... + T_K
-//   term K+1:      w' = E O
-// One CTA per walker.  The A operand (128 rows p x K) is streamed from global
-// memory in 64-wide K chunks of 3 BF16 slices (48 KB, 2-stage ring): E (K = 128,
-// 2 chunks, shared by all walkers) or this walker's [Vr | Vi] (K = 256, 4
-// chunks).  The B operand (NB rows x K, 3 slices) holds the previous term T in
-// shared memory, row 2j giving the real and row 2j + 1 the imaginary part of
-// output column j: for a V term row 2j = [Tr_j ; -Ti_j] and row 2j + 1 =
-// [Ti_j ; Tr_j] over K = [Re rows 0..127 ; Im rows 128..255], for an E term
-// rows 2j / 2j + 1 = Tr_j / Ti_j over K = 128.  3-term BF16 splits of
-// both operands, products t + u <= 2 (6 MMAs per K step), FP32 accumulation in
-// TMEM (~2^-24 relative, the FP32 path's accuracy).  Warps 0-3 (thread = row p
-// = TMEM lane) turn each accumulator into the next B operand and accumulate O
-// in registers; warp 4 lane 0 streams A and issues the MMAs.  The tail (FP64
-// overlap, phaseless weight) is shared with the other Trotter kernels.
-static constexpr int kTcThreads = 160;
-static constexpr uint32_t kTcChunk = 3 * kVSlice;  // 48 KB: 3 slices x 128 rows x 64 K
+//   step 0:          T0 = E w                      (E = exp(-dt/2 h1_eff), real)
+//   steps k=1..K:    T_k = (i sqrt(dt)/k) V T_{k-1}, O = T0 + ... + T_K
+//   step K+1:        w' = E O
+// The A operand (128 rows p x K) is streamed from global memory in 32-wide K
+// chunks of 3 BF16 slices (24 KB, 2-stage ring): E (K = 128, 4 chunks, shared by
+// all walkers) or the walker's [Vr | Vi] (K = 256, 8 chunks).  The B operand
+// (NB rows x K, 3 slices) holds the previous term T in shared memory, row 2j
+// giving the real and row 2j + 1 the imaginary part of output column j: for a V
+// step row 2j = [Re T_j ; -Im T_j] and row 2j + 1 = [Im T_j ; Re T_j] over
+// K = [Re rows 0..127 ; Im rows 128..255], for an E step rows 2j / 2j + 1 =
+// Re / Im T_j over K = 128.  3-term BF16 splits of both operands, products
+// t + u <= 2 (6 MMAs per 16-wide K step), FP32 accumulation in TMEM (~2^-24
+// relative, the FP32 path's accuracy).
+// Each CTA carries WPC walkers through the steps in lockstep: while the
+// epilogue turns walker 0's accumulator into its next B operand the tensor core
+// runs walker 1's step, and vice versa.  Warp 8 lane 0 streams A and issues
+// the MMAs; warps 0-7 are the epilogue (warp w: TMEM lanes / orbital rows
+// 32 (w % 4) .., output columns of half w / 4), accumulating O in registers.
+// The new overlaps and phaseless weights are computed afterwards by the FP64
+// determinant kernel (full occupancy) and phaseless_update.
+static constexpr int kTcThreads = 288;
+static constexpr int kTcKC = 32;                                // K per A / B chunk
+static constexpr uint32_t kTcSlice = 128 * kTcKC * 2;           // 8 KB: one slice of one A chunk
+static constexpr uint32_t kTcChunk = 3 * kTcSlice;              // 24 KB
+static constexpr int kTcStages = 2;
 
 struct TrotTcArgs {
   TrotterArgs t;
-  const uint16_t* vimg;  // (W, 4 chunks, 3, 128, 64) bf16 image of [Vr | Vi]
-  const uint16_t* eimg;  // (2 chunks, 3, 128, 64) bf16 image of E
+  const uint16_t* vimg;  // (W, 8 chunks, 3, 128, 32) bf16 image of [Vr | Vi]
+  const uint16_t* eimg;  // (4 chunks, 3, 128, 32) bf16 image of E
   int* status;
 };
 
@@ -898,201 +967,212 @@ __device__ __forceinline__ void split3_bf16(float x, uint16_t& h, uint16_t& m, u
   l = *reinterpret_cast<const uint16_t*>(&bl);
 }
 
-// B element (row j, k) = x as 3 slices; B image = [kchunk][slice][NB rows][64]
-__device__ __forceinline__ void put_b(unsigned char* B, int NB, int j, int k, float x) {
+// B element (row j, k) = x as 3 slices; B image = [kchunk][slice][NB rows][32]
+template <int NB>
+__device__ __forceinline__ void put_b(unsigned char* B, int j, int k, float x) {
   uint16_t h, m, l;
   split3_bf16(x, h, m, l);
-  const uint32_t sl = (uint32_t)NB * 128;  // bytes of one slice of one chunk
-  unsigned char* c = B + (size_t)(k >> 6) * 3 * sl + tc::tile_off(j, k & 63);
+  constexpr uint32_t sl = (uint32_t)NB * kTcKC * 2;  // bytes of one slice of one chunk
+  unsigned char* c = B + (size_t)(k / kTcKC) * 3 * sl + tc::tile_off32(j, k % kTcKC);
   *reinterpret_cast<uint16_t*>(c) = h;
   *reinterpret_cast<uint16_t*>(c + sl) = m;
   *reinterpret_cast<uint16_t*>(c + 2 * sl) = l;
 }
 
-template <int NBT>
+template <int NBT, int WPC>
 __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, TrotTcArgs g) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  __shared__ double2 red[32];
-  __shared__ int piv;
-  __shared__ __align__(8) uint64_t bars[6];
+  __shared__ __align__(8) uint64_t bars[4 + 2 * WPC];
   __shared__ uint32_t tslot;
-  __shared__ int okflag;
+  constexpr int NB = NBT, NH = NBT / 4;          // complex output columns per epilogue half
+  constexpr uint32_t kBBytes = 8u * 3u * NB * kTcKC * 2u;
   unsigned char* base = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
-  unsigned char* Abuf = base;                    // 2 x 48 KB
-  unsigned char* Bbuf = base + 2 * kTcChunk;     // 4 chunks x 3 slices x NB x 128 B
-  uint64_t* full = bars;       // [2]
-  uint64_t* empty = bars + 2;  // [2]
-  uint64_t* acc_full = bars + 4;
-  uint64_t* b_ready = bars + 5;
+  unsigned char* Abuf = base;                                  // kTcStages x 24 KB
+  unsigned char* Bbuf = base + kTcStages * kTcChunk;           // WPC x kBBytes
+  uint64_t* full = bars;             // [2]
+  uint64_t* empty = bars + 2;        // [2]
+  uint64_t* acc_full = bars + 4;     // [WPC]
+  uint64_t* b_ready = bars + 4 + WPC;  // [WPC]
   const TrotterArgs& a = g.t;
-  const int b = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int N = a.N, nc = sp.ntot, nterms = a.nterms;
-  constexpr int NB = NBT, NJ = NBT / 2;
   const int nsteps = nterms + 2;  // E, V x nterms, E
-  if (warp == 4) tc::tmem_alloc(&tslot, 64);
-  if (tid == 128) {
+  const int b0 = blockIdx.x * WPC;
+  const int nw = min(WPC, a.W - b0);
+  if (warp == 8) tc::tmem_alloc(&tslot, WPC * 64);
+  if (tid == 256) {
     for (int k = 0; k < 2; ++k) {
       tc::mbar_init(&full[k], 1);
       tc::mbar_init(&empty[k], 1);
     }
-    tc::mbar_init(acc_full, 1);
-    tc::mbar_init(b_ready, 128);
-    okflag = 1;
+    for (int wi = 0; wi < WPC; ++wi) {
+      tc::mbar_init(&acc_full[wi], 1);
+      tc::mbar_init(&b_ready[wi], 256);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  // zero the B image once: padding rows (j >= 2 nc) and columns (k >= N) stay zero
-  {
-    const int words = 4 * 3 * NB * 128 / 16;
+  {  // zero the B images: padding rows (j >= 2 nc) and K rows (p >= N) stay zero
     uint4* bz = reinterpret_cast<uint4*>(Bbuf);
-    for (int e = tid; e < words; e += kTcThreads) bz[e] = make_uint4(0u, 0u, 0u, 0u);
-    tc::fence_proxy_async();  // visible to the tensor core (async proxy)
+    for (int e = tid; e < (int)(WPC * kBBytes / 16); e += kTcThreads) bz[e] = make_uint4(0u, 0u, 0u, 0u);
+    tc::fence_proxy_async();
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = tslot;
-  if (warp == 4) {
+  if (warp == 8) {
     if (lane == 0) {
       bool ok = true;
       const uint32_t idesc = tc::idesc_bf16_f32(128, NB);
       const uint32_t sa = tc::smem_u32(Abuf), sb = tc::smem_u32(Bbuf);
-      const uint32_t bsl = (uint32_t)NB * 128;
-      const uint16_t* vimg = g.vimg + (size_t)b * 4 * (kTcChunk / 2);
+      constexpr uint32_t bsl = (uint32_t)NB * kTcKC * 2;
       int chunk = 0;
       for (int step = 0; step < nsteps && ok; ++step) {
         const bool vterm = step > 0 && step <= nterms;
-        const int nk = vterm ? 4 : 2;
-        for (int kc = 0; kc < nk && ok; ++kc, ++chunk) {
-          const int st = chunk & 1;
-          if (chunk >= 2) ok = tc::mbar_wait(&empty[st], (uint32_t)(((chunk - 2) >> 1) & 1));
-          if (!ok) break;
-          const uint16_t* src = (vterm ? vimg : g.eimg) + (size_t)kc * (kTcChunk / 2);
-          tc::mbar_expect_tx(&full[st], kTcChunk);
-          tc::bulk_g2s(Abuf + (size_t)st * kTcChunk, src, kTcChunk, &full[st]);
-          if (kc == 0) {  // the B operand of this step is written by the epilogue warps
-            ok = tc::mbar_wait(b_ready, (uint32_t)(step & 1));
+        const int nk = vterm ? 8 : 4;
+        for (int wi = 0; wi < nw && ok; ++wi) {
+          const uint16_t* vimg = g.vimg + (size_t)(b0 + wi) * 8 * (kTcChunk / 2);
+          const uint32_t bw = sb + (uint32_t)wi * kBBytes;
+          for (int kc = 0; kc < nk && ok; ++kc, ++chunk) {
+            const int st = chunk & 1;
+            if (chunk >= 2) ok = tc::mbar_wait(&empty[st], (uint32_t)(((chunk - 2) >> 1) & 1));
             if (!ok) break;
-          }
-          ok = tc::mbar_wait(&full[st], (uint32_t)((chunk >> 1) & 1));
-          if (!ok) break;
-          tc::fence_after_sync();
-          const uint32_t a0 = sa + (uint32_t)st * kTcChunk;
-          const uint32_t b0 = sb + (uint32_t)kc * 3 * bsl;
-          for (int t = 0; t < 3; ++t)
-            for (int u = 0; t + u <= 2; ++u) {
-#pragma unroll
-              for (int ks = 0; ks < 4; ++ks) {
-                const uint64_t ad = tc::smem_desc(a0 + (uint32_t)t * kVSlice + ks * 256, 128, 1024);
-                const uint64_t bd = tc::smem_desc(b0 + (uint32_t)u * bsl + ks * 256, 128, 1024);
-                tc::mma_bf16(taddr, ad, bd, idesc, (kc | t | u | ks) ? 1u : 0u);
-              }
+            const uint16_t* src = (vterm ? vimg : g.eimg) + (size_t)kc * (kTcChunk / 2);
+            tc::mbar_expect_tx(&full[st], kTcChunk);
+            tc::bulk_g2s(Abuf + (size_t)st * kTcChunk, src, kTcChunk, &full[st]);
+            if (kc == 0) {  // this walker's B operand for the step is written by the epilogue
+              ok = tc::mbar_wait(&b_ready[wi], (uint32_t)(step & 1));
+              if (!ok) break;
             }
-          tc::mma_commit(&empty[st]);
+            ok = tc::mbar_wait(&full[st], (uint32_t)((chunk >> 1) & 1));
+            if (!ok) break;
+            tc::fence_after_sync();
+            const uint32_t a0 = sa + (uint32_t)st * kTcChunk;
+            const uint32_t bk = bw + (uint32_t)kc * 3 * bsl;
+            for (int t = 0; t < 3; ++t)
+              for (int u = 0; t + u <= 2; ++u) {
+#pragma unroll
+                for (int ks = 0; ks < kTcKC / 16; ++ks) {
+                  const uint64_t ad = tc::smem_desc(a0 + (uint32_t)t * kTcSlice + ks * 256, 128, 512);
+                  const uint64_t bd = tc::smem_desc(bk + (uint32_t)u * bsl + ks * 256, 128, 512);
+                  tc::mma_bf16(taddr + (uint32_t)(wi * 64), ad, bd, idesc, (kc | t | u | ks) ? 1u : 0u);
+                }
+              }
+            tc::mma_commit(&empty[st]);
+          }
+          if (ok) tc::mma_commit(&acc_full[wi]);
         }
-        if (ok) tc::mma_commit(acc_full);
       }
       if (!ok) {
         atomicExch(g.status, (int)TROT_ERR_DEVICE_TIMEOUT);
-        okflag = 0;
         // let copies / MMAs already issued land before the tensor memory is released
         for (int k = 0; k < 2; ++k) tc::mbar_wait(&empty[k], 0u, 1000000u);
-        tc::mbar_wait(&full[0], 0u, 1000000u);
+        for (int k = 0; k < 2; ++k) tc::mbar_wait(&full[k], 0u, 1000000u);
       }
     }
     __syncwarp();
   } else {
-    // thread r: row p = r of every accumulator (TMEM lane r); output column j of
-    // the complex product is B row 2j (real part) and 2j + 1 (imaginary part)
-    const int p = tid;
+    // thread: orbital row p (TMEM lane), complex output columns j = jbase + jj, jj < NH
+    const int q = warp & 3, h = warp >> 2;
+    const int p = q * 32 + lane;
     const bool prow = p < N;
-    float orr[NJ], oi[NJ];
+    const int jbase = h * NH;
+    float orr[WPC][NH], oi[WPC][NH];
 #pragma unroll
-    for (int j = 0; j < NJ; ++j) { orr[j] = 0.f; oi[j] = 0.f; }
-    // term 0 operand: B[2j][p] = Re w[p][j], B[2j+1][p] = Im w[p][j]
+    for (int wi = 0; wi < WPC; ++wi)
 #pragma unroll
-    for (int j = 0; j < NJ; ++j) {
-      if (j < nc) {
-        const int s = j < sp.n[0] ? 0 : 1, n = sp.n[s], col = j - sp.off[s];
-        const double2* w = (s == 0 ? a.in_a : a.in_b) + (size_t)b * N * n;
-        const double2 x = prow ? w[(size_t)p * n + col] : make_double2(0.0, 0.0);
-        put_b(Bbuf, NB, 2 * j, p, (float)x.x);
-        put_b(Bbuf, NB, 2 * j + 1, p, (float)x.y);
-      }
-    }
-    tc::fence_proxy_async();
-    tc::fence_before_sync();
-    tc::mbar_arrive(b_ready);
-    const uint32_t trow = taddr + ((uint32_t)(warp * 32) << 16);
-    for (int step = 0; step < nsteps; ++step) {
-      if (!tc::mbar_wait(acc_full, (uint32_t)(step & 1))) {
-        atomicExch(g.status, (int)TROT_ERR_DEVICE_TIMEOUT);
-        okflag = 0;
-        break;
-      }
-      tc::fence_after_sync();
-      float d[NB];
+      for (int jj = 0; jj < NH; ++jj) { orr[wi][jj] = 0.f; oi[wi][jj] = 0.f; }
+    // step 0 operand: B[2j][p] = Re w[p][j], B[2j+1][p] = Im w[p][j]
+    for (int wi = 0; wi < nw; ++wi) {
+      unsigned char* B = Bbuf + (size_t)wi * kBBytes;
+      const int b = b0 + wi;
 #pragma unroll
-      for (int c = 0; c < NB; c += 16) tc::tmem_ld16(trow + c, d + c);
-      if (step == nsteps - 1) {
-        // w' = E O: write the walker (FP64) to global memory and to shared memory for the tail
-        double2* W2 = reinterpret_cast<double2*>(Abuf);
-#pragma unroll
-        for (int j = 0; j < NJ; ++j) {
-          if (j < nc && prow) {
-            const double2 x = make_double2((double)d[2 * j], (double)d[2 * j + 1]);
-            W2[p * nc + j] = x;
-            const int s = j < sp.n[0] ? 0 : 1, n = sp.n[s], col = j - sp.off[s];
-            (s == 0 ? a.out_a : a.out_b)[((size_t)b * N + p) * n + col] = x;
-          }
-        }
-        break;
-      }
-      const bool next_is_v = step < nterms;  // the operand built now feeds a V term
-      const float coef = step == 0 ? 1.f : (float)(a.sqrt_dt / (double)step);
-#pragma unroll
-      for (int j = 0; j < NJ; ++j) {
+      for (int jj = 0; jj < NH; ++jj) {
+        const int j = jbase + jj;
         if (j < nc) {
-          float tr, ti;
-          if (step == 0) { tr = d[2 * j]; ti = d[2 * j + 1]; }
-          else { tr = -coef * d[2 * j + 1]; ti = coef * d[2 * j]; }
-          orr[j] += tr;
-          oi[j] += ti;
-          if (next_is_v) {
-            put_b(Bbuf, NB, 2 * j, p, tr);
-            put_b(Bbuf, NB, 2 * j, 128 + p, -ti);
-            put_b(Bbuf, NB, 2 * j + 1, p, ti);
-            put_b(Bbuf, NB, 2 * j + 1, 128 + p, tr);
-          } else {
-            put_b(Bbuf, NB, 2 * j, p, orr[j]);
-            put_b(Bbuf, NB, 2 * j + 1, p, oi[j]);
-          }
+          const int s = j < sp.n[0] ? 0 : 1, n = sp.n[s], col = j - sp.off[s];
+          const double2* w = (s == 0 ? a.in_a : a.in_b) + (size_t)b * N * n;
+          const double2 x = prow ? w[(size_t)p * n + col] : make_double2(0.0, 0.0);
+          put_b<NB>(B, 2 * j, p, (float)x.x);
+          put_b<NB>(B, 2 * j + 1, p, (float)x.y);
         }
       }
       tc::fence_proxy_async();
       tc::fence_before_sync();
-      tc::mbar_arrive(b_ready);
+      tc::mbar_arrive(&b_ready[wi]);
+    }
+    bool ok = true;
+    for (int step = 0; step < nsteps && ok; ++step) {
+      const bool next_is_v = step < nterms;  // the operand built now feeds a V step
+      const float coef = step == 0 ? 1.f : (float)(a.sqrt_dt / (double)step);
+#pragma unroll
+      for (int wi = 0; wi < WPC; ++wi) {
+        if (wi >= nw) break;
+        if (!tc::mbar_wait(&acc_full[wi], (uint32_t)(step & 1))) {
+          atomicExch(g.status, (int)TROT_ERR_DEVICE_TIMEOUT);
+          ok = false;
+          break;
+        }
+        tc::fence_after_sync();
+        float d[2 * NH];
+        const uint32_t tl = taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(wi * 64 + h * 2 * NH);
+#pragma unroll
+        for (int c = 0; c < 2 * NH; c += 8) tc::tmem_ld8(tl + c, d + c);
+        const int b = b0 + wi;
+        if (step == nsteps - 1) {  // w' = E O
+#pragma unroll
+          for (int jj = 0; jj < NH; ++jj) {
+            const int j = jbase + jj;
+            if (j < nc && prow) {
+              const int s = j < sp.n[0] ? 0 : 1, n = sp.n[s], col = j - sp.off[s];
+              (s == 0 ? a.out_a : a.out_b)[((size_t)b * N + p) * n + col] =
+                  make_double2((double)d[2 * jj], (double)d[2 * jj + 1]);
+            }
+          }
+          continue;
+        }
+        unsigned char* B = Bbuf + (size_t)wi * kBBytes;
+#pragma unroll
+        for (int jj = 0; jj < NH; ++jj) {
+          const int j = jbase + jj;
+          if (j < nc) {
+            float tr, ti;
+            if (step == 0) { tr = d[2 * jj]; ti = d[2 * jj + 1]; }
+            else { tr = -coef * d[2 * jj + 1]; ti = coef * d[2 * jj]; }
+            orr[wi][jj] += tr;
+            oi[wi][jj] += ti;
+            if (next_is_v) {
+              put_b<NB>(B, 2 * j, p, tr);
+              put_b<NB>(B, 2 * j, 128 + p, -ti);
+              put_b<NB>(B, 2 * j + 1, p, ti);
+              put_b<NB>(B, 2 * j + 1, 128 + p, tr);
+            } else {
+              put_b<NB>(B, 2 * j, p, orr[wi][jj]);
+              put_b<NB>(B, 2 * j + 1, p, oi[wi][jj]);
+            }
+          }
+        }
+        tc::fence_proxy_async();
+        tc::fence_before_sync();
+        tc::mbar_arrive(&b_ready[wi]);
+      }
     }
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 4) tc::tmem_dealloc(taddr, 64);
-  if (!okflag) return;
-  if (a.overlaps == nullptr) return;
-  double2* W2 = reinterpret_cast<double2*>(Abuf);
-  double2* Ms = reinterpret_cast<double2*>(Bbuf);
-  overlap_and_weight(sp, a, N, nc, W2, Ms, &piv, red);
+  if (warp == 8) tc::tmem_dealloc(taddr, WPC * 64);
 }
 
-// [Vr | Vi] of every walker as the A image of trotter_tc_kernel: (W, 4 chunks, 3 slices, 128 rows, 64)
+// [Vr | Vi] of every walker as the A image of trotter_tc_kernel: (W, 8 chunks, 3 slices, 128 rows, 32)
 // from the VHS GEMM output (rows 2b / 2b+1 = Re / Im of walker b, n2pad columns pq).
 // One thread per (walker, chunk, row, 8 consecutive k): three 16-byte stores.
 __global__ void vhs_image_kernel(int W, int N, int n2pad, const float* __restrict__ D, uint16_t* __restrict__ img) {
-  const size_t total = (size_t)W * 4 * 128 * 8;
+  const size_t total = (size_t)W * 8 * 128 * 4;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-    const int kg = (int)(e & 7), p = (int)((e >> 3) & 127), kc = (int)((e >> 10) & 3);
+    const int kg = (int)(e & 3), p = (int)((e >> 2) & 127), kc = (int)((e >> 9) & 7);
     const size_t b = e >> 12;
-    const int k0 = kc * 64 + kg * 8;                 // 0..255
+    const int k0 = kc * kTcKC + kg * 8;              // 0..255
     const int im = k0 >= 128 ? 1 : 0, q0 = k0 & 127;
     const float* src = D + (2 * b + im) * (size_t)n2pad + (size_t)p * N;
     uint32_t hw[4], mw[4], lw[4];
@@ -1107,11 +1187,18 @@ __global__ void vhs_image_kernel(int W, int N, int n2pad, const float* __restric
       mw[i / 2] = (uint32_t)m0 | ((uint32_t)m1 << 16);
       lw[i / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
     }
-    unsigned char* dst = reinterpret_cast<unsigned char*>(img) + (b * 4 + kc) * (size_t)kTcChunk + tc::tile_off(p, kg * 8);
+    unsigned char* dst =
+        reinterpret_cast<unsigned char*>(img) + (b * 8 + kc) * (size_t)kTcChunk + tc::tile_off32(p, kg * 8);
     *reinterpret_cast<uint4*>(dst) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-    *reinterpret_cast<uint4*>(dst + kVSlice) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
-    *reinterpret_cast<uint4*>(dst + 2 * kVSlice) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+    *reinterpret_cast<uint4*>(dst + kTcSlice) = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+    *reinterpret_cast<uint4*>(dst + 2 * kTcSlice) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
   }
+}
+
+// phaseless weights from overlaps computed after the propagation
+__global__ void tc_weight_kernel(TrotterArgs a, const double2* __restrict__ ov_new) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < a.W) phaseless_update(a, b, ov_new[b]);
 }
 
 // ------------------------------------------------------------------ host orchestration
@@ -1143,11 +1230,7 @@ static int launch_exchange_exact(int jh, dim3 grid, const ExArgs& a, cudaStream_
     case 2: exchange_exact_launch<2>(grid, a, st); break;
     case 3: exchange_exact_launch<3>(grid, a, st); break;
     case 4: exchange_exact_launch<4>(grid, a, st); break;
-    case 5: exchange_exact_launch<5>(grid, a, st); break;
-    case 6: exchange_exact_launch<6>(grid, a, st); break;
-    case 7: exchange_exact_launch<7>(grid, a, st); break;
-    case 8: exchange_exact_launch<8>(grid, a, st); break;
-    default: set_error("exchange: n_pad/2 = %d unsupported", jh); return TROT_ERR_UNSUPPORTED;
+    default: set_error("exchange: n_pad/4 = %d unsupported", jh); return TROT_ERR_UNSUPPORTED;
   }
   TROT_CHECK_LAUNCH("exchange_exact_kernel");
   return TROT_OK;
@@ -1170,11 +1253,10 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
     ExArgs a{};
     a.L = L;
     a.G = G; a.W = W; a.mult = sp.mult[q];
-    // about two CTAs' worth of walker tiles per SM, one CTA per SM at a time
-    int chunks = (2 * 152 + L.nblk - 1) / L.nblk;
-    if (chunks > L.ntiles) chunks = L.ntiles;
-    a.tiles_per_cta = (L.ntiles + chunks - 1) / chunks;
-    chunks = (L.ntiles + a.tiles_per_cta - 1) / a.tiles_per_cta;
+    // persistent grid: one CTA per SM walks (Cholesky block, 16 walker tiles) items
+    a.tiles_per_item = std::min(16, L.ntiles);
+    a.chunks = (L.ntiles + a.tiles_per_item - 1) / a.tiles_per_item;
+    a.n_items = L.nblk * a.chunks;
     a.rot_img = s->mixed->rot_slices[mq];
     a.rot_e = s->mixed->rot_exp[mq];
     a.green_img = m.gq[q];
@@ -1183,8 +1265,8 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
     a.xpart = m.xpart;
     a.nblk_total = m.nblk_total;
     a.status = m.status;
-    dim3 grid(L.nblk, chunks);
-    TROT_TIMED("exchange_exact_tc", st, launch_exchange_exact(L.n_pad / 2, grid, a, st));
+    dim3 grid(std::min(a.n_items, 152));
+    TROT_TIMED("exchange_exact_tc", st, launch_exchange_exact(L.n_pad / 4, grid, a, st));
   }
   const int n = W * G;
   fb_combine_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, sp.nspin, sp.mult[0], sp.mult[1], m.cs[0],
@@ -1266,10 +1348,12 @@ static int run_trotter32(const trot_system* s, const Spins& sp, const TrotterArg
   return TROT_OK;
 }
 
-template <int NBT>
-static void trotter_tc_launch(const Spins& sp, const TrotTcArgs& g, int W, size_t smem, cudaStream_t st) {
-  cudaFuncSetAttribute(trotter_tc_kernel<NBT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  trotter_tc_kernel<NBT><<<W, kTcThreads, smem, st>>>(sp, g);
+template <int NBT, int WPC>
+static void trotter_tc_launch(const Spins& sp, const TrotTcArgs& g, int W, cudaStream_t st) {
+  constexpr size_t smem = 1024 + kTcStages * (size_t)kTcChunk + WPC * (8u * 3u * NBT * kTcKC * 2u);
+  static_assert(smem <= 227 * 1024, "tensor-core Trotter shared memory");
+  cudaFuncSetAttribute(trotter_tc_kernel<NBT, WPC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  trotter_tc_kernel<NBT, WPC><<<(W + WPC - 1) / WPC, kTcThreads, smem, st>>>(sp, g);
 }
 
 static int run_trotter_tc(const trot_system* s, const Spins& sp, const TrotterArgs& t, const MixedBuffers& m,
@@ -1280,9 +1364,9 @@ static int run_trotter_tc(const trot_system* s, const Spins& sp, const TrotterAr
     set_error("tensor-core Trotter: N=%d nc=%d nterms=%d unsupported", N, nc, t.nterms);
     return TROT_ERR_UNSUPPORTED;
   }
-  static_assert(kTcChunkBytes == kTcChunk, "A chunk size");
+  static_assert(kTcImgBytes == 8 * (size_t)kTcChunk, "operand image size");
   TROT_TIMED("vhs_image", st, ([&]() -> int {
-    const size_t threads = (size_t)W * 4 * 128 * 8;
+    const size_t threads = (size_t)W * 8 * 128 * 4;
     const int blocks = (int)std::min<size_t>((threads + 255) / 256, 152 * 32);
     vhs_image_kernel<<<blocks, 256, 0, st>>>(W, N, s->mixed->n2pad, m.vhs, m.vimg);
     TROT_CHECK_LAUNCH("vhs_image_kernel");
@@ -1293,17 +1377,21 @@ static int run_trotter_tc(const trot_system* s, const Spins& sp, const TrotterAr
   g.vimg = m.vimg;
   g.eimg = s->mixed->exp_h1_half_img;
   g.status = m.status;
-  const size_t smem = 1024 + 2 * (size_t)kTcChunk + 4 * 3 * (size_t)NB * 128;
   TROT_TIMED("trotter_tc", st, ([&]() -> int {
     switch (NB) {
-      case 16: trotter_tc_launch<16>(sp, g, W, smem, st); break;
-      case 32: trotter_tc_launch<32>(sp, g, W, smem, st); break;
-      case 48: trotter_tc_launch<48>(sp, g, W, smem, st); break;
-      default: trotter_tc_launch<64>(sp, g, W, smem, st); break;
+      case 16: trotter_tc_launch<16, 2>(sp, g, W, st); break;
+      case 32: trotter_tc_launch<32, 2>(sp, g, W, st); break;
+      case 48: trotter_tc_launch<48, 2>(sp, g, W, st); break;
+      default: trotter_tc_launch<64, 1>(sp, g, W, st); break;
     }
     TROT_CHECK_LAUNCH("trotter_tc_kernel");
     return TROT_OK;
   })());
+  if (t.overlaps) {  // step mode: FP64 overlaps of the new walkers, then the phaseless weights
+    TROT_TIMED("overlap_fp64", st, launch_green(sp, W, N, t.out_a, t.out_b, nullptr, m.ov_new, nullptr, st));
+    tc_weight_kernel<<<(W + 127) / 128, 128, 0, st>>>(t, m.ov_new);
+    TROT_CHECK_LAUNCH("tc_weight_kernel");
+  }
   return TROT_OK;
 }
 

@@ -139,6 +139,23 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 32 lanes x 32-bit, 8 consecutive columns (same lane rule as tmem_ld16).
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Byte offset of element (row r, k) inside a [rows x 32] K-major tile (8-row
+// groups 512 B apart, k groups 128 B apart): descriptor LBO 128, SBO 512.
+__host__ __device__ __forceinline__ uint32_t tile_off32(int r, int k) {
+  return (uint32_t)((r >> 3) * 512 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
 // Byte offset of element (row r, k) inside a [rows x 64] K-major tile in the
 // core-matrix layout described above.
 __host__ __device__ __forceinline__ uint32_t tile_off(int r, int k) {

@@ -60,21 +60,21 @@ def plain_split(x: np.ndarray, slices: int = VHS_SLICES) -> list[torch.Tensor]:
     return out
 
 
-def split3_image(bt: np.ndarray):
-    """Operand image of a real matrix B (K, ncols) for the split-BF16 GEMM
-    kernel, given its transpose bt (ncols, K): rows padded to a multiple of
-    128, K to a multiple of 64, split into 3 BF16 terms and laid out as
-    [ncols/128][K/64][3][128][64] tiles in core-matrix order (8 x 8 blocks).
-    Returns (image (bf16, host), ncols_pad, k_pad)."""
+def split3_image(bt: np.ndarray, kchunk: int = 64):
+    """Operand image of a real matrix B (K, ncols) for the split-BF16 tensor-core
+    kernels, given its transpose bt (ncols, K): rows padded to a multiple of
+    128, K to a multiple of kchunk, split into 3 BF16 terms and laid out as
+    [ncols/128][K/kchunk][3][128][kchunk] tiles in core-matrix order (8 x 8
+    blocks).  Returns (image (bf16, host), ncols_pad, k_pad)."""
     bt = np.asarray(bt, dtype=np.float64)
     nc, K = bt.shape
-    npad, kpad = (nc + 127) // 128 * 128, (K + 63) // 64 * 64
+    npad, kpad = (nc + 127) // 128 * 128, (K + kchunk - 1) // kchunk * kchunk
     lt = np.zeros((npad, kpad), dtype=np.float64)
     lt[:nc, :K] = bt
     sl = torch.stack(plain_split(lt))  # (3, npad, kpad)
-    nt, nk = npad // 128, kpad // 64
-    sl = sl.reshape(3, nt, 16, 8, nk, 8, 8).permute(1, 4, 0, 2, 5, 3, 6).contiguous()
-    return sl.reshape(nt, nk, 3, 128, 64).contiguous(), npad, kpad
+    nt, nk = npad // 128, kpad // kchunk
+    sl = sl.reshape(3, nt, 16, 8, nk, kchunk // 8, 8).permute(1, 4, 0, 2, 5, 3, 6).contiguous()
+    return sl.reshape(nt, nk, 3, 128, kchunk).contiguous(), npad, kpad
 
 
 def gammas_per_block(n: int) -> int:
@@ -133,8 +133,8 @@ class MixedCtx:
         if E.shape[0] <= 128:
             E128 = np.zeros((128, 128))  # the kernel reads K = 128 (two 64-wide chunks) for every N
             E128[: E.shape[0], : E.shape[1]] = E
-            ei, _, kp = split3_image(E128)  # A operand rows p, K = q: (1, 2, 3, 128, 64)
-            assert tuple(ei.shape) == (1, 2, 3, 128, 64) and kp == 128
+            ei, _, kp = split3_image(E128, kchunk=32)  # A operand rows p, K = q: (1, 4, 3, 128, 32)
+            assert tuple(ei.shape) == (1, 4, 3, 128, 32) and kp == 128
             ei = ei.to(dev)
             self._keep.append(ei)
             s.exp_h1_half_img = ei.data_ptr()
