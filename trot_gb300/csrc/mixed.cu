@@ -419,6 +419,8 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
       bool ok = true;
       const uint32_t idesc = tc::idesc_bf16_f32(128, kBN);
       const uint32_t sA_u = tc::smem_u32(sA), ring_u = tc::smem_u32(ring);
+      const uint64_t ad0 = tc::smem_desc(sA_u, 128, kKP * 16);
+      const uint32_t adlo = (uint32_t)ad0, dhi = (uint32_t)(ad0 >> 32);  // A and B share the high word
       int g_issue = 0, g_base = 0, tg = 0, kitem = 0;  // CTA-wide slice / tile / item counters
       for (int item = blockIdx.x; item < a.n_items && ok; item += gridDim.x, ++kitem) {
         const int blk = item / a.chunks;
@@ -453,16 +455,18 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
           ok = tc::mbar_wait(&full[slot], (uint32_t)((gs / kSlots) & 1));
           if (!ok) break;
           tc::fence_after_sync();
-          const int tmax = min(kSlices - 1, (kGroups - 1) - u);
+          // slice u of the Green's function meets the rot_chol slices t <= 4 - u; products with
+          // t + u = d accumulate into group d.  Descriptors advance by constants.
+          const uint32_t blo = (uint32_t)tc::smem_desc(ring_u + (uint32_t)(slot * kBImg), 128, kKP * 16);
+          const uint32_t dcol = taddr + (uint32_t)(abuf * kGroups * kBN + u * kBN);
+          const int tmax = (kGroups - 1) - u;
           for (int t = 0; t <= tmax; ++t) {
-            const int d = t + u;
+            const uint32_t alo = adlo + (uint32_t)(t * (128 * kKP * 2 / 16));
+            const uint32_t dt = dcol + (uint32_t)(t * kBN);
 #pragma unroll
-            for (int ks = 0; ks < kKP / 16; ++ks) {
-              const uint64_t ad = tc::smem_desc(sA_u + (uint32_t)(t * 128 * kKP * 2 + ks * 256), 128, kKP * 16);
-              const uint64_t bd = tc::smem_desc(ring_u + (uint32_t)(slot * kBImg + ks * 256), 128, kKP * 16);
-              tc::mma_bf16(taddr + (uint32_t)(abuf * kGroups * kBN + d * kBN), ad, bd, idesc,
-                           (u == 0 && ks == 0) ? 0u : 1u);
-            }
+            for (int ks = 0; ks < kKP / 16; ++ks)
+              tc::mma_bf16_lo(dt, alo + (uint32_t)(ks * 16), blo + (uint32_t)(ks * 16), dhi, idesc,
+                              (u == 0 && ks == 0) ? 0u : 1u);
           }
           tc::mma_commit(&empty[slot]);
           if (u == kSlices - 1) tc::mma_commit(&acc_full[abuf]);
@@ -723,18 +727,18 @@ vhs_gemm_kernel(int mtiles, int ntiles, int gpad, int n2pad, const uint16_t* __r
           ok = tc::mbar_wait(&full[st], (uint32_t)((chunk / 2) & 1));
           if (!ok) break;
           tc::fence_after_sync();
-          const uint32_t s0 = su + (uint32_t)st * kVStage;
-          int first = kc == 0;
-          for (int t = 0; t < 3; ++t)
-            for (int u = 0; t + u <= 2; ++u) {
+          const uint64_t s0d = tc::smem_desc(su + (uint32_t)st * kVStage, 128, 1024);
+          const uint32_t slo = (uint32_t)s0d, dhi = (uint32_t)(s0d >> 32);  // A and B share the high word
+          const uint32_t dcol = taddr + (uint32_t)(abuf * 128);
 #pragma unroll
-              for (int ks = 0; ks < kVK / 16; ++ks) {
-                const uint64_t ad = tc::smem_desc(s0 + (uint32_t)(t * kVSlice + ks * 256), 128, 1024);
-                const uint64_t bd = tc::smem_desc(s0 + (uint32_t)((3 + u) * kVSlice + ks * 256), 128, 1024);
-                tc::mma_bf16(taddr + (uint32_t)(abuf * 128), ad, bd, idesc, first ? 0u : 1u);
-                first = 0;
-              }
-            }
+          for (int t = 0; t < 3; ++t)
+#pragma unroll
+            for (int u = 0; t + u <= 2; ++u)
+#pragma unroll
+              for (int ks = 0; ks < kVK / 16; ++ks)
+                tc::mma_bf16_lo(dcol, slo + (uint32_t)((t * kVSlice + ks * 256) >> 4),
+                                slo + (uint32_t)(((3 + u) * kVSlice + ks * 256) >> 4), dhi, idesc,
+                                (kc | t | u | ks) ? 1u : 0u);
           tc::mma_commit(&empty[st]);
         }
         if (ok) tc::mma_commit(&acc_full[abuf]);
@@ -1047,17 +1051,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, Tro
             ok = tc::mbar_wait(&full[st], (uint32_t)((chunk >> 1) & 1));
             if (!ok) break;
             tc::fence_after_sync();
-            const uint32_t a0 = sa + (uint32_t)st * kTcChunk;
-            const uint32_t bk = bw + (uint32_t)kc * 3 * bsl;
-            for (int t = 0; t < 3; ++t)
-              for (int u = 0; t + u <= 2; ++u) {
+            const uint64_t a0 = tc::smem_desc(sa + (uint32_t)st * kTcChunk, 128, 512);
+            const uint32_t alo = (uint32_t)a0, dhi = (uint32_t)(a0 >> 32);  // A and B share the high word
+            const uint32_t blo = (uint32_t)tc::smem_desc(bw + (uint32_t)kc * 3 * bsl, 128, 512);
+            const uint32_t dcol = taddr + (uint32_t)(wi * 64);
 #pragma unroll
-                for (int ks = 0; ks < kTcKC / 16; ++ks) {
-                  const uint64_t ad = tc::smem_desc(a0 + (uint32_t)t * kTcSlice + ks * 256, 128, 512);
-                  const uint64_t bd = tc::smem_desc(bk + (uint32_t)u * bsl + ks * 256, 128, 512);
-                  tc::mma_bf16(taddr + (uint32_t)(wi * 64), ad, bd, idesc, (kc | t | u | ks) ? 1u : 0u);
-                }
-              }
+            for (int t = 0; t < 3; ++t)
+#pragma unroll
+              for (int u = 0; t + u <= 2; ++u)
+#pragma unroll
+                for (int ks = 0; ks < kTcKC / 16; ++ks)
+                  tc::mma_bf16_lo(dcol, alo + (uint32_t)((t * kTcSlice + ks * 256) >> 4),
+                                  blo + (uint32_t)((u * bsl + ks * 256) >> 4), dhi, idesc,
+                                  (kc | t | u | ks) ? 1u : 0u);
             tc::mma_commit(&empty[st]);
           }
           if (ok) tc::mma_commit(&acc_full[wi]);

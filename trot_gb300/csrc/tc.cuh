@@ -59,6 +59,35 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
+// Same with a constant enable-input-d (accumulate = true) / overwrite (false): no
+// per-MMA predicate set-up in the issuing thread's instruction stream.
+__device__ __forceinline__ void mma_bf16_acc(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.eq.u32 p, 1, 1;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc));
+}
+__device__ __forceinline__ void mma_bf16_first(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.eq.u32 p, 1, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc));
+}
+// A descriptor advanced by `bytes` (a multiple of 16, start address staying below 256 KB):
+// the start-address field is the low 14 bits in 16-byte units.
+__device__ __forceinline__ uint64_t desc_add(uint64_t desc, uint32_t bytes) { return desc + (uint64_t)(bytes >> 4); }
+
+// MMA from the low words of two descriptors that share their high word (same SBO,
+// version bits): the issuing thread advances 32-bit values only.
+__device__ __forceinline__ void mma_bf16_lo(uint32_t d_tmem, uint32_t alo, uint32_t blo, uint32_t hi, uint32_t idesc,
+                                            uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .b64 ad, bd;\n.reg .pred p;\nmov.b64 ad, {%1, %3};\nmov.b64 bd, {%2, %3};\n"
+      "setp.ne.b32 p, %5, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %4, p;\n}\n" ::"r"(d_tmem),
+      "r"(alo), "r"(blo), "r"(hi), "r"(idesc), "r"(accumulate));
+}
+
 // Arrive on the mbarrier once every previously issued MMA of this thread completed.
 __device__ __forceinline__ void mma_commit(uint64_t* mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
