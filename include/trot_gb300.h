@@ -342,6 +342,16 @@ int trot_fp_step(const trot_system* sys, const trot_state* state, const double* 
 int trot_tc_gemm_bf16(const uint16_t* A, const uint16_t* B, float* D, int M, int N, int K, int* status,
                       void* stream);
 
+/* Tuning knobs (process-wide; 0 restores the built-in default).  Chosen by
+ * timing candidates on the caller's workload (trot_gb300.autotune); every
+ * setting computes bit-identical results.  No counterpart in the reference.
+ *   TROT_TUNE_EXCHANGE_TILES: walker tiles per work item of the exact-slice
+ *     exchange kernel (default 16);
+ *   TROT_TUNE_EXCHANGE_GRID: persistent CTAs of that kernel (default 152). */
+typedef enum { TROT_TUNE_EXCHANGE_TILES = 0, TROT_TUNE_EXCHANGE_GRID = 1, TROT_TUNE_COUNT = 2 } trot_tune_knob;
+int trot_set_tuning(int knob, int value);
+int trot_get_tuning(int knob);
+
 /* Per-kernel timers for measurement: trot_profile_enable(n) creates a pool
  * for n launches (0 disables); while enabled every kernel launch of the C ABI
  * is bracketed by CUDA events on its stream.  trot_profile_collect

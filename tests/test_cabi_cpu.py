@@ -137,3 +137,15 @@ def test_cisd_workspace_and_errors():
                                    ctypes.byref(st), 0x1000, None, 0x1000, 1 << 40, None) == 1
     assert lib.trot_cisd_prop_step(ctypes.byref(c), ctypes.byref(s), ctypes.byref(st), 0x1000, None, 0x1000, 16,
                                    None) == 4
+
+
+def test_tuning_knobs():
+    lib = _lib.load()
+    assert lib.trot_get_tuning(_lib.TUNE_EXCHANGE_TILES) == 0
+    assert lib.trot_set_tuning(_lib.TUNE_EXCHANGE_TILES, 8) == 0
+    assert lib.trot_get_tuning(_lib.TUNE_EXCHANGE_TILES) == 8
+    assert lib.trot_set_tuning(_lib.TUNE_EXCHANGE_TILES, 0) == 0
+    assert lib.trot_set_tuning(7, 1) == 1
+    assert b"unknown tuning knob" in lib.trot_last_error()
+    assert lib.trot_set_tuning(_lib.TUNE_EXCHANGE_GRID, -3) == 1
+    assert lib.trot_get_tuning(99) == 0

@@ -20,6 +20,8 @@ CASES = [
     ("uhf_u", 17, (5, 3), 33, 9, 30.0),
     ("rhf_r", 7, (3, 3), 5, 3, 30.0),
     ("uhf_u", 80, (16, 9), 300, 13, 30.0),
+    # 48.7 KB of dynamic shared memory in the Green's-function kernel: needs the opt-in limit
+    ("rhf_r", 117, (14, 14), 468, 5, 30.0),
 ]
 
 

@@ -19,6 +19,8 @@ STATUS_NAMES = {
 }
 # trot_kind
 RHF_R, RHF_U, UHF_U = 0, 1, 2
+# trot_tune_knob
+TUNE_EXCHANGE_TILES, TUNE_EXCHANGE_GRID = 0, 1
 # trot_precision
 FP64, MIXED = 0, 1
 # trot_op
@@ -108,6 +110,8 @@ _SIGNATURES = {
                                  _p, _p, _p, ctypes.c_size_t, _p]),
     "trot_fp_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(TrotSystem)]),
     "trot_fp_step": (_i, [ctypes.POINTER(TrotSystem), ctypes.POINTER(TrotState), _p, _p, _p, ctypes.c_size_t, _p]),
+    "trot_set_tuning": (_i, [_i, _i]),
+    "trot_get_tuning": (_i, [_i]),
     "trot_profile_enable": (_i, [_i]),
     "trot_profile_collect": (_i, [_i, ctypes.c_char_p, _p, _p]),
 }

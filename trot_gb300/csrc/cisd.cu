@@ -573,7 +573,7 @@ static int cisd_run(const trot_cisd* c, int W, const double2* w, CisdBuffers& b,
   TROT_TIMED("cisd_ci2g", st, launch_zgemm_cr(W, nv, nv, 1.0, b.x, nv, c->ci2m, nv, false, b.cg, nv, false, st));
   if (stage == 0) return TROT_OK;
   const size_t smem = cisd_mats_smem(N, n, v);
-  if (smem > 48 * 1024) cudaFuncSetAttribute(cisd_mats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 40 * 1024) cudaFuncSetAttribute(cisd_mats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   TROT_TIMED("cisd_mats", st, ([&]() -> int {
     cisd_mats_kernel<<<W, 256, smem, st>>>(N, n, v, b.green, c->ci1, b.cg, b.x, c->h1, b.m1, b.m2, b.wsc);
     TROT_CHECK_LAUNCH("cisd_mats_kernel");

@@ -77,7 +77,7 @@ int launch_green(const Spins& sp, int W, int N, const double2* wa, const double2
     set_error("green: walker tile of %zu bytes exceeds shared memory", smem);
     return TROT_ERR_UNSUPPORTED;
   }
-  if (smem > 48 * 1024)
+  if (smem > 40 * 1024)
     cudaFuncSetAttribute(green_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   green_kernel<<<W, kGreenThreads, smem, st>>>(sp, N, wa, wb, green, ovlp_out, e1_out);
   TROT_CHECK_LAUNCH("green_kernel");

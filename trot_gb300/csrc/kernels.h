@@ -27,6 +27,7 @@ struct StepBuffers {
 };
 
 Spins make_spins(const trot_system* s);
+int tune_get(int knob);  // tune.cu: 0 = default
 
 // Green's function / overlap per walker (green.cu).
 // green: complex (W, ntot*N) half Green's functions, spin blocks concatenated

@@ -170,7 +170,7 @@ static int launch_green_ff(const Spins& sp, int W, int N, const double2* wa, con
     set_error("green_ff: %zu bytes of shared memory needed", smem);
     return TROT_ERR_UNSUPPORTED;
   }
-  if (smem > 48 * 1024) cudaFuncSetAttribute(green_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 40 * 1024) cudaFuncSetAttribute(green_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   green_ff_kernel<<<W, 256, smem, st>>>(sp, N, wa, wb, green, e1_out);
   TROT_CHECK_LAUNCH("green_ff_kernel");
   return TROT_OK;
@@ -1207,6 +1207,68 @@ __global__ void tc_weight_kernel(TrotterArgs a, const double2* __restrict__ ov_n
   if (b < a.W) phaseless_update(a, b, ov_new[b]);
 }
 
+// New overlaps of the propagated walkers and their phaseless weights in one pass:
+// M_s = C_s^T w'_s in float-float (four independent accumulators per element),
+// det by FP64 Gauss-Jordan, overlap = prod_s det(M_s)^mult_s, then phaseless_update.
+// One CTA per walker.
+__global__ void __launch_bounds__(256) overlap_weight_ff_kernel(Spins sp, TrotterArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double2 red[32];
+  __shared__ int piv;
+  const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const int N = a.N;
+  const int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
+  ffc* Wf = reinterpret_cast<ffc*>(smem_raw);                      // N x n
+  ff* Cf = reinterpret_cast<ff*>(Wf + (size_t)N * nmax);            // N x n
+  double2* Md = reinterpret_cast<double2*>(Cf + (size_t)N * nmax + ((N * nmax) & 1));  // n x n
+  double2 det_all = cmk(1.0, 0.0);
+  for (int s = 0; s < sp.nspin; ++s) {
+    const int n = sp.n[s];
+    const double2* w = (s == 0 ? a.out_a : a.out_b) + (size_t)b * N * n;
+    const double* C = sp.mo[s];
+    __syncthreads();
+    for (int e = tid; e < N * n; e += nt) {
+      const double2 x = w[e];
+      Wf[e] = ffc{ff_from_d(x.x), ff_from_d(x.y)};
+      Cf[e] = ff_from_d(C[e]);
+    }
+    __syncthreads();
+    for (int e = tid; e < n * n; e += nt) {
+      const int i = e / n, j = e % n;
+      ff ar[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      ff ai[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      int p = 0;
+      for (; p + 4 <= N; p += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const ff c = Cf[(p + u) * n + i];
+          const ffc x = Wf[(p + u) * n + j];
+          ff_mad(ar[u], c, x.re);
+          ff_mad(ai[u], c, x.im);
+        }
+      }
+      for (; p < N; ++p) {
+        const ff c = Cf[p * n + i];
+        const ffc x = Wf[p * n + j];
+        ff_mad(ar[0], c, x.re);
+        ff_mad(ai[0], c, x.im);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        ar[u] = ff_fast(ar[u].hi, ar[u].lo);
+        ai[u] = ff_fast(ai[u].hi, ai[u].lo);
+      }
+      const ff sr = ff_add(ff_add(ar[0], ar[1]), ff_add(ar[2], ar[3]));
+      const ff si = ff_add(ff_add(ai[0], ai[1]), ff_add(ai[2], ai[3]));
+      Md[e] = make_double2(ff_d(sr), ff_d(si));
+    }
+    __syncthreads();
+    const double2 det = block_gauss_jordan(Md, n, n, nullptr, &piv, red);
+    det_all = cmul(det_all, sp.mult[s] == 2 ? cmul(det, det) : det);
+  }
+  if (tid == 0) phaseless_update(a, b, det_all);
+}
+
 // ------------------------------------------------------------------ host orchestration
 static int check_mixed_shapes(const trot_system* s, const Spins& sp) {
   if (!s->mixed) { set_error("mixed precision needs a trot_mixed context"); return TROT_ERR_NULL_PTR; }
@@ -1260,7 +1322,8 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
     a.L = L;
     a.G = G; a.W = W; a.mult = sp.mult[q];
     // persistent grid: one CTA per SM walks (Cholesky block, 16 walker tiles) items
-    a.tiles_per_item = std::min(16, L.ntiles);
+    const int tpi = tune_get(TROT_TUNE_EXCHANGE_TILES);
+    a.tiles_per_item = std::min(tpi > 0 ? tpi : 16, L.ntiles);
     a.chunks = (L.ntiles + a.tiles_per_item - 1) / a.tiles_per_item;
     a.n_items = L.nblk * a.chunks;
     a.rot_img = s->mixed->rot_slices[mq];
@@ -1271,7 +1334,8 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
     a.xpart = m.xpart;
     a.nblk_total = m.nblk_total;
     a.status = m.status;
-    dim3 grid(std::min(a.n_items, 152));
+    const int gknob = tune_get(TROT_TUNE_EXCHANGE_GRID);
+    dim3 grid(std::min(a.n_items, gknob > 0 ? gknob : 152));
     TROT_TIMED("exchange_exact_tc", st, launch_exchange_exact(L.n_pad / 4, grid, a, st));
   }
   const int n = W * G;
@@ -1393,10 +1457,16 @@ static int run_trotter_tc(const trot_system* s, const Spins& sp, const TrotterAr
     TROT_CHECK_LAUNCH("trotter_tc_kernel");
     return TROT_OK;
   })());
-  if (t.overlaps) {  // step mode: FP64 overlaps of the new walkers, then the phaseless weights
-    TROT_TIMED("overlap_fp64", st, launch_green(sp, W, N, t.out_a, t.out_b, nullptr, m.ov_new, nullptr, st));
-    tc_weight_kernel<<<(W + 127) / 128, 128, 0, st>>>(t, m.ov_new);
-    TROT_CHECK_LAUNCH("tc_weight_kernel");
+  if (t.overlaps) {  // step mode: overlaps of the new walkers (float-float C^T w', FP64 LU) and weights
+    const int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
+    const size_t smem = (size_t)N * nmax * (sizeof(ffc) + sizeof(ff)) + 16 + (size_t)nmax * nmax * 16;
+    if (smem > 40 * 1024)
+      cudaFuncSetAttribute(overlap_weight_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    TROT_TIMED("overlap_weight_ff", st, ([&]() -> int {
+      overlap_weight_ff_kernel<<<W, 256, smem, st>>>(sp, t);
+      TROT_CHECK_LAUNCH("overlap_weight_ff_kernel");
+      return TROT_OK;
+    })());
   }
   return TROT_OK;
 }

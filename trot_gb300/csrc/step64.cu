@@ -116,7 +116,7 @@ int launch_trotter(const Spins& sp, const TrotterArgs& a, cudaStream_t st) {
     set_error("trotter: 3 walker tiles of %zu bytes exceed shared memory", smem);
     return TROT_ERR_UNSUPPORTED;
   }
-  if (smem > 48 * 1024)
+  if (smem > 40 * 1024)
     cudaFuncSetAttribute(trotter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   trotter_kernel<<<a.W, kTrotThreads, smem, st>>>(sp, a);
   TROT_CHECK_LAUNCH("trotter_kernel");
@@ -205,7 +205,7 @@ int launch_exchange(const Spins& sp, int W, int N, int G, const double2* green, 
     set_error("exchange: tile of %zu bytes exceeds shared memory", smem);
     return TROT_ERR_UNSUPPORTED;
   }
-  if (smem > 48 * 1024)
+  if (smem > 40 * 1024)
     cudaFuncSetAttribute(exchange_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   dim3 grid(exchange_chunks(G), W);
   exchange_kernel<<<grid, 256, smem, st>>>(sp, N, G, green, partial);

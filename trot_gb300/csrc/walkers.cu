@@ -77,7 +77,7 @@ int launch_qr(const Spins& sp, int W, int N, double2* wa, double2* wb, double2* 
     set_error("qr: walker tile of %zu bytes exceeds shared memory", smem);
     return TROT_ERR_UNSUPPORTED;
   }
-  if (smem > 48 * 1024) cudaFuncSetAttribute(qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (smem > 40 * 1024) cudaFuncSetAttribute(qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   qr_kernel<<<W, kQrThreads, smem, st>>>(N, sp.n[0], wa, norm_out, sp.mult[0] == 2 ? 1 : 0, write_q ? 1 : 0);
   TROT_CHECK_LAUNCH("qr_kernel");
   if (sp.nspin == 2) {

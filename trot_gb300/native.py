@@ -20,12 +20,15 @@ def ptr(t) -> int:
 
 
 def workspace(nbytes: int) -> torch.Tensor:
-    """A cached uint8 device buffer of at least ``nbytes`` (per device)."""
+    """A cached uint8 device buffer of at least ``nbytes``, one per (device,
+    stream): calls on one stream are ordered and may share it, calls running
+    concurrently on different streams (fragment batches) get their own."""
     dev = torch.cuda.current_device()
-    buf = _workspaces.get(dev)
+    key = (dev, torch.cuda.current_stream().cuda_stream)
+    buf = _workspaces.get(key)
     if buf is None or buf.numel() < nbytes:
         buf = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=f"cuda:{dev}")
-        _workspaces[dev] = buf
+        _workspaces[key] = buf
     return buf
 
 
