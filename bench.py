@@ -69,6 +69,25 @@ def flops_per_walker_step_cisd(N, n, G, nterms=6):
     return d
 
 
+# DRAM bytes per launch of the dominant kernel, measured by ncu on the named workload (one counter
+# pass; command and table in profiles/dram_traffic_uhf_n120_w1024_mixed.md)
+NCU_DRAM_BYTES = {("cfg2_uhf_n120", "mixed", "exchange_exact_tc"): ((41.47 + 0.26) + (39.87 + 0.02)) / 2 * 1e6}
+
+
+def exchange_tensor_flops(cfg, W):
+    """BF16 tensor flops the exact-slice exchange kernel issues per launch (mean over spins):
+    15 products of 128 x 48 x 128 per (Cholesky block, walker tile)."""
+    N, (na, nb), G = cfg["norb"], cfg["nelec"], cfg["nchol"]
+    spins = [na] if cfg["kind"] == "rhf_r" else [na, nb]
+    tot = 0
+    for n in spins:
+        n_pad = (n + 3) & ~3
+        wb = 48 // (2 * n_pad)
+        gb = max(1, 128 // n)
+        tot += 15 * 2 * 128 * 48 * 128 * ((W + wb - 1) // wb) * ((G + gb - 1) // gb)
+    return tot / len(spins)
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -170,7 +189,8 @@ def build_workload(cfg, precision):
 
 def build_workload_cisd(cfg, precision):
     """CISD trial (N, nocc, G) with restricted walkers; "mixed" = the reference's
-    default CISD dtypes (tensor-core l2ci2, FP32 gl), "fp64" = testing=True."""
+    default CISD dtypes (tensor-core l2ci2, FP32 gl) and tensor-core propagation,
+    "fp64" = testing=True and FP64 propagation."""
     import torch
 
     import trot_gb300 as tg
@@ -188,7 +208,7 @@ def build_workload_cisd(cfg, precision):
     else:
         meas_ops = tg.make_cisd_meas_ops(sysm, mixed_precision=False, testing=True)
     meas_ctx = meas_ops.build_meas_ctx(ham, trial)
-    prop_ops = tg.make_prop_ops("restricted", "restricted")
+    prop_ops = tg.make_prop_ops("restricted", "restricted", mixed_precision=(precision == "mixed"))
     prop_ctx = prop_ops.build_prop_ctx(ham, trial_ops.get_rdm1(trial), params)
     state = prop_ops.init_prop_state(sys=sysm, ham_data=ham, trial_ops=trial_ops, trial_data=trial,
                                      meas_ops=meas_ops, params=params)
@@ -505,8 +525,18 @@ def main():
     peak = peaks["bf16_tflops"]
     roofline = {"bound": "tensor", "kernel": tname, "achieved": achieved_tflops, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved_tflops / peak, "peak_source": f"{peak_src} bf16 dense (MEASURED_PEAKS.json)",
-                "traffic": None, "algorithmic_flops_per_launch": kfl * W,
+                "traffic": NCU_DRAM_BYTES.get((args.config, args.precision, tname)),
+                "algorithmic_flops_per_launch": kfl * W,
                 "note": "fp64 kernels run on the FP64 pipe; the bf16 tensor peak is the denominator the contract names"}
+    if tname == "exchange_exact_tc":
+        # the exact-slice kernel executes 15 BF16 products per output tile on top of the
+        # algorithmic (FP64-equivalent) contraction: tensor work actually issued per launch
+        ex = exchange_tensor_flops(cfg, W)
+        roofline["executed_bf16_flops_per_launch"] = ex
+        roofline["executed_bf16_tflops"] = ex / per_launch_s / 1e12
+        roofline["executed_frac"] = ex / per_launch_s / 1e12 / peak
+        roofline["traffic_note"] = ("DRAM bytes per launch (mean of the two spin launches) measured by ncu on this "
+                                    "workload: profiles/dram_traffic_uhf_n120_w1024_mixed.md")
     step_flops = sum(fl.values()) * W
     kernels = {k: {"ms_total": round(v[0], 4), "launches": v[1], "ms_per_launch": round(v[0] / max(v[1], 1), 5)}
                for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}

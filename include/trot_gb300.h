@@ -308,11 +308,14 @@ int trot_cisd_rdm1(const trot_cisd* cisd, int n_walkers, const double* walkers, 
  * make_cisd_meas_ops): force bias (and, if energy_out is not null, the local
  * energy of the incoming walkers), shifted fields, VHS, Taylor propagation
  * with one-body half steps, CISD overlaps of the new walkers, phaseless
- * weights and population shift, all FP64.  `prop` carries the propagation
- * context (kind TROT_RHF_R, precision TROT_FP64, n_walkers, n_exp_terms, dt,
- * sqrt_dt, h0_prop, weight_floor/cap, pop_control_damping, exp_h1_half,
- * chol_flat, mf_shifts_im); state->walkers_a (W, norb, nocc) is updated in
- * place.  Workspace: trot_cisd_workspace_size(cisd, W, TROT_OP_PROP_STEP). */
+ * weights and population shift.  `prop` carries the propagation context (kind
+ * TROT_RHF_R, n_walkers, n_exp_terms, dt, sqrt_dt, h0_prop,
+ * weight_floor/cap, pop_control_damping, exp_h1_half, chol_flat,
+ * mf_shifts_im; precision TROT_FP64, or TROT_MIXED with prop->mixed for the
+ * tensor-core VHS / Taylor action); state->walkers_a (W, norb, nocc) is
+ * updated in place.  Workspace: trot_cisd_workspace_size(cisd, W,
+ * TROT_OP_PROP_STEP), plus trot_workspace_size(prop, TROT_OP_APPLY_TROTTER)
+ * bytes (at the next 256-byte boundary) for the mixed propagation. */
 int trot_cisd_prop_step(const trot_cisd* cisd, const trot_system* prop, const trot_state* state,
                         const double* fields, double* energy_out, void* workspace, size_t workspace_bytes,
                         void* stream);

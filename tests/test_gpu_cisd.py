@@ -179,3 +179,36 @@ def test_cisd_rejects_bad_inputs():
     core = tg.CisdTrial(cs.ci1[1:], cs.ci2[1:, :, 1:, :], nocc_t_core=1)
     with pytest.raises(NotImplementedError):
         S.trial_ops.overlap(dev(w), core)
+
+
+def test_cisd_step_mixed_propagation():
+    """Tensor-core VHS / Taylor action in the CISD step: walkers within 2e-5 relative of the FP64
+    step on the same fields; weights within 1e-3 on live walkers; same local energy (FP64 meas)."""
+    import trot_gb300 as tg
+    from trot_gb300 import synthetic
+
+    N, n, G, W = 40, 6, 100, 24
+    cs, w = _synthetic(N, n, G, W, 0.05, seed=3)
+    S = CisdSetup(cs.h0, cs.h1, cs.chol, cs.ci1, cs.ci2, W, dt=0.01)
+    pm = tg.make_prop_ops("restricted", "restricted", mixed_precision=True)
+    pcm = pm.build_prop_ctx(S.ham, S.trial_ops.get_rdm1(S.trial), S.params)
+    ov = cpu(S.overlap(dev(w)))
+    fields = dev(synthetic.fields(W, G, 1, seed=4)[0])
+
+    def run(ops, ctx):
+        st = tg.PropState(walkers=dev(w), weights=dev(np.ones(W)), overlaps=dev(ov), rng_key=tg.rng.key(0),
+                          scalars=dev(np.array([0.1, 0.1])), node_encounters=dev(np.zeros(1, np.int64)))
+        e = torch.empty(W, dtype=torch.complex128, device="cuda")
+        st = ops.step(st, params=S.params, ham_data=S.ham, trial_data=S.trial, trial_ops=S.trial_ops,
+                      meas_ops=S.meas_ops, meas_ctx=S.meas_ctx, prop_ctx=ctx, fields=fields, energy_out=e)
+        return st, e
+
+    s64, e64 = run(S.prop_ops, S.prop_ctx)
+    smx, emx = run(pm, pcm)
+    assert rel(cpu(smx.walkers), cpu(s64.walkers)) <= 2e-5
+    assert np.array_equal(cpu(emx), cpu(e64))
+    wf, wm = cpu(s64.weights), cpu(smx.weights)
+    assert np.array_equal(wf > 0, wm > 0)
+    live = wf > 0
+    if live.any():
+        assert rel(wm[live], wf[live]) <= 1e-3

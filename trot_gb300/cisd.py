@@ -272,9 +272,10 @@ def make_cisd_meas_ops(sys: System, memory_mode: str = "high", mixed_precision: 
 
 
 def afqmc_step(state: PropState, *, params, ham_data, trial_data: CisdTrial, meas_ctx: CisdMeasCtx, prop_ctx,
-               fields=None, energy_out=None) -> PropState:
+               fields=None, energy_out=None, precision: int = _lib.FP64) -> PropState:
     """trot/prop/afqmc.py:79-144 with the CISD meas ops, as one call
-    (``trot_cisd_prop_step``); the state's buffers are updated in place."""
+    (``trot_cisd_prop_step``); the state's buffers are updated in place.
+    ``precision`` = MIXED propagates on the tensor cores (VHS, Taylor action)."""
     w = state.walkers
     W = _check(w, trial_data)
     c = _struct(trial_data, meas_ctx)
@@ -292,6 +293,13 @@ def afqmc_step(state: PropState, *, params, ham_data, trial_data: CisdTrial, mea
     s.weight_floor = float(getattr(params, "weight_floor", 1.0e-3))
     s.weight_cap = float(getattr(params, "weight_cap", 100.0))
     s.pop_control_damping = float(getattr(params, "pop_control_damping", 0.1))
+    extra = 0
+    if precision == _lib.MIXED:
+        from . import mixed
+
+        mx = mixed.context(None, prop_ctx)
+        s.precision, s.mixed = _lib.MIXED, mx.data_ptr()
+        extra = _lib.load().trot_workspace_size(ctypes.byref(s), _lib.OP_APPLY_TROTTER) + 256
     if fields is None:
         fields = rng.normal_fields(state.rng_key, W, G)
     elif fields.dtype != torch.float64 or not fields.is_cuda or tuple(fields.shape) != (W, G):
@@ -301,7 +309,11 @@ def afqmc_step(state: PropState, *, params, ham_data, trial_data: CisdTrial, mea
     st.walkers_a, st.walkers_b = w.data_ptr(), 0
     st.weights, st.overlaps = state.weights.data_ptr(), state.overlaps.data_ptr()
     st.scalars, st.node_encounters = state.scalars.data_ptr(), state.node_encounters.data_ptr()
-    ws, nws = _workspace(c, W, _lib.OP_PROP_STEP)
+    n = _lib.load().trot_cisd_workspace_size(ctypes.byref(c), W, _lib.OP_PROP_STEP)
+    if n == 0:
+        raise _lib.TrotError(1, _lib.load().trot_last_error().decode())
+    buf = native.workspace(n + 256 + extra)
+    ws, nws = buf.data_ptr(), buf.numel()
     _lib.call("trot_cisd_prop_step", ctypes.byref(c), ctypes.byref(s), ctypes.byref(st), fields.data_ptr(),
               native.ptr(energy_out), ws, nws, native.stream_ptr())
     return state

@@ -712,11 +712,14 @@ int trot_cisd_prop_step(const trot_cisd* c, const trot_system* prop, const trot_
   if (!prop || !state || !fields) { set_error("null system, state or fields"); return TROT_ERR_NULL_PTR; }
   const int W = prop->n_walkers;
   TROT_TRY(check_cisd(c, W));
-  if (prop->kind != TROT_RHF_R || prop->precision != TROT_FP64 || prop->norb != c->norb ||
-      prop->nchol != c->nchol || prop->nocc_a != c->nocc) {
-    set_error("CISD step: propagation context must be restricted FP64 with norb %d, nchol %d, nocc %d", c->norb,
+  if (prop->kind != TROT_RHF_R || prop->norb != c->norb || prop->nchol != c->nchol || prop->nocc_a != c->nocc) {
+    set_error("CISD step: propagation context must be restricted with norb %d, nchol %d, nocc %d", c->norb,
               c->nchol, c->nocc);
     return TROT_ERR_BAD_SHAPE;
+  }
+  if (prop->precision != TROT_FP64 && !(prop->precision == TROT_MIXED && prop->mixed)) {
+    set_error("CISD step: propagation precision must be FP64, or mixed with a trot_mixed context");
+    return TROT_ERR_BAD_DTYPE;
   }
   if (!prop->exp_h1_half || !prop->chol_flat || !prop->mf_shifts_im) {
     set_error("CISD step: null propagation context array");
@@ -731,6 +734,17 @@ int trot_cisd_prop_step(const trot_cisd* c, const trot_system* prop, const trot_
   CisdBuffers b;
   carve_cisd(c, W, TROT_OP_PROP_STEP, cv, b);
   if (!cv.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, cv.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
+  // mixed propagation: the tensor-core Trotter path gets its own workspace after the CISD buffers
+  const size_t cisd_bytes = (cv.used + 255) & ~(size_t)255;
+  size_t prop_bytes = 0;
+  if (prop->precision == TROT_MIXED) {
+    prop_bytes = trot_workspace_size(prop, TROT_OP_APPLY_TROTTER);
+    if (prop_bytes == 0) return TROT_ERR_BAD_SHAPE;
+    if (cisd_bytes + prop_bytes > ws_bytes) {
+      set_error("workspace too small: %zu < %zu", ws_bytes, cisd_bytes + prop_bytes);
+      return TROT_ERR_WORKSPACE_TOO_SMALL;
+    }
+  }
   cudaStream_t st = (cudaStream_t)stream;
   const int N = c->norb, G = c->nchol;
   double2* w = (double2*)state->walkers_a;
@@ -747,13 +761,19 @@ int trot_cisd_prop_step(const trot_cisd* c, const trot_system* prop, const trot_
   // 2. shifted fields, 3. VHS, 4. propagation in place
   TROT_TIMED("fields", st,
              launch_fields(W, G, prop->sqrt_dt, b.fb, prop->mf_shifts_im, fields, b.xs, b.shift_term, b.fb_term, st));
-  TROT_TIMED("vhs_fp64", st,
-             launch_zgemm_cr(W, N * N, G, 1.0, b.xs, G, prop->chol_flat, N * N, false, b.vhs, N * N, false, st));
   Spins sp = make_spins(prop);
   TrotterArgs a{};
   a.W = W; a.N = N; a.G = G; a.nterms = prop->n_exp_terms; a.sqrt_dt = prop->sqrt_dt; a.expH = prop->exp_h1_half;
-  a.vhs = b.vhs; a.in_a = w; a.out_a = w;
-  TROT_TIMED("trotter_fp64", st, launch_trotter(sp, a, st));
+  a.in_a = w; a.out_a = w;
+  if (prop->precision == TROT_MIXED) {
+    TROT_TRY(trot_apply_trotter(prop, (const double*)w, nullptr, (const double*)b.xs, (double*)w, nullptr,
+                                static_cast<char*>(ws) + cisd_bytes, ws_bytes - cisd_bytes, stream));
+  } else {
+    TROT_TIMED("vhs_fp64", st,
+               launch_zgemm_cr(W, N * N, G, 1.0, b.xs, G, prop->chol_flat, N * N, false, b.vhs, N * N, false, st));
+    a.vhs = b.vhs;
+    TROT_TIMED("trotter_fp64", st, launch_trotter(sp, a, st));
+  }
   // 5. CISD overlaps of the new walkers, weights, population shift
   TROT_TRY(cisd_run(c, W, w, b, 0, st));
   cisd_overlap_kernel<<<W, 256, 0, st>>>(c->nocc * c->nvir, b.x, b.cg, b.wsc, b.det2, b.ov_new);

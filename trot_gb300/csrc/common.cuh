@@ -96,7 +96,7 @@ TROT_D double2 block_gauss_jordan(double2* A, int n, int ld, double2* inv, int* 
       inv[i * ld + j] = cmk(i == j ? 1.0 : 0.0, 0.0);
     }
   }
-  __shared__ double2 det_s;
+  __shared__ double2 det_s, rp_s;  // running determinant; reciprocal of the current pivot
   if (tid == 0) det_s = cmk(1.0, 0.0);
   __syncthreads();
   for (int k = 0; k < n; ++k) {
@@ -125,11 +125,14 @@ TROT_D double2 block_gauss_jordan(double2* A, int n, int ld, double2* inv, int* 
     }
     __syncthreads();
     const double2 piv = A[k * ld + k];
-    if (tid == 0) det_s = cmul(p != k ? cmk(-det_s.x, -det_s.y) : det_s, piv);
+    if (tid == 0) {
+      det_s = cmul(p != k ? cmk(-det_s.x, -det_s.y) : det_s, piv);
+      rp_s = cdiv(cmk(1.0, 0.0), piv);  // one division per pivot, shared by all threads
+    }
+    __syncthreads();
+    const double2 rp = rp_s;
     if (inv) {
       // Gauss-Jordan: normalise row k, eliminate column k from every other row
-      const double2 rp = cdiv(cmk(1.0, 0.0), piv);
-      __syncthreads();
       for (int j = tid; j < n; j += nt) {
         A[k * ld + j] = cmul(A[k * ld + j], rp);
         inv[k * ld + j] = cmul(inv[k * ld + j], rp);
@@ -148,12 +151,13 @@ TROT_D double2 block_gauss_jordan(double2* A, int n, int ld, double2* inv, int* 
         if (i != k) A[i * ld + k] = cmk(0.0, 0.0);
       __syncthreads();
     } else {
-      // plain LU elimination below the pivot
-      for (int e = tid; e < (n - k - 1) * (n - k); e += nt) {
-        int i = k + 1 + e / (n - k), j = k + e % (n - k);
-        if (j == k) continue;
-        double2 f = cdiv(A[i * ld + k], piv);
-        A[i * ld + j] = csub(A[i * ld + j], cmul(f, A[k * ld + j]));
+      // plain LU elimination below the pivot: multipliers once per row (stored in column k)
+      for (int i = k + 1 + tid; i < n; i += nt) A[i * ld + k] = cmul(A[i * ld + k], rp);
+      __syncthreads();
+      const int m = n - k - 1;
+      for (int e = tid; e < m * m; e += nt) {
+        const int i = k + 1 + e / m, j = k + 1 + e % m;
+        A[i * ld + j] = csub(A[i * ld + j], cmul(A[i * ld + k], A[k * ld + j]));
       }
       __syncthreads();
     }

@@ -138,7 +138,7 @@ def afqmc_step(state: PropState, *, params, ham_data, trial_data, meas_ops: Meas
         from . import cisd
 
         return cisd.afqmc_step(state, params=params, ham_data=ham_data, trial_data=trial_data, meas_ctx=meas_ctx,
-                               prop_ctx=prop_ctx, fields=fields, energy_out=energy_out)
+                               prop_ctx=prop_ctx, fields=fields, energy_out=energy_out, precision=precision)
     kind = native.kind_of(trial_data, walker_kind)
     wa, wb = native.split_walkers(state.walkers, kind)
     W = wa.shape[0]
