@@ -179,18 +179,23 @@ static int launch_green_ff(const Spins& sp, int W, int N, const double2* wa, con
 // ------------------------------------------------------------------ layouts
 static constexpr size_t kTcImgBytes = 3 * 128 * 256 * 2;  // [Vr | Vi] operand image of one walker (192 KB)
 static constexpr int kKP = 128;       // padded orbital dimension of the exact product
-static constexpr int kBN = 48;        // MMA N of the exchange tile (columns = walker rows)
+static constexpr int kBN = 96;        // MMA N of the exchange tile (columns = walker rows)
+static constexpr int kKH = 64;        // K per half-slice of the Green's-function operand (ring unit)
 static constexpr int kGroups = 5;     // accumulators for t + u = 0..4
 static constexpr int kSlices = 5;
 static constexpr int kSlots = 2;      // ring of Green's-function slice buffers
 static constexpr int kMaxOcc = 16;    // largest n the epilogue handles (2 * n_pad <= 32 columns per walker)
 static constexpr uint32_t kAImg = (uint32_t)kSlices * 128 * kKP * 2;  // 163840 B: 5 rot slices of a tile
-static constexpr uint32_t kBImg = (uint32_t)kBN * kKP * 2;            // 12288 B: one green slice of a tile
+static constexpr uint32_t kBImg = (uint32_t)kBN * kKH * 2;            // 12288 B: one K-half of a green slice
 
 // Row-major [rows x 128] bf16 tile -> core-matrix order (8 x 8 blocks, K fastest):
 // element (r, k) at 16-bit index (r/8)*1024 + (k/8)*64 + (r%8)*8 + k%8.
 TROT_HD uint32_t img_idx(int r, int k) {
   return (uint32_t)((r >> 3) * 1024 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7));
+}
+// Same for a [rows x 64] tile: element (r, k) at (r/8)*512 + (k/8)*64 + (r%8)*8 + k%8.
+TROT_HD uint32_t img_idx64(int r, int k) {
+  return (uint32_t)((r >> 3) * 512 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7));
 }
 
 struct SpinLayout {
@@ -280,8 +285,9 @@ size_t mixed_workspace_size(const trot_system* s, int op) {
 // p, as exact fixed-point bf16 slices: v = round(x 2^(40 - e)) (|v| <= 2^40),
 // balanced base-256 digits q_0..q_4 (|q| <= 255), x ~= sum_t q_t 2^(e - 8(t+1)).
 // Written straight into the shared-memory image of the exchange kernel's B
-// operand: per walker tile, per slice, kBN rows (walker bl, row c*n_pad + j) x
-// kKP orbitals in core-matrix order; padding rows are zero.  One CTA per tile.
+// operand: per walker tile, per slice, per K-half, kBN rows (walker bl, row
+// c*n_pad + j) x 64 orbitals in core-matrix order; padding rows are zero.
+// One CTA per tile.
 __global__ void __launch_bounds__(256)
 green_slices_kernel(int N, int n, int n_pad, int WB, int W, int ntot, int off, const double2* __restrict__ green,
                     uint16_t* __restrict__ gq, int32_t* __restrict__ ge) {
@@ -325,22 +331,25 @@ green_slices_kernel(int N, int n, int n_pad, int WB, int W, int ntot, int off, c
         d = d > 255 ? 255 : (d < -255 ? -255 : d);
         v -= d << sh;
         const __nv_bfloat16 h = __int2bfloat16_rn((int)d);
-        gq[((size_t)tile * kSlices + t) * kBN * kKP + img_idx(row, p)] = *reinterpret_cast<const uint16_t*>(&h);
+        gq[(((size_t)tile * kSlices + t) * 2 + (p >> 6)) * kBN * kKH + img_idx64(row, p & 63)] =
+            *reinterpret_cast<const uint16_t*>(&h);
       }
     }
   }
 }
 
 // ------------------------------------------------------------------ exact exchange / trace kernel
-// One CTA = one tile of gb Cholesky vectors (128 rows (g, i)) against a range of
-// walker tiles (WB walkers x S rows, kBN MMA columns).  Warp 8 (one lane) is
-// the producer: it bulk-copies the five rot_chol slices of the tile into shared
-// memory once, streams the Green's-function slices of each walker tile through
-// a 3-slot ring, and issues the MMAs: products q_t (rot) x q_u (green) with
-// t + u = d accumulate exactly in TMEM group d (d = 0..4), in one of two
-// accumulator buffers, so the MMAs of walker tile k+1 overlap the epilogue of
-// tile k.  Warps 0-7 are the epilogue (two warps per TMEM lane quadrant, each
-// taking half of the columns j): they rebuild
+// A persistent CTA walks work items = (tile of gb Cholesky vectors: 128 rows
+// (g, i), run of walker tiles: WB walkers x S rows = kBN = 96 MMA columns).
+// Warp 16 (one lane) is the producer: it bulk-copies the five rot_chol slices of
+// the item's Cholesky tile into shared memory, streams the Green's-function
+// slices of each walker tile as 64-wide K halves through a 2-slot ring, and
+// issues the MMAs: products q_t (rot) x q_u (green) with t + u = d accumulate
+// exactly in TMEM group d (d = 0..4).  One accumulator buffer (5 x 96 columns):
+// the epilogue copies a tile's values out of TMEM into registers and releases it
+// at once, so the MMAs of the next tile overlap the epilogue's arithmetic.
+// Warps 0-15 are the epilogue (four warps per TMEM lane quadrant, each taking a
+// quarter of the columns j): they rebuild
 // f_g[i][j] = 2^(eA + eB - 16) sum_d 2^(-8 d) A_d in float-float and form, per
 // walker, the exchange sum_g sum_ij f_gij f_gji (trot/meas/rhf.py:33-60) and the
 // traces c_g = sum_i f_gii (Coulomb / force bias, trot/meas/rhf.py:119-125).
@@ -384,11 +393,12 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
   uint64_t* a_full = bars;
   uint64_t* full = bars + 1;        // [kSlots <= 3]
   uint64_t* empty = bars + 4;       // [kSlots <= 3]
-  uint64_t* acc_full = bars + 7;    // [2]
-  uint64_t* acc_empty = bars + 9;   // [2]
+  uint64_t* acc_full = bars + 7;    // the tile's accumulators are complete
+  uint64_t* acc_empty = bars + 8;   // the epilogue has copied them out of TMEM
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 11);
   int* flag = reinterpret_cast<int*>(bars + 12);  // epilogue go/stop broadcast
   uint64_t* a_free = bars + 13;     // the MMAs of the previous work item are done with sA
+  constexpr int WBT = 24 / (2 * JH);  // walkers per tile: kBN / (2 n_pad) with n_pad = 4 JH
 
   const SpinLayout& L = a.L;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -402,10 +412,8 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
       tc::mbar_init(&full[k], 1);
       tc::mbar_init(&empty[k], 1);
     }
-    for (int k = 0; k < 2; ++k) {
-      tc::mbar_init(&acc_full[k], 1);
-      tc::mbar_init(&acc_empty[k], 16);
-    }
+    tc::mbar_init(acc_full, 1);
+    tc::mbar_init(acc_empty, 16);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   tc::fence_before_sync();
@@ -420,35 +428,39 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
       const uint32_t idesc = tc::idesc_bf16_f32(128, kBN);
       const uint32_t sA_u = tc::smem_u32(sA), ring_u = tc::smem_u32(ring);
       const uint64_t ad0 = tc::smem_desc(sA_u, 128, kKP * 16);
-      const uint32_t adlo = (uint32_t)ad0, dhi = (uint32_t)(ad0 >> 32);  // A and B share the high word
-      int g_issue = 0, g_base = 0, tg = 0, kitem = 0;  // CTA-wide slice / tile / item counters
+      const uint32_t adlo = (uint32_t)ad0, ahi = (uint32_t)(ad0 >> 32);
+      const uint64_t bd0 = tc::smem_desc(ring_u, 128, kKH * 16);
+      const uint32_t bhi = (uint32_t)(bd0 >> 32);
+      constexpr int kUnits = kSlices * 2;  // ring units per tile: (slice u, K-half h)
+      int g_issue = 0, g_base = 0, tg = 0, kitem = 0;  // CTA-wide unit / tile / item counters
       for (int item = blockIdx.x; item < a.n_items && ok; item += gridDim.x, ++kitem) {
         const int blk = item / a.chunks;
         const int t0 = (item % a.chunks) * a.tiles_per_item, t1 = min(L.ntiles, t0 + a.tiles_per_item);
-        const int ntl = t1 - t0, total = ntl * kSlices;
+        const int ntl = t1 - t0, total = ntl * kUnits;
         if (kitem > 0) ok = tc::mbar_wait(a_free, (uint32_t)((kitem - 1) & 1));
         if (!ok) break;
         tc::mbar_expect_tx(a_full, kAImg);
         tc::bulk_g2s(sA, a.rot_img + (size_t)blk * (kAImg / 2), kAImg, a_full);
         for (int sidx = 0; sidx < total && ok; ++sidx) {
-          const int i = sidx / kSlices, u = sidx % kSlices;
-          // keep up to kSlots slice copies of this item in flight ahead of the MMAs
+          const int i = sidx / kUnits, uh = sidx % kUnits, u = uh >> 1, h = uh & 1;
+          // keep up to kSlots ring units of this item in flight ahead of the MMAs
           while (g_issue < g_base + total && g_issue < g_base + sidx + kSlots && ok) {
             const int slot = g_issue % kSlots;
             if (g_issue >= kSlots) ok = tc::mbar_wait(&empty[slot], (uint32_t)((g_issue / kSlots - 1) & 1));
             if (!ok) break;
             const int li = g_issue - g_base;
-            const int ti = t0 + li / kSlices, tu = li % kSlices;
+            const int ti = t0 + li / kUnits, tuh = li % kUnits;
             tc::mbar_expect_tx(&full[slot], kBImg);
-            tc::bulk_g2s(ring + (size_t)slot * kBImg, a.green_img + ((size_t)ti * kSlices + tu) * (kBImg / 2), kBImg,
+            tc::bulk_g2s(ring + (size_t)slot * kBImg, a.green_img + ((size_t)ti * kUnits + tuh) * (kBImg / 2), kBImg,
                          &full[slot]);
             ++g_issue;
           }
           if (!ok) break;
-          const int tgi = tg + i, abuf = tgi & 1;
-          if (u == 0) {
+          const int tgi = tg + i;
+          if (uh == 0) {
             if (i == 0) ok = tc::mbar_wait(a_full, (uint32_t)(kitem & 1));
-            if (ok && tgi >= 2) ok = tc::mbar_wait(&acc_empty[abuf], (uint32_t)(((tgi - 2) / 2) & 1));
+            // one accumulator buffer: the epilogue copies a tile out of TMEM before the next one starts
+            if (ok && tgi >= 1) ok = tc::mbar_wait(acc_empty, (uint32_t)((tgi - 1) & 1));
             if (!ok) break;
           }
           const int gs = g_base + sidx, slot = gs % kSlots;
@@ -457,19 +469,19 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
           tc::fence_after_sync();
           // slice u of the Green's function meets the rot_chol slices t <= 4 - u; products with
           // t + u = d accumulate into group d.  Descriptors advance by constants.
-          const uint32_t blo = (uint32_t)tc::smem_desc(ring_u + (uint32_t)(slot * kBImg), 128, kKP * 16);
-          const uint32_t dcol = taddr + (uint32_t)(abuf * kGroups * kBN + u * kBN);
+          const uint32_t blo = (uint32_t)bd0 + (uint32_t)(slot * kBImg / 16);
+          const uint32_t dcol = taddr + (uint32_t)(u * kBN);
           const int tmax = (kGroups - 1) - u;
           for (int t = 0; t <= tmax; ++t) {
-            const uint32_t alo = adlo + (uint32_t)(t * (128 * kKP * 2 / 16));
+            const uint32_t alo = adlo + (uint32_t)((t * 128 * kKP * 2 + h * kKH * 16) / 16);
             const uint32_t dt = dcol + (uint32_t)(t * kBN);
 #pragma unroll
-            for (int ks = 0; ks < kKP / 16; ++ks)
-              tc::mma_bf16_lo(dt, alo + (uint32_t)(ks * 16), blo + (uint32_t)(ks * 16), dhi, idesc,
-                              (u == 0 && ks == 0) ? 0u : 1u);
+            for (int ks = 0; ks < kKH / 16; ++ks)
+              tc::mma_bf16_lo2(dt, alo + (uint32_t)(ks * 16), ahi, blo + (uint32_t)(ks * 16), bhi, idesc,
+                               (u == 0 && h == 0 && ks == 0) ? 0u : 1u);
           }
           tc::mma_commit(&empty[slot]);
-          if (u == kSlices - 1) tc::mma_commit(&acc_full[abuf]);
+          if (uh == kUnits - 1) tc::mma_commit(acc_full);
         }
         if (ok) tc::mma_commit(a_free);
         g_base += total;
@@ -490,7 +502,7 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
     const int j0 = h * JH;
     const int etid = tid;  // 0..511
     bool stop = false;
-    int tgl = 0;  // CTA-wide tile counter (TMEM buffer and phase)
+    int tgl = 0;  // CTA-wide tile counter (accumulator phase)
     for (int item = blockIdx.x; item < a.n_items && !stop; item += gridDim.x) {
     const int blk = item / a.chunks;
     const int t0 = (item % a.chunks) * a.tiles_per_item, t1 = min(L.ntiles, t0 + a.tiles_per_item);
@@ -499,8 +511,8 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
     const bool rvalid = r < rows_valid;
     const int ea = a.rot_e[(size_t)blk * 128 + r];
     for (int it = 0; it < ntl; ++it, ++tgl) {
-      const int tile = t0 + it, abuf = tgl & 1;
-      if (etid == 0) *flag = tc::mbar_wait(&acc_full[abuf], (uint32_t)((tgl / 2) & 1)) ? 1 : 0;
+      const int tile = t0 + it;
+      if (etid == 0) *flag = tc::mbar_wait(acc_full, (uint32_t)(tgl & 1)) ? 1 : 0;
       tc::named_bar(1, kExEpi);
       if (!*flag) {
         if (etid == 0) atomicExch(a.status, (int)TROT_ERR_DEVICE_TIMEOUT);
@@ -508,52 +520,57 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
         break;
       }
       tc::fence_after_sync();
-      const uint32_t tlane = taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(abuf * kGroups * kBN);
+      const uint32_t tlane = taddr + ((uint32_t)(q * 32) << 16);
       const int32_t* eB = a.green_e + (size_t)tile * kBN;
-      for (int bl = 0; bl < L.WB; ++bl) {
-        const int b = tile * L.WB + bl;
-        if (b >= a.W) break;  // uniform across the epilogue warps
-        // f values for my row and my j-half: re (column bl*S + j), im (column bl*S + n_pad + j)
-        ff fre[JH], fim[JH];
-        {
-          uint32_t raw[2][kGroups][JH];
+      // copy every walker's f values of my row / column quarter out of TMEM, then release it
+      ff fre[WBT][JH], fim[WBT][JH];
 #pragma unroll
-          for (int c = 0; c < 2; ++c)
+      for (int bl = 0; bl < WBT; ++bl) {
+        uint32_t raw[2][kGroups][JH];
 #pragma unroll
-            for (int d = 0; d < kGroups; ++d)
+        for (int c = 0; c < 2; ++c)
 #pragma unroll
-              for (int jj = 0; jj < JH; ++jj)
-                raw[c][d][jj] = tc::tmem_ld1(tlane + (uint32_t)(d * kBN + bl * L.S + c * L.n_pad + j0 + jj));
-          tc::tmem_wait_ld();
+          for (int d = 0; d < kGroups; ++d)
 #pragma unroll
-          for (int c = 0; c < 2; ++c)
+            for (int jj = 0; jj < JH; ++jj)
+              raw[c][d][jj] = tc::tmem_ld1(tlane + (uint32_t)(d * kBN + bl * L.S + c * L.n_pad + j0 + jj));
+        tc::tmem_wait_ld();
 #pragma unroll
-            for (int jj = 0; jj < JH; ++jj) {
-              float g[kGroups];
+        for (int c = 0; c < 2; ++c)
 #pragma unroll
-              for (int d = 0; d < kGroups; ++d) {
-                uint32_t v = raw[c][d][jj];
-                asm volatile("" : "+r"(v));  // consume after tcgen05.wait::ld
-                g[d] = __uint_as_float(v);
-              }
-              ff x = ff_two_sum(g[0], g[1] * 0.00390625f);
-              float lo = x.lo + g[2] * 1.52587890625e-05f;
-              lo += g[3] * 5.9604644775390625e-08f;
-              lo += g[4] * 2.3283064365386963e-10f;
-              x = ff_fast(x.hi, lo);
-              const float sc = pow2f(ea + eB[bl * L.S + c * L.n_pad + j0 + jj] - 16);
-              const ff y{x.hi * sc, x.lo * sc};
-              if (c == 0) fre[jj] = y; else fim[jj] = y;
+          for (int jj = 0; jj < JH; ++jj) {
+            float g[kGroups];
+#pragma unroll
+            for (int d = 0; d < kGroups; ++d) {
+              uint32_t v = raw[c][d][jj];
+              asm volatile("" : "+r"(v));  // consume after tcgen05.wait::ld
+              g[d] = __uint_as_float(v);
             }
-        }
+            ff x = ff_two_sum(g[0], g[1] * 0.00390625f);
+            float lo = x.lo + g[2] * 1.52587890625e-05f;
+            lo += g[3] * 5.9604644775390625e-08f;
+            lo += g[4] * 2.3283064365386963e-10f;
+            x = ff_fast(x.hi, lo);
+            const float sc = pow2f(ea + eB[bl * L.S + c * L.n_pad + j0 + jj] - 16);
+            const ff y{x.hi * sc, x.lo * sc};
+            if (c == 0) fre[bl][jj] = y; else fim[bl][jj] = y;
+          }
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(acc_empty);
+#pragma unroll
+      for (int bl = 0; bl < WBT; ++bl) {
+        const int b = tile * WBT + bl;
+        if (b >= a.W) break;  // uniform across the epilogue warps
         // exchange sum_j f_ij f_ji: stage re and im of this row's f values, one barrier
         const int brow = gl * L.n;
         ff* sFr = sF;
         ff* sFi = sF + 128 * kFS;
 #pragma unroll
         for (int jj = 0; jj < JH; ++jj) {
-          sFr[r * kFS + j0 + jj] = fre[jj];
-          sFi[r * kFS + j0 + jj] = fim[jj];
+          sFr[r * kFS + j0 + jj] = fre[bl][jj];
+          sFi[r * kFS + j0 + jj] = fim[bl][jj];
         }
         tc::named_bar(1, kExEpi);
         ff xr{0.f, 0.f}, xi{0.f, 0.f};
@@ -565,10 +582,10 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
             if (j0 + jj >= L.n) break;
             const ff orr = sFr[(brow + j0 + jj) * kFS + i], oi = sFi[(brow + j0 + jj) * kFS + i];
             // (a + ib)(c + id) = (ac - bd) + i(ad + bc)
-            ff_mad(xr, fre[jj], orr);
-            ff_mad(xr, ff{-fim[jj].hi, -fim[jj].lo}, oi);
-            ff_mad(xi, fre[jj], oi);
-            ff_mad(xi, fim[jj], orr);
+            ff_mad(xr, fre[bl][jj], orr);
+            ff_mad(xr, ff{-fim[bl][jj].hi, -fim[bl][jj].lo}, oi);
+            ff_mad(xi, fre[bl][jj], oi);
+            ff_mad(xi, fim[bl][jj], orr);
           }
           if (h == 0) {  // f_ii of this row for the trace (force bias)
             sC[2 * r] = sFr[r * kFS + i];
@@ -613,10 +630,6 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
           if (ii == 0 && gv < L.gb && g < a.G) a.cs[(size_t)b * a.G + g] = make_double2(ff_d(tr), ff_d(ti));
         }
       }
-      // this accumulator buffer is free again
-      tc::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&acc_empty[abuf]);
     }
     }
   }
@@ -984,7 +997,7 @@ __device__ __forceinline__ void put_b(unsigned char* B, int j, int k, float x) {
 }
 
 template <int NBT, int WPC>
-__global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, TrotTcArgs g) {
+__global__ void __maxnreg__(224) trotter_tc_kernel(Spins sp, TrotTcArgs g) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bars[4 + 2 * WPC];
   __shared__ uint32_t tslot;
@@ -1122,8 +1135,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, Tro
         tc::fence_after_sync();
         float d[2 * NH];
         const uint32_t tl = taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(wi * 64 + h * 2 * NH);
+        {  // all column groups in flight, one wait
+          uint32_t raw[2 * NH];
 #pragma unroll
-        for (int c = 0; c < 2 * NH; c += 8) tc::tmem_ld8(tl + c, d + c);
+          for (int c = 0; c < 2 * NH; c += 8) tc::tmem_ld8_raw(tl + c, raw + c);
+          tc::tmem_wait_ld();
+#pragma unroll
+          for (int c = 0; c < 2 * NH; ++c) {
+            uint32_t v = raw[c];
+            asm volatile("" : "+r"(v));  // consume after tcgen05.wait::ld
+            d[c] = __uint_as_float(v);
+          }
+        }
         const int b = b0 + wi;
         if (step == nsteps - 1) {  // w' = E O
 #pragma unroll
@@ -1212,7 +1235,7 @@ __global__ void tc_weight_kernel(TrotterArgs a, const double2* __restrict__ ov_n
 // det by FP64 Gauss-Jordan, overlap = prod_s det(M_s)^mult_s, then phaseless_update.
 // One CTA per walker.
 __global__ void __launch_bounds__(256) overlap_weight_ff_kernel(Spins sp, TrotterArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ double2 red[32];
   __shared__ int piv;
   const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
@@ -1323,7 +1346,7 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
     a.G = G; a.W = W; a.mult = sp.mult[q];
     // persistent grid: one CTA per SM walks (Cholesky block, 16 walker tiles) items
     const int tpi = tune_get(TROT_TUNE_EXCHANGE_TILES);
-    a.tiles_per_item = std::min(tpi > 0 ? tpi : 16, L.ntiles);
+    a.tiles_per_item = std::min(tpi > 0 ? tpi : 8, L.ntiles);
     a.chunks = (L.ntiles + a.tiles_per_item - 1) / a.tiles_per_item;
     a.n_items = L.nblk * a.chunks;
     a.rot_img = s->mixed->rot_slices[mq];

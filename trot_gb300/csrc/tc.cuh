@@ -77,6 +77,16 @@ __device__ __forceinline__ void mma_bf16_first(uint32_t d_tmem, uint64_t adesc, 
 // the start-address field is the low 14 bits in 16-byte units.
 __device__ __forceinline__ uint64_t desc_add(uint64_t desc, uint32_t bytes) { return desc + (uint64_t)(bytes >> 4); }
 
+// MMA from the low words of the A and B descriptors and their (fixed) high words.
+__device__ __forceinline__ void mma_bf16_lo2(uint32_t d_tmem, uint32_t alo, uint32_t ahi, uint32_t blo, uint32_t bhi,
+                                             uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .b64 ad, bd;\n.reg .pred p;\nmov.b64 ad, {%1, %2};\nmov.b64 bd, {%3, %4};\n"
+      "setp.ne.b32 p, %6, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], ad, bd, %5, p;\n}\n" ::"r"(d_tmem),
+      "r"(alo), "r"(ahi), "r"(blo), "r"(bhi), "r"(idesc), "r"(accumulate));
+}
+
 // MMA from the low words of two descriptors that share their high word (same SBO,
 // version bits): the issuing thread advances 32-bit values only.
 __device__ __forceinline__ void mma_bf16_lo(uint32_t d_tmem, uint32_t alo, uint32_t blo, uint32_t hi, uint32_t idesc,
@@ -177,6 +187,14 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
   asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 8 consecutive columns without the wait (pair with tmem_wait_ld(); consume the
+// registers only after it).
+__device__ __forceinline__ void tmem_ld8_raw(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
 }
 
 // Byte offset of element (row r, k) inside a [rows x 32] K-major tile (8-row
