@@ -997,7 +997,7 @@ __device__ __forceinline__ void put_b(unsigned char* B, int j, int k, float x) {
 }
 
 template <int NBT, int WPC>
-__global__ void __maxnreg__(224) trotter_tc_kernel(Spins sp, TrotTcArgs g) {
+__global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, TrotTcArgs g) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bars[4 + 2 * WPC];
   __shared__ uint32_t tslot;
@@ -1109,7 +1109,7 @@ __global__ void __maxnreg__(224) trotter_tc_kernel(Spins sp, TrotTcArgs g) {
       for (int jj = 0; jj < NH; ++jj) {
         const int j = jbase + jj;
         if (j < nc) {
-          const int s = j < sp.n[0] ? 0 : 1, n = sp.n[s], col = j - sp.off[s];
+          const int s = j < sp.n[0] ? 0 : 1, n = s ? sp.n[1] : sp.n[0], col = s ? j - sp.off[1] : j;
           const double2* w = (s == 0 ? a.in_a : a.in_b) + (size_t)b * N * n;
           const double2 x = prow ? w[(size_t)p * n + col] : make_double2(0.0, 0.0);
           put_b<NB>(B, 2 * j, p, (float)x.x);
@@ -1153,7 +1153,7 @@ __global__ void __maxnreg__(224) trotter_tc_kernel(Spins sp, TrotTcArgs g) {
           for (int jj = 0; jj < NH; ++jj) {
             const int j = jbase + jj;
             if (j < nc && prow) {
-              const int s = j < sp.n[0] ? 0 : 1, n = sp.n[s], col = j - sp.off[s];
+              const int s = j < sp.n[0] ? 0 : 1, n = s ? sp.n[1] : sp.n[0], col = s ? j - sp.off[1] : j;
               (s == 0 ? a.out_a : a.out_b)[((size_t)b * N + p) * n + col] =
                   make_double2((double)d[2 * jj], (double)d[2 * jj + 1]);
             }
