@@ -335,6 +335,83 @@ size_t trot_fp_workspace_size(const trot_system* sys);
 int trot_fp_step(const trot_system* sys, const trot_state* state, const double* fields, const double* zeta_dev,
                  void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------------------------------- one-time constants on the device
+ * Propagation context (replaces the host precompute _build_restricted_prop_ctx_from_host,
+ * trot/runtime_layout.py:125-197, and _build_prop_ctx, trot/prop/chol_afqmc_ops.py:103-127):
+ * from h1 (norb, norb), chol (nchol, norb, norb) and the spin-summed trial 1-RDM rdm1
+ * (norb, norb), all float64 on the device, writes
+ *   mf_im[g]    = tr(L_g rdm1)           (mf_shifts = i mf_im, nchol doubles)
+ *   *h0_prop    = -h0 + 1/2 sum_g mf_im[g]^2
+ *   exp_h1_half = expm(-dt/2 (h1 - 1/2 sum_g L_g L_g + sum_g mf_im[g] L_g))   (norb, norb)
+ * Workspace: trot_prop_ctx_workspace_size(norb, nchol) bytes; after the stream
+ * reaches the end of the call, trot_workspace_status(workspace) is
+ * TROT_ERR_NUMERIC_GUARD when h1_eff had a non-finite entry or
+ * dt/2 ||h1_eff||_1 > 2^39 (outputs undefined then), else TROT_OK. */
+size_t trot_prop_ctx_workspace_size(int norb, int nchol);
+int trot_build_prop_ctx(int norb, int nchol, double h0, double dt, const double* h1, const double* chol,
+                        const double* rdm1, double* mf_im, double* h0_prop, double* exp_h1_half,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* Half rotation with a real trial (replaces _build_rhf_meas_ctx_from_host,
+ * trot/runtime_layout.py:200-245, and build_meas_ctx, trot/meas/rhf.py:308-319,
+ * trot/meas/uhf.py:318-336): rot_h1 = mo^T h1 (nocc, norb) and rot_chol[g] =
+ * mo^T L_g (nchol, nocc, norb) for mo (norb, nocc) row-major.  Either h1 or chol
+ * may be null (its output is then not written). */
+int trot_half_rotate(int norb, int nchol, int nocc, const double* mo, const double* h1, const double* chol,
+                     double* rot_h1, double* rot_chol, void* stream);
+
+/* CISD lci1 (replaces the loop of _build_cisd_meas_ctx_from_host,
+ * trot/runtime_layout.py:248-292; trot/meas/cisd.py:92-110):
+ * lci1[g][i][p] = sum_t chol[g][i][nocc + t] ci1[p][t], ci1 (nocc, norb - nocc),
+ * lci1 (nchol, norb, nocc). */
+int trot_cisd_lci1(int norb, int nchol, int nocc, const double* ci1, const double* chol, double* lci1,
+                   void* stream);
+
+/* ---------------------------------------------------------------- adjoint (reverse mode)
+ * Hand-written vector-Jacobian products for an RHF trial with restricted
+ * walkers (TROT_RHF_R) in FP64; other kinds return TROT_ERR_UNSUPPORTED.  The
+ * reference has no adjoint: these differentiate its forward formulas
+ * (trot/prop/afqmc.py:91-144, trot/meas/rhf.py:21-60,128-138,
+ * trot/trial/rhf.py:45-47, trot/walkers.py:137-179) so that gradients of an
+ * energy estimator with respect to h1 come out of one run.  Cotangents of a
+ * real objective J: g_z = dJ/dRe z + i dJ/dIm z for complex z (complex128
+ * arrays), dJ/dz for real z.  Workspace: trot_vjp_workspace_size(sys, op)
+ * with op TROT_OP_PROP_STEP, TROT_OP_LOCAL_ENERGY or TROT_OP_OVERLAP.
+ *
+ * trot_prop_step_vjp: given the state BEFORE the step (in), the step's fields
+ * and the cotangents of the state after it (walkers, weights (may be NULL),
+ * overlaps (may be NULL), scalars [E_shift, e_estimate]), writes the
+ * cotangents of the state before it and adds dJ/d exp_h1_half (N x N) into
+ * g_exp_h1_half.  The forward step is recomputed inside; weights that the
+ * step's floor / cap / non-finite guards set to zero pass no gradient.
+ * trot_local_energy_vjp: adds g_energy[b] * d Re E_L[b] / d walkers into
+ * g_walkers and sum_b g_energy[b] d Re E_L[b] / d h1 (through rot_h1 = C^T h1)
+ * into g_h1 (N x N).
+ * trot_overlap_vjp: adds the cotangent of det(C^T w)^2 into g_walkers.
+ * trot_orthonormalize_vjp: g_walkers = g_q (w^H q)^-1 for q the orthonormalised
+ * walkers (everything downstream is invariant under q -> q M). */
+size_t trot_vjp_workspace_size(const trot_system* sys, int op);
+int trot_prop_step_vjp(const trot_system* sys, const trot_state* state_in, const double* fields,
+                       const double* g_walkers_out, const double* g_weights_out, const double* g_overlaps_out,
+                       const double* g_scalars_out, double* g_walkers_in, double* g_weights_in,
+                       double* g_overlaps_in, double* g_scalars_in, double* g_exp_h1_half, void* workspace,
+                       size_t workspace_bytes, void* stream);
+int trot_local_energy_vjp(const trot_system* sys, const double* walkers, const double* g_energy,
+                          double* g_walkers, double* g_h1, void* workspace, size_t workspace_bytes, void* stream);
+int trot_overlap_vjp(const trot_system* sys, const double* walkers, const double* g_overlaps, double* g_walkers,
+                     void* workspace, size_t workspace_bytes, void* stream);
+int trot_orthonormalize_vjp(const trot_system* sys, const double* walkers, const double* walkers_q,
+                            const double* g_q, double* g_walkers, void* stream);
+
+/* Adjoint of the propagation context's exp(-dt/2 h1_eff) with respect to h1:
+ * adds the Frechet-derivative adjoint of expm applied to g_exp_h1_half, times
+ * -dt/2, into g_h1 (N x N); same inputs as trot_build_prop_ctx.  Workspace:
+ * trot_prop_ctx_vjp_workspace_size(norb, nchol). */
+size_t trot_prop_ctx_vjp_workspace_size(int norb, int nchol);
+int trot_prop_ctx_vjp(int norb, int nchol, double dt, const double* h1, const double* chol, const double* rdm1,
+                      const double* g_exp_h1_half, double* g_h1, void* workspace, size_t workspace_bytes,
+                      void* stream);
+
 /* Plain BF16 tensor-core GEMM (tcgen05, accumulator in tensor memory):
  * D (M x N, float32) = A (M x K, bf16) * B (N x K, bf16)^T, all row-major,
  * M and N multiples of 128, K a multiple of 64, A and B 16-byte aligned.

@@ -110,6 +110,13 @@ def force_bias(w, tr: CisdTrial, chol):
     return fb / ov[:, None]
 
 
+
+def meas_lci1(chol, ci1, vir):
+    """lci1[g][i][p] = sum_t chol[g][i][vir_t] ci1[p][t] (trot/runtime_layout.py:272-281;
+    trot/meas/cisd.py:92-110), (G, N, nocc)."""
+    return np.einsum("git,pt->gip", np.asarray(chol)[:, :, vir], ci1, optimize=True)
+
+
 def energy(w, tr: CisdTrial, h0, h1, chol):
     """``energy_kernel_rw_rh`` (trot/meas/cisd.py:608-769), "high" mode, float64."""
     ci1, ci2 = tr.ci1, tr.ci2
@@ -143,7 +150,7 @@ def energy(w, tr: CisdTrial, h0, h1, chol):
     e2_1_2 = -2.0 * np.sum(lci1g * lg, axis=1)
     ci1g1 = np.einsum("pt,bqt->bpq", ci1, g[:, :, tr.vir])  # (W, nocc_act, nocc_full)
     e2_1_3_1 = np.einsum("bgpq,bgqa,bap->b", lg1, lg1[:, :, :, tr.occ], ci1g1, optimize=True)
-    lci1 = np.einsum("git,pt->gip", chol[:, :, tr.vir], ci1, optimize=True)  # meas ctx lci1 (G, N, n_act)
+    lci1 = meas_lci1(chol, ci1, tr.vir)  # meas ctx lci1 (G, N, n_act)
     lci1g_mat = np.einsum("gia,bqi->bgaq", lci1, g, optimize=True)
     e2_1_3_2 = -np.einsum("bgaq,bgqa->b", lci1g_mat, lg1[:, :, :, tr.occ], optimize=True)
     e2_1 = e2_1_1 + 2.0 * (e2_1_2 + e2_1_3_1 + e2_1_3_2)

@@ -149,3 +149,24 @@ def test_tuning_knobs():
     assert b"unknown tuning knob" in lib.trot_last_error()
     assert lib.trot_set_tuning(_lib.TUNE_EXCHANGE_GRID, -3) == 1
     assert lib.trot_get_tuning(99) == 0
+
+
+def test_ctx_builders_errors():
+    """One-time context builders: size query, and argument errors before any launch."""
+    lib = _lib.load()
+    n1 = lib.trot_prop_ctx_workspace_size(24, 120)
+    n2 = lib.trot_prop_ctx_workspace_size(120, 600)
+    assert 0 < n1 < n2
+    assert lib.trot_prop_ctx_workspace_size(0, 10) == 0
+    p = 0x1000
+    d = ctypes.c_double
+    assert lib.trot_build_prop_ctx(24, 120, d(0.0), d(0.01), p, p, p, p, p, p, None, n1, None) == 3
+    assert lib.trot_build_prop_ctx(24, 0, d(0.0), d(0.01), p, p, p, p, p, p, p, n1, None) == 1
+    assert lib.trot_build_prop_ctx(24, 120, d(0.0), d(-1.0), p, p, p, p, p, p, p, n1, None) == 1
+    assert lib.trot_build_prop_ctx(24, 120, d(0.0), d(0.01), p, p, p, p, p, p, p, n1 - 4096, None) == 4
+    assert lib.trot_half_rotate(24, 10, 0, p, p, p, p, p, None) == 1
+    assert lib.trot_half_rotate(24, 10, 25, p, p, p, p, p, None) == 1
+    assert lib.trot_half_rotate(24, 10, 5, None, p, p, p, p, None) == 3
+    assert lib.trot_half_rotate(24, 10, 5, p, p, p, None, p, None) == 3
+    assert lib.trot_cisd_lci1(24, 10, 24, p, p, p, None) == 1
+    assert lib.trot_cisd_lci1(24, 10, 5, p, None, p, None) == 3

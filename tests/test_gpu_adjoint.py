@@ -1,0 +1,177 @@
+"""Hand-written adjoint (trot_*_vjp) vs torch autograd of the twin restatement
+(oracle/afqmc_torch_twin.py, the gradient oracle) and vs central finite
+differences of the CUDA forward with common random numbers.
+
+Tolerances: vector-Jacobian products of single operators 1e-9 relative
+(max-norm); whole-run gradient 1e-8 relative to the twin's autograd and 1e-6
+relative to finite differences (lambda = +-1e-4)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import afqmc_torch_twin as twin
+from tests.gpu_helpers import rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _problem(N=12, n=3, G=20, W=6, T=8, spb=4, dt=0.01, noise=0.05, seed=4):
+    import trot_gb300 as tg
+    from trot_gb300 import adjoint, synthetic
+
+    ss = synthetic.make_system(N, (n, n), G, decay=30.0, seed=seed, h0=0.3)
+    rng = np.random.default_rng(seed + 1)
+    fields = rng.standard_normal((T, W, G))
+    w0 = synthetic.perturbed_walkers(ss.mo_a, W, noise, seed + 2)
+    params = tg.QmcParams(dt=dt, n_exp_terms=6, n_prop_steps=spb, n_walkers=W)
+    prob = adjoint.as_problem(ss.h0, ss.chol, tg.RhfTrial(ss.mo_a), params, torch.as_tensor(fields).cuda(),
+                              walkers0=torch.as_tensor(w0).cuda(), e_estimate0=-2.0, steps_per_block=spb)
+    return ss, fields, w0, prob
+
+
+def _c(x):
+    return torch.as_tensor(np.asarray(x))
+
+
+def _rand_like(x, seed):
+    g = torch.Generator().manual_seed(seed)
+    if x.is_complex():
+        return torch.complex(torch.randn(x.shape, generator=g, dtype=torch.float64),
+                             torch.randn(x.shape, generator=g, dtype=torch.float64))
+    return torch.randn(x.shape, generator=g, dtype=torch.float64)
+
+
+def test_prop_ctx_vjp():
+    from trot_gb300 import adjoint
+
+    ss, _, _, prob = _problem()
+    h1 = torch.as_tensor(ss.h1).cuda().requires_grad_(True)
+    eh = adjoint.ExpH1Half.apply(h1, prob)
+    g = _rand_like(eh.detach().cpu(), 1)
+    (gh1,) = torch.autograd.grad(eh, h1, g.cuda())
+    h1c = _c(ss.h1).clone().requires_grad_(True)
+    _, _, ehc = twin.prop_consts(ss.h0, h1c, _c(ss.chol), prob.rdm1.cpu(), prob.params.dt)
+    assert rel(eh.detach().cpu().numpy(), ehc.detach().numpy()) < 1e-12
+    (ref,) = torch.autograd.grad(ehc, h1c, g)
+    assert rel(gh1.cpu().numpy(), ref.numpy()) < 1e-9
+
+
+def test_step_vjp():
+    from trot_gb300 import adjoint
+
+    ss, fields, w0, prob = _problem()
+    W = w0.shape[0]
+    dev = lambda x: x.cuda().requires_grad_(True)
+    w = dev(_c(w0))
+    wt = dev(torch.linspace(0.5, 1.5, W, dtype=torch.float64))
+    ov = dev(twin.overlap(_c(w0), _c(ss.mo_a)).detach())
+    scal = dev(torch.tensor([-1.7, -2.1], dtype=torch.float64))
+    h1 = torch.as_tensor(ss.h1).cuda()
+    eh = dev(adjoint.ExpH1Half.apply(h1, prob).detach())
+    x = torch.as_tensor(fields[0]).cuda()
+    outs = adjoint.Step.apply(w, wt, ov, scal, eh, x, prob)
+    gs = [_rand_like(o.detach().cpu(), 10 + i) for i, o in enumerate(outs)]
+    grads = torch.autograd.grad(outs, (w, wt, ov, scal, eh), [g.cuda() for g in gs])
+
+    cw, cwt, cov = _c(w0).requires_grad_(True), wt.detach().cpu().requires_grad_(True), ov.detach().cpu().requires_grad_(True)
+    ces = torch.tensor(-1.7, dtype=torch.float64, requires_grad=True)
+    cee = torch.tensor(-2.1, dtype=torch.float64, requires_grad=True)
+    ceh = eh.detach().cpu().requires_grad_(True)
+    rot_chol = torch.einsum("pi,gpj->gij", _c(ss.mo_a), _c(ss.chol))
+    p = prob.params
+    wn, wtn, ovn, esn = twin.step(cw, cwt, cov, ces, cee, _c(fields[0]), mo=_c(ss.mo_a), rot_chol=rot_chol,
+                                  chol=_c(ss.chol), mf_im=prob.mf_im.cpu(), h0_prop=prob.h0_prop, eh=ceh, dt=p.dt,
+                                  n_terms=6)
+    # forward parity of the library step and the twin
+    assert rel(outs[0].detach().cpu().numpy(), wn.detach().numpy()) < 1e-12
+    assert rel(outs[1].detach().cpu().numpy(), wtn.detach().numpy()) < 1e-12
+    scal_n = torch.stack([esn, cee])
+    loss = sum(torch.sum((g.conj() * o).real) if o.is_complex() else torch.sum(g * o)
+               for g, o in zip(gs, (wn, wtn, ovn, scal_n)))
+    ref = torch.autograd.grad(loss, (cw, cwt, cov, ces, cee, ceh))
+    assert rel(grads[0].cpu().numpy(), ref[0].numpy()) < 1e-9
+    assert rel(grads[1].cpu().numpy(), ref[1].numpy()) < 1e-9
+    assert rel(grads[2].cpu().numpy(), ref[2].numpy()) < 1e-9
+    assert rel(grads[3].cpu().numpy(), np.array([ref[3].item(), ref[4].item()])) < 1e-9
+    assert rel(grads[4].cpu().numpy(), ref[5].numpy()) < 1e-9
+
+
+def test_local_energy_overlap_qr_vjp():
+    from trot_gb300 import adjoint
+
+    ss, _, w0, prob = _problem(N=14, n=4, G=24, W=5)
+    w = torch.as_tensor(w0).cuda().requires_grad_(True)
+    h1 = torch.as_tensor(ss.h1).cuda().requires_grad_(True)
+    e = adjoint.LocalEnergy.apply(w, h1, prob)
+    ov = adjoint.Overlap.apply(w, prob)
+    ge = _rand_like(e.detach().cpu(), 3)
+    gov = _rand_like(ov.detach().cpu(), 4)
+    gw, gh1 = torch.autograd.grad((e, ov), (w, h1), (ge.cuda(), gov.cuda()))
+    cw = _c(w0).requires_grad_(True)
+    ch1 = _c(ss.h1).requires_grad_(True)
+    rot_chol = torch.einsum("pi,gpj->gij", _c(ss.mo_a), _c(ss.chol))
+    ce = twin.local_energy(cw, _c(ss.mo_a), ss.h0, _c(ss.mo_a).T @ ch1, rot_chol).real
+    cov = twin.overlap(cw, _c(ss.mo_a))
+    assert rel(e.detach().cpu().numpy(), ce.detach().numpy()) < 1e-12
+    loss = torch.sum(ge * ce) + torch.sum((gov.conj() * cov).real)
+    rw, rh1 = torch.autograd.grad(loss, (cw, ch1))
+    assert rel(gw.cpu().numpy(), rw.numpy()) < 1e-9
+    assert rel(gh1.cpu().numpy(), rh1.numpy()) < 1e-9
+    # QR: the energy is invariant under w -> w R, so E(qr(w)) has the gradient of E(w)
+    w2 = torch.as_tensor(w0).cuda().requires_grad_(True)
+    e2 = adjoint.LocalEnergy.apply(adjoint.Orthonormalize.apply(w2, prob), h1.detach(), prob)
+    (gq,) = torch.autograd.grad(e2, w2, ge.cuda())
+    w3 = torch.as_tensor(w0).cuda().requires_grad_(True)
+    e3 = adjoint.LocalEnergy.apply(w3, h1.detach(), prob)
+    (gd,) = torch.autograd.grad(e3, w3, ge.cuda())
+    assert rel(gq.cpu().numpy(), gd.cpu().numpy()) < 1e-9
+
+
+@pytest.mark.parametrize("spb,T", [(4, 8), (3, 9)])
+def test_mixed_energy_gradient(spb, T):
+    """Whole run (steps, QR, overlaps, energies, clamps, e_estimate updates, checkpointed blocks)."""
+    from trot_gb300 import adjoint
+
+    ss, fields, w0, prob = _problem(T=T, spb=spb)
+    J, g = adjoint.energy_and_grad(ss.h1, prob)
+    kw = dict(h0=ss.h0, chol=_c(ss.chol), mo=_c(ss.mo_a), rdm1=prob.rdm1.cpu(), fields=_c(fields),
+              walkers0=_c(w0), e_estimate0=-2.0, steps_per_block=spb, dt=prob.params.dt, n_terms=6)
+    h1c = _c(ss.h1).clone().requires_grad_(True)
+    Jc = twin.mixed_energy(h1c, **kw)
+    (gc,) = torch.autograd.grad(Jc, h1c)
+    assert abs(float(J) - float(Jc.detach())) <= 1e-11 * abs(float(Jc.detach()))
+    assert rel(g.cpu().numpy(), gc.numpy()) < 1e-8
+    # finite differences of the CUDA forward along a symmetric one-body perturbation O
+    O = np.random.default_rng(9).normal(scale=0.1, size=ss.h1.shape)
+    O = 0.5 * (O + O.T)
+    eps = 1e-4
+    fd = (adjoint.energy(ss.h1 + eps * O, prob) - adjoint.energy(ss.h1 - eps * O, prob)) / (2 * eps)
+    ad = float(torch.sum(g.cpu() * _c(O)))
+    assert abs(ad - fd) <= 1e-6 * abs(fd), (ad, fd)
+
+
+def test_checkpointing_is_exact():
+    from trot_gb300 import adjoint
+
+    ss, _, _, prob = _problem()
+    _, g1 = adjoint.energy_and_grad(ss.h1, prob, checkpoint_blocks=True)
+    _, g2 = adjoint.energy_and_grad(ss.h1, prob, checkpoint_blocks=False)
+    assert torch.equal(g1, g2)
+
+
+def test_adjoint_rejects_other_kinds():
+    import ctypes
+
+    from trot_gb300 import _lib
+
+    _, _, _, prob = _problem()
+    s = prob.system()
+    s.kind = _lib.UHF_U
+    assert _lib.load().trot_vjp_workspace_size(ctypes.byref(s), _lib.OP_PROP_STEP) == 0
+    assert b"restricted" in _lib.load().trot_last_error()

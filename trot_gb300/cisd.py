@@ -23,6 +23,7 @@ import numpy as np
 import torch
 
 from . import _lib, native, rng
+from . import ctx as ctx_dev
 from .core import (HamChol, MeasOps, PropState, System, TrialOps, as_dev, batched, k_energy, k_force_bias,
                    o_rdm1, real_part)
 
@@ -136,12 +137,12 @@ def build_meas_ctx(ham_data: HamChol, trial_data: CisdTrial, cfg: CisdMeasCfg = 
     """trot/meas/cisd.py:92-110: lci1[g][i][p] = sum_a chol[g][i][nocc + a] ci1[p][a]."""
     if ham_data.basis != "restricted":
         raise ValueError("CISD MeasOps currently assumes HamChol.basis == 'restricted'.")
-    h1 = as_dev(real_part(ham_data.h1, "h1"))
-    chol = as_dev(real_part(ham_data.chol, "chol"))
+    h1 = ctx_dev.real_dev(ham_data.h1, "h1")
+    chol = ctx_dev.real_dev(ham_data.chol, "chol")
     if chol.shape[1] != trial_data.norb:
         raise ValueError(f"chol norb {chol.shape[1]} != trial norb {trial_data.norb}")
     n = trial_data.nocc_full
-    lci1 = torch.einsum("git,pt->gip", chol[:, :, trial_data.vir_act_slice], trial_data.ci1).contiguous()
+    lci1 = ctx_dev.cisd_lci1(trial_data.ci1, chol)  # whole orbital space active: vir_act_slice = nocc..N
     h0 = ham_data.h0.item() if isinstance(ham_data.h0, torch.Tensor) else ham_data.h0
     img, ncpad, nvpad = None, 0, 0
     if not cfg.testing:

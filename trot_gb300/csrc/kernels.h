@@ -80,4 +80,7 @@ int launch_sr(const Spins& sp, int W, int N, const double* weights, const double
               const double2* inb, double2* outa, double2* outb, double* weights_out, long long* idx,
               double* cw, cudaStream_t st);
 
+// ctx.cu: out = expm(A) (real n x n, device); status[0] guard, status[1] squarings; p0, p1 n x n scratch
+int launch_expm(int n, const double* A, double* out, double* p0, double* p1, int* status, cudaStream_t st);
+
 }  // namespace trot

@@ -9,7 +9,8 @@ import numpy as np
 import torch
 
 from . import _lib, native
-from .core import HamChol, MeasOps, System, as_dev, batched, k_energy, k_force_bias, real_part
+from . import ctx as ctx_dev
+from .core import HamChol, MeasOps, System, batched, k_energy, k_force_bias
 from .trial import RhfTrial, UhfTrial, _make_overlap
 
 
@@ -43,34 +44,24 @@ class UhfMeasCtx:
         return self.rot_h1_a, self.rot_h1_b, self.rot_chol_a, self.rot_chol_b
 
 
-def _half_rotate(h1, chol, mo):
-    cT = mo.T
-    rot_h1 = cT @ h1
-    rot_chol = np.einsum("pi,gij->gpj", cT, chol, optimize=True)
-    return rot_h1, rot_chol
-
-
 def build_rhf_meas_ctx(ham_data: HamChol, trial_data: RhfTrial, memory_mode: str = "high") -> RhfMeasCtx:
     """One-time half rotation (trot/meas/rhf.py:308-319; host twin
-    trot/runtime_layout.py:200-245)."""
+    trot/runtime_layout.py:200-245), on the device (``trot_half_rotate``)."""
     if ham_data.basis != "restricted":
         raise ValueError("RHF MeasOps currently assumes HamChol.basis == 'restricted'.")
-    mo = trial_data.mo_coeff.cpu().numpy()
-    h1 = real_part(ham_data.h1, "h1")
-    chol = real_part(ham_data.chol, "chol")
-    rot_h1, rot_chol = _half_rotate(h1, chol, mo)
-    return RhfMeasCtx(as_dev(rot_h1), as_dev(rot_chol), memory_mode)
+    rot_h1, rot_chol = ctx_dev.half_rotate(trial_data.mo_coeff, ham_data.h1, ham_data.chol)
+    return RhfMeasCtx(rot_h1, rot_chol, memory_mode)
 
 
 def build_uhf_meas_ctx(ham_data: HamChol, trial_data: UhfTrial) -> UhfMeasCtx:
-    """trot/meas/uhf.py:318-336."""
+    """trot/meas/uhf.py:318-336, on the device."""
     if ham_data.basis != "restricted":
         raise ValueError("UHF MeasOps currently assumes HamChol.basis == 'restricted'.")
-    h1 = real_part(ham_data.h1, "h1")
-    chol = real_part(ham_data.chol, "chol")
-    ha, ra = _half_rotate(h1, chol, trial_data.mo_coeff_a.cpu().numpy())
-    hb, rb = _half_rotate(h1, chol, trial_data.mo_coeff_b.cpu().numpy())
-    return UhfMeasCtx(as_dev(ha), as_dev(hb), as_dev(ra), as_dev(rb))
+    h1 = ctx_dev.real_dev(ham_data.h1, "h1")
+    chol = ctx_dev.real_dev(ham_data.chol, "chol")
+    ha, ra = ctx_dev.half_rotate(trial_data.mo_coeff_a, h1, chol)
+    hb, rb = ctx_dev.half_rotate(trial_data.mo_coeff_b, h1, chol)
+    return UhfMeasCtx(ha, hb, ra, rb)
 
 
 def _h0(ham_data) -> float:

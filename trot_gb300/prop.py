@@ -15,12 +15,11 @@ from dataclasses import dataclass
 from typing import Any, NamedTuple
 
 import numpy as np
-import scipy.linalg
 import torch
 
 from . import _lib, native, rng
-from .core import (HamChol, MeasOps, PropOps, PropState, QmcParamsBase, System, TrialOps, as_dev,
-                   k_energy, real_part)
+from . import ctx as ctx_dev
+from .core import HamChol, MeasOps, PropOps, PropState, QmcParamsBase, System, TrialOps, k_energy
 
 
 @dataclass(frozen=True)
@@ -41,33 +40,16 @@ class CholAfqmcCtx:
         return torch.complex(torch.zeros_like(self.mf_shifts_im), self.mf_shifts_im)
 
 
-def build_prop_ctx_host(h0, h1, chol, rdm1, dt):
-    """One-time propagation constants (trot/prop/chol_afqmc_ops.py:74-127; host
-    twin trot/runtime_layout.py:125-197), in float64 numpy:
-    mf = i tr(L_g rho), h0_prop = -h0 - 1/2 sum mf^2,
-    h1_eff = h1 - 1/2 sum_g L_g L_g - sum_g Re(i mf_g) L_g, exp(-dt/2 h1_eff)."""
-    rdm1 = np.asarray(rdm1)
-    dm = rdm1[0] + rdm1[1] if (rdm1.ndim == 3 and rdm1.shape[0] == 2) else rdm1
-    G, N, _ = chol.shape
-    t = np.einsum("gij,ji->g", chol, dm, optimize=True)  # mf = i t
-    h0_prop = float(-h0 + 0.5 * np.sum(t * t))
-    v0 = 0.5 * np.einsum("gik,gkj->ij", chol, chol, optimize=True)
-    v1 = np.einsum("g,gik->ik", -t, chol, optimize=True)  # Re(i * i t) = -t
-    h1_eff = h1 - v0 - v1
-    exp_h1_half = scipy.linalg.expm(-0.5 * dt * h1_eff)
-    return t, h0_prop, exp_h1_half, chol.reshape(G, N * N)
-
-
 def _build_prop_ctx(ham_data: HamChol, rdm1, dt: float, mixed_precision: bool = False) -> CholAfqmcCtx:
-    h1 = real_part(ham_data.h1, "h1")
-    chol = real_part(ham_data.chol, "chol")
+    """One-time propagation constants (trot/prop/chol_afqmc_ops.py:74-127; host
+    twin trot/runtime_layout.py:125-197), built on the device by
+    ``trot_build_prop_ctx``: mf = i tr(L_g rho), h0_prop = -h0 - 1/2 sum mf^2,
+    exp(-dt/2 h1_eff) with h1_eff = h1 - 1/2 sum_g L_g L_g - sum_g Re(i mf_g) L_g."""
     h0 = float(np.real(np.asarray(ham_data.h0.item() if isinstance(ham_data.h0, torch.Tensor) else ham_data.h0)))
-    rd = rdm1.detach().cpu().numpy() if isinstance(rdm1, torch.Tensor) else np.asarray(rdm1)
-    t, h0_prop, eh, chol_flat = build_prop_ctx_host(h0, h1, chol, np.real(rd), dt)
-    ctx = CholAfqmcCtx(dt=float(dt), sqrt_dt=float(np.sqrt(dt)), exp_h1_half=as_dev(eh),
-                       mf_shifts_im=as_dev(t), h0_prop=h0_prop, chol_flat=as_dev(chol_flat),
-                       norb=int(h1.shape[0]))
-    return ctx
+    mf_im, h0_prop, eh, chol = ctx_dev.prop_ctx(h0, ham_data.h1, ham_data.chol, rdm1, dt)
+    G, N = int(chol.shape[0]), int(chol.shape[1])
+    return CholAfqmcCtx(dt=float(dt), sqrt_dt=float(np.sqrt(dt)), exp_h1_half=eh, mf_shifts_im=mf_im,
+                        h0_prop=h0_prop, chol_flat=chol.reshape(G, N * N), norb=N)
 
 
 class TrotterOps(NamedTuple):
