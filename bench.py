@@ -336,6 +336,53 @@ def cpu_port_rate(cfg, W_sample, steps, threads=None, min_seconds=0.0, max_steps
     return W_sample * k / dt, dt, k
 
 
+def adjoint_leg(chol_scale=0.1, seed=11):
+    """Energy gradient through a whole run on the config-3 shapes (RHF trial, N=80, n=10,
+    G=400, W=512, dt=0.01, 200 steps, checkpoints / blocks of 20 steps): one forward run,
+    one forward + adjoint run, and central finite differences of the forward along a
+    symmetric one-body perturbation O ~ N(0, 0.1) (lambda = +-1e-4, same fields).  The
+    Cholesky vectors of the recipe are scaled by ``chol_scale``: unscaled, every walker
+    weight of this recipe hits the floor / cap within two steps and the mixed energy is
+    undefined (0 / 0); the work per step does not depend on the values."""
+    import torch
+
+    import trot_gb300 as tg
+    from trot_gb300 import adjoint, synthetic
+
+    cfg = synthetic.CONFIGS["cfg3_rhf_n80"]
+    N, (n, _), G, W, T, spb, dt = (cfg["norb"], cfg["nelec"], cfg["nchol"], cfg["n_walkers"], cfg["n_steps"],
+                                   cfg["qr_every"], cfg["dt"])
+    h0, h1, chol = synthetic.hamiltonian(N, G, cfg["decay"], seed, 0.0)
+    chol = chol * chol_scale
+    mo = synthetic.scf(h1, chol, n, n, 30)[0]
+    fields = torch.as_tensor(np.random.default_rng(seed + 1).standard_normal((T, W, G))).cuda()
+    params = tg.QmcParams(dt=dt, n_exp_terms=6, n_prop_steps=spb, n_walkers=W)
+    trial = tg.RhfTrial(mo)
+    one = adjoint.as_problem(h0, chol, trial, params, fields[:, :1].contiguous(), steps_per_block=spb)
+    e0 = float(adjoint.LocalEnergy.apply(one.walkers0, torch.as_tensor(h1).cuda(), one)[0])
+    prob = adjoint.as_problem(h0, chol, trial, params, fields, e_estimate0=e0, steps_per_block=spb)
+    adjoint.energy(h1, prob)  # warm-up (first launches, workspaces)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J = adjoint.energy(h1, prob)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    _, g = adjoint.energy_and_grad(h1, prob)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    O = np.random.default_rng(9).normal(scale=0.1, size=h1.shape)
+    O = 0.5 * (O + O.T)
+    eps = 1e-4
+    fd = (adjoint.energy(h1 + eps * O, prob) - adjoint.energy(h1 - eps * O, prob)) / (2 * eps)
+    ad = float(torch.sum(g.cpu() * torch.as_tensor(O)))
+    return {"workload": f"rhf_r N={N} n={n} G={G} W={W} dt={dt} {T} steps, blocks/checkpoints of {spb}, "
+                        f"Cholesky x{chol_scale}, SR off, FP64",
+            "objective": "sum_b sum_w wt E~ / sum_b sum_w wt (block energies after QR, clamp, e_estimate EMA)",
+            "mixed_energy": J, "forward_s": t1 - t0, "forward_and_adjoint_s": t2 - t1,
+            "dJ_dlambda_adjoint": ad, "dJ_dlambda_fd": fd, "rel_diff_vs_fd": abs(ad - fd) / max(abs(fd), 1e-300),
+            "fd_lambda": eps}
+
+
 def cpu_cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -354,6 +401,7 @@ def main():
     ap.add_argument("--config", default="cfg2_uhf_n120")
     ap.add_argument("--cpu-sample", type=int, default=0, help="walkers in the CPU baseline sample (0 = auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the config-3 energy-gradient leg")
     ap.add_argument("--profile-run", action="store_true",
                     help="timed steps only (no e2e, FP64 comparison, precision check or CPU baseline): "
                          "for profiler launch lists")
@@ -553,6 +601,8 @@ def main():
         line["speedup_vs_fp64"] = value / fp64["value"]
     if precision_info is not None:
         line["precision_check"] = precision_info
+    if not args.no_adjoint and rank == 0 and world == 1:
+        line["adjoint"] = adjoint_leg()
     if not args.no_cpu_baseline:
         sample = args.cpu_sample or 64
         r, secs, ks = cpu_port_rate(cfg, sample, 2, min_seconds=10.0)

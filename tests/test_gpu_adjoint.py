@@ -175,3 +175,28 @@ def test_adjoint_rejects_other_kinds():
     s.kind = _lib.UHF_U
     assert _lib.load().trot_vjp_workspace_size(ctypes.byref(s), _lib.OP_PROP_STEP) == 0
     assert b"restricted" in _lib.load().trot_last_error()
+
+
+def test_dead_walkers_pass_no_gradient():
+    """Walkers with zero weight cannot influence the objective: the gradient stays
+    finite when such a walker holds NaN and does not depend on its values."""
+    import trot_gb300 as tg
+    from trot_gb300 import adjoint
+
+    ss, fields, w0, prob = _problem()
+    W = w0.shape[0]
+    wt0 = torch.ones(W, dtype=torch.float64)
+    wt0[1] = 0.0
+    wt0[4] = 0.0
+    grads = []
+    for fill in (np.nan, 0.37):
+        w = w0.copy()
+        w[1] = fill
+        w[4] = fill * 2
+        p = adjoint.as_problem(ss.h0, ss.chol, tg.RhfTrial(ss.mo_a), prob.params, prob.fields,
+                               walkers0=torch.as_tensor(w).cuda(), e_estimate0=-2.0,
+                               steps_per_block=prob.steps_per_block, weights0=wt0.cuda())
+        J, g = adjoint.energy_and_grad(ss.h1, p)
+        assert np.isfinite(float(J)) and bool(torch.isfinite(g).all())
+        grads.append(g)
+    assert torch.equal(grads[0], grads[1])

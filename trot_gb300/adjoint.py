@@ -54,6 +54,7 @@ class AdjointProblem:
     walkers0: torch.Tensor
     e_estimate0: float
     steps_per_block: int
+    weights0: torch.Tensor | None = None
 
     def __post_init__(self):
         self.chol = ctx_dev.real_dev(self.chol, "chol")
@@ -281,7 +282,8 @@ def mixed_energy(h1: torch.Tensor, prob: AdjointProblem, checkpoint_blocks: bool
     eh = ExpH1Half.apply(h1, prob)
     w = prob.walkers0
     W = prob.n_walkers
-    wt = torch.ones(W, dtype=torch.float64, device=w.device)
+    wt = (torch.ones(W, dtype=torch.float64, device=w.device) if prob.weights0 is None
+          else ctx_dev.real_dev(prob.weights0, "weights0"))
     ov = Overlap.apply(w, prob).detach()
     scal = torch.tensor([prob.e_estimate0, prob.e_estimate0], dtype=torch.float64, device=w.device)
     num = torch.zeros((), dtype=torch.float64, device=w.device)
@@ -318,16 +320,17 @@ def initial_walkers(trial: RhfTrial, n_walkers: int) -> torch.Tensor:
     return mo.unsqueeze(0).repeat(n_walkers, 1, 1).contiguous()
 
 
-def as_problem(h0, chol, trial, params, fields, walkers0=None, e_estimate0=None, steps_per_block=None):
+def as_problem(h0, chol, trial, params, fields, walkers0=None, e_estimate0=None, steps_per_block=None,
+               weights0=None):
     """Convenience constructor; e_estimate0 defaults to 0 (it only enters the
-    clamp and the population-control shift)."""
+    clamp and the population-control shift); weights0 defaults to ones."""
     W = int(fields.shape[1])
     if walkers0 is None:
         walkers0 = initial_walkers(trial, W)
     rdm1 = torch.stack([trial.mo_coeff @ trial.mo_coeff.T, trial.mo_coeff @ trial.mo_coeff.T])
     return AdjointProblem(h0=float(h0), chol=chol, trial=trial, rdm1=rdm1, params=params, fields=fields,
                           walkers0=walkers0, e_estimate0=float(e_estimate0 or 0.0),
-                          steps_per_block=int(steps_per_block or params.n_prop_steps))
+                          steps_per_block=int(steps_per_block or params.n_prop_steps), weights0=weights0)
 
 
 __all__ = ["AdjointProblem", "mixed_energy", "energy_and_grad", "energy", "as_problem", "initial_walkers",

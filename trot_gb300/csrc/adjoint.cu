@@ -41,21 +41,25 @@ __device__ __forceinline__ double2 ld_op(const double2* X, int ld, int op, int r
   return cmk(v.x, -v.y);
 }
 
-__global__ void __launch_bounds__(256) zgemm_batched_kernel(ZBatch z) {
-  __shared__ double2 As[32][17], Bs[16][33];
+// Tile 32 x BN, K chunks of 16, 8 * BN threads; thread (ty, tx) owns rows ty + 8 r (r < 4) of column tx.
+// BN = 16 for the skinny per-walker products (n columns), 32 otherwise.
+template <int BN>
+__global__ void __launch_bounds__(8 * BN) zgemm_batched_kernel(ZBatch z) {
+  constexpr int NT = 8 * BN;
+  __shared__ double2 As[32][17], Bs[16][BN + 1];
   const int b = blockIdx.z;
-  const int m0 = blockIdx.y * 32, n0 = blockIdx.x * 32;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int m0 = blockIdx.y * 32, n0 = blockIdx.x * BN;
+  const int tx = threadIdx.x % BN, ty = threadIdx.x / BN;
   const double2* A = z.A + (size_t)b * z.sA;
   const double2* B = z.B + (size_t)b * z.sB;
   double2 acc[4] = {cmk(0.0, 0.0), cmk(0.0, 0.0), cmk(0.0, 0.0), cmk(0.0, 0.0)};
   for (int k0 = 0; k0 < z.K; k0 += 16) {
-    for (int e = threadIdx.x; e < 32 * 16; e += 256) {
+    for (int e = threadIdx.x; e < 32 * 16; e += NT) {
       const int r = e >> 4, c = e & 15, m = m0 + r, k = k0 + c;
       As[r][c] = (m < z.M && k < z.K) ? ld_op(A, z.lda, z.opA, m, k) : cmk(0.0, 0.0);
     }
-    for (int e = threadIdx.x; e < 16 * 32; e += 256) {
-      const int r = e >> 5, c = e & 31, k = k0 + r, n = n0 + c;
+    for (int e = threadIdx.x; e < 16 * BN; e += NT) {
+      const int r = e / BN, c = e % BN, k = k0 + r, n = n0 + c;
       Bs[r][c] = (k < z.K && n < z.Nc) ? ld_op(B, z.ldb, z.opB, k, n) : cmk(0.0, 0.0);
     }
     __syncthreads();
@@ -84,10 +88,16 @@ static int zgemm_batched(int batch, int M, int Nc, int K, double2 alpha, const d
                          int opA, const double2* B, long long sB, int ldb, int opB, double2 beta, double2* C,
                          long long sC, int ldc, cudaStream_t st) {
   ZBatch z{M, Nc, K, alpha, beta, A, sA, lda, opA, B, sB, ldb, opB, C, sC, ldc};
-  zgemm_batched_kernel<<<dim3((Nc + 31) / 32, (M + 31) / 32, batch), 256, 0, st>>>(z);
+  if (Nc <= 16) {
+    zgemm_batched_kernel<16><<<dim3(1, (M + 31) / 32, batch), 128, 0, st>>>(z);
+  } else {
+    zgemm_batched_kernel<32><<<dim3((Nc + 31) / 32, (M + 31) / 32, batch), 256, 0, st>>>(z);
+  }
   TROT_CHECK_LAUNCH("zgemm_batched_kernel");
   return TROT_OK;
 }
+
+static int grid_of_(size_t len) { return (int)((len + 255) / 256 < 4096 ? (len + 255) / 256 : 4096); }
 
 // ---------------------------------------------------------------- per-walker small kernels
 // O = C^T w, P = O^-1, G = (w P)^T (n x N), det(O); one block per walker (n <= 32).
@@ -141,7 +151,8 @@ __global__ void adj_kappa_kernel(int W, const double2* __restrict__ det, const d
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= W) return;
   const double2 ov = cmul(det[b], det[b]);
-  kappa[b] = cscale(cmul(cmk(ov.x, -ov.y), gov[b]), 2.0);
+  const double2 g = gov[b];
+  kappa[b] = (g.x == 0.0 && g.y == 0.0) ? cmk(0.0, 0.0) : cscale(cmul(cmk(ov.x, -ov.y), g), 2.0);
 }
 
 // g_w += (g_Gt - C X) P^H with X = Gt^H g_Gt (n x n); Gt = G^T, g_Gt = g_G^T.
@@ -202,6 +213,13 @@ __global__ void adj_qr_kernel(int N, int n, const double2* __restrict__ w, const
   block_gauss_jordan(M, n, n, Mi, &piv, red);
   __syncthreads();
   const double2* g = gq + (size_t)b * N * n;
+  // a walker with a zero cotangent (no influence on the objective) gets exactly zero
+  int nz = 0;
+  for (int e = tid; e < N * n; e += blockDim.x) nz |= (g[e].x != 0.0 || g[e].y != 0.0);
+  if (!__syncthreads_or(nz)) {
+    for (int e = tid; e < N * n; e += blockDim.x) gw[(size_t)b * N * n + e] = cmk(0.0, 0.0);
+    return;
+  }
   for (int e = tid; e < N * n; e += blockDim.x) {
     const int p = e / n, k = e % n;
     double2 acc = cmk(0.0, 0.0);
@@ -265,6 +283,29 @@ static int combine(size_t len, const Comb& cb, double2* out, bool accumulate, cu
   return TROT_OK;
 }
 
+// Walkers that cannot influence the objective (zero weight before the step, or
+// a weight the step's guards set to zero; zero energy / overlap cotangent) get
+// exactly zero cotangents: their recomputed data, which may be non-finite, is
+// replaced by zeros so that no 0 * inf enters a sum over walkers.
+__global__ void adj_zero_inactive_kernel(int W, size_t per, const int* __restrict__ act, double2* __restrict__ x) {
+  const size_t total = (size_t)W * per;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x)
+    if (!act[e / per]) x[e] = cmk(0.0, 0.0);
+}
+
+// act[b] = (g[b] != 0) for a real or complex per-walker cotangent
+__global__ void adj_act_from_cotangent_kernel(int W, const double* __restrict__ g, int complex_g, int* __restrict__ act) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= W) return;
+  act[b] = complex_g ? (g[2 * b] != 0.0 || g[2 * b + 1] != 0.0) : (g[b] != 0.0);
+}
+
+static int zero_inactive(int W, size_t per, const int* act, double2* x, cudaStream_t st) {
+  adj_zero_inactive_kernel<<<grid_of_(W * per), 256, 0, st>>>(W, per, act, x);
+  TROT_CHECK_LAUNCH("adj_zero_inactive_kernel");
+  return TROT_OK;
+}
+
 // ---------------------------------------------------------------- step: scalar forward + backward per walker
 struct StepScalars {
   double2 ov_old, ov_new, st, ft;
@@ -297,7 +338,7 @@ __global__ void adj_step_fwd_kernel(int W, const double2* __restrict__ ov_old, c
                                     const double2* __restrict__ st, const double2* __restrict__ ft,
                                     const double* __restrict__ wt, const double* __restrict__ scal, double dt,
                                     double sqrt_dt, double h0_prop, double w_floor, double w_cap,
-                                    double* __restrict__ wt_new) {
+                                    double* __restrict__ wt_new, int* __restrict__ act) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= W) return;
   StepScalars s{ov_old[b], cmul(det_new[b], det_new[b]), st[b], ft[b], wt[b], scal[0], dt, sqrt_dt, h0_prop,
@@ -307,6 +348,7 @@ __global__ void adj_step_fwd_kernel(int W, const double2* __restrict__ ov_old, c
   bool live;
   const double ip = imp_forward(s, &E, &r, &live);
   wt_new[b] = live ? wt[b] * ip : 0.0;
+  act[b] = (live && wt[b] != 0.0) ? 1 : 0;
 }
 
 // fixed-order sum of x[0..n) into out[0] (one block)
@@ -357,11 +399,12 @@ __global__ void adj_step_bwd_kernel(int W, const double2* __restrict__ ov_old, c
   const double2 inv_old = cdiv(cmk(1.0, 0.0), s.ov_old);
   gov_new = cadd(gov_new, cmul(cmk(inv_old.x, -inv_old.y), grho));
   const double2 rq = cmul(rho, inv_old);
-  g_ov[b] = cscale(cmul(cmk(rq.x, -rq.y), grho), -1.0);
-  kappa[b] = cscale(cmul(cmk(ovn.x, -ovn.y), gov_new), 2.0);
-  g_req[b] = greq;
-  g_c[b] = gc;
-  g_es[b] = dt * greq;
+  const bool active = live && wt[b] != 0.0;
+  g_ov[b] = active ? cscale(cmul(cmk(rq.x, -rq.y), grho), -1.0) : cmk(0.0, 0.0);
+  kappa[b] = active ? cscale(cmul(cmk(ovn.x, -ovn.y), gov_new), 2.0) : cmk(0.0, 0.0);
+  g_req[b] = active ? greq : 0.0;
+  g_c[b] = active ? gc : 0.0;
+  g_es[b] = active ? dt * greq : 0.0;
 }
 
 // g_fb[b][g] from g_xs^V and the per-walker scalars (see header): xs = x - fs, fs = -i sqrt(dt) (fb - m),
@@ -483,6 +526,8 @@ struct StepWs {
   double2 *green, *P, *det, *fb, *xs, *st, *ft, *V, *U, *w2, *wnew, *greenn, *Pn, *detn, *Bc;
   double2 *gwn, *gw2, *Vv, *S, *gV, *gxsv, *gfb, *gG, *gw1, *kappa, *gov_tmp;
   double *wt_new, *wsum, *g_req, *g_c, *g_es;
+  int* act;
+  double2* wz;
 };
 
 static void carve_step(const AdjCommon& a, Carver& c, StepWs& b) {
@@ -518,10 +563,13 @@ static void carve_step(const AdjCommon& a, Carver& c, StepWs& b) {
   b.g_req = c.take<double>(W);
   b.g_c = c.take<double>(W);
   b.g_es = c.take<double>(W);
+  b.act = c.take<int>(W);
+  b.wz = c.take<double2>(a.wn);
 }
 
 struct EnergyWs {
   double2 *green, *P, *det, *F, *Ft, *c, *D, *gG, *H;
+  int* act;
 };
 
 static void carve_energy(const AdjCommon& a, Carver& c, EnergyWs& b) {
@@ -535,6 +583,7 @@ static void carve_energy(const AdjCommon& a, Carver& c, EnergyWs& b) {
   b.D = c.take<double2>(W * a.nN);
   b.gG = c.take<double2>(W * a.nN);
   b.H = c.take<double2>(a.nN);
+  b.act = c.take<int>(W);
 }
 
 static int green_launch(const AdjCommon& a, const double* C, const double2* w, double2* green, double2* P,
@@ -572,7 +621,7 @@ size_t trot_vjp_workspace_size(const trot_system* s, int op) {
     c.take<double2>(a.W * a.nN);
     c.take<double2>((size_t)a.W * a.n * a.n);
     c.take<double2>(a.W);
-    c.take<double2>(a.W);
+    c.take<double2>((size_t)2 * a.W);
   } else if (op == TROT_OP_QR) {
     return 256;
   } else {
@@ -638,10 +687,23 @@ int trot_prop_step_vjp(const trot_system* s, const trot_state* in, const double*
   const int wb = (W + 127) / 128;
   adj_step_fwd_kernel<<<wb, 128, 0, st>>>(W, (const double2*)in->overlaps, b.detn, b.st, b.ft, in->weights,
                                            in->scalars, s->dt, s->sqrt_dt, s->h0_prop, s->weight_floor, s->weight_cap,
-                                           b.wt_new);
+                                           b.wt_new, b.act);
   TROT_CHECK_LAUNCH("adj_step_fwd_kernel");
   adj_sum_kernel<<<1, 256, 0, st>>>(W, b.wt_new, b.wsum);
   TROT_CHECK_LAUNCH("adj_sum_kernel");
+  // inactive walkers: zero their recomputed data (see adj_zero_inactive_kernel)
+  {
+    cudaError_t e0 = cudaMemcpyAsync(b.wz, w, a.wn * sizeof(double2), cudaMemcpyDeviceToDevice, st);
+    if (e0 != cudaSuccess) return cuda_status(e0, "trot_prop_step_vjp copy");
+    TROT_TRY(zero_inactive(W, (size_t)N * n, b.act, b.wz, st));
+    for (int l = 0; l <= K; ++l) TROT_TRY(zero_inactive(W, (size_t)N * n, b.act, b.U + (size_t)l * a.wn, st));
+    TROT_TRY(zero_inactive(W, (size_t)N * n, b.act, b.w2, st));
+    TROT_TRY(zero_inactive(W, NN, b.act, b.V, st));
+    TROT_TRY(zero_inactive(W, a.nN, b.act, b.green, st));
+    TROT_TRY(zero_inactive(W, (size_t)n * n, b.act, b.P, st));
+    TROT_TRY(zero_inactive(W, (size_t)n * n, b.act, b.Pn, st));
+    TROT_TRY(zero_inactive(W, G, b.act, b.xs, st));
+  }
   // ---------------- backward
   adj_step_bwd_kernel<<<wb, 128, 0, st>>>(W, (const double2*)in->overlaps, b.detn, b.st, b.ft, in->weights,
                                            in->scalars, s->dt, s->sqrt_dt, s->h0_prop, s->weight_floor, s->weight_cap,
@@ -657,6 +719,7 @@ int trot_prop_step_vjp(const trot_system* s, const trot_state* in, const double*
   // g_w' (incoming) + overlap term
   cudaError_t e = cudaMemcpyAsync(b.gwn, g_walkers_out, a.wn * sizeof(double2), cudaMemcpyDeviceToDevice, st);
   if (e != cudaSuccess) return cuda_status(e, "trot_prop_step_vjp copy");
+  TROT_TRY(zero_inactive(W, (size_t)N * n, b.act, b.gwn, st));
   adj_overlap_kernel<<<W, 256, 0, st>>>(N, n, s->mo_a, b.Pn, b.kappa, b.gwn);
   TROT_CHECK_LAUNCH("adj_overlap_kernel");
   // w' = B w2: g_B += Re sum g_w' w2^H; g_w2 = B^T g_w'
@@ -691,7 +754,7 @@ int trot_prop_step_vjp(const trot_system* s, const trot_state* in, const double*
   // fb = 2 G R^T: g_G = 2 g_fb R
   TROT_TRY(launch_zgemm_cr(W, (int)a.nN, G, 2.0, b.gfb, G, s->rot_chol_a, (int)a.nN, false, b.gG, (int)a.nN, false, st));
   // w1 = B w: g_B += Re sum g_w1 w^H; g_w = B^T g_w1 + G-term
-  adj_outer_sum_kernel<<<dim3((N + 31) / 32, (N + 31) / 32), 256, 0, st>>>(W, N, n, b.gw1, w, g_exp_h1_half);
+  adj_outer_sum_kernel<<<dim3((N + 31) / 32, (N + 31) / 32), 256, 0, st>>>(W, N, n, b.gw1, b.wz, g_exp_h1_half);
   TROT_CHECK_LAUNCH("adj_outer_sum_kernel");
   TROT_TRY(zgemm_batched(W, N, n, N, one, b.Bc, 0, N, 1, b.gw1, (long long)N * n, n, 0, zero, (double2*)g_walkers_in,
                          (long long)N * n, n, st));
@@ -716,6 +779,10 @@ int trot_local_energy_vjp(const trot_system* s, const double* walkers, const dou
   const int W = a.W, N = a.N, n = a.n, G = a.G;
   const double2* w = (const double2*)walkers;
   TROT_TRY(green_launch(a, s->mo_a, w, b.green, b.P, b.det, st));
+  adj_act_from_cotangent_kernel<<<(W + 127) / 128, 128, 0, st>>>(W, g_energy, 0, b.act);
+  TROT_CHECK_LAUNCH("adj_act_from_cotangent_kernel");
+  TROT_TRY(zero_inactive(W, a.nN, b.act, b.green, st));
+  TROT_TRY(zero_inactive(W, (size_t)n * n, b.act, b.P, st));
   // F[b n + j][g n + i] = f_g[i][j] = sum_p R_g[i][p] G[j][p]
   TROT_TRY(launch_zgemm_cr(W * n, G * n, N, 1.0, b.green, N, s->rot_chol_a, N, true, b.F, G * n, false, st));
   adj_trace_kernel<<<grid_of((size_t)W * G), 256, 0, st>>>(W, G, n, b.F, b.c);
@@ -744,10 +811,14 @@ int trot_overlap_vjp(const trot_system* s, const double* walkers, const double* 
   double2* green = c.take<double2>(a.W * a.nN);
   double2* P = c.take<double2>((size_t)a.W * a.n * a.n);
   double2* det = c.take<double2>(a.W);
-  double2* kappa = c.take<double2>(a.W);
+  double2* kappa = c.take<double2>((size_t)2 * a.W);  // kappa, then W ints of walker flags
   if (!c.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, c.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
   cudaStream_t st = (cudaStream_t)stream;
   TROT_TRY(green_launch(a, s->mo_a, (const double2*)walkers, green, P, det, st));
+  int* act = reinterpret_cast<int*>(kappa + a.W);
+  adj_act_from_cotangent_kernel<<<(a.W + 127) / 128, 128, 0, st>>>(a.W, g_overlaps, 1, act);
+  TROT_CHECK_LAUNCH("adj_act_from_cotangent_kernel");
+  TROT_TRY(zero_inactive(a.W, (size_t)a.n * a.n, act, P, st));
   adj_kappa_kernel<<<(a.W + 127) / 128, 128, 0, st>>>(a.W, det, (const double2*)g_overlaps, kappa);
   TROT_CHECK_LAUNCH("adj_kappa_kernel");
   adj_overlap_kernel<<<a.W, 256, 0, st>>>(a.N, a.n, s->mo_a, P, kappa, (double2*)g_walkers);
