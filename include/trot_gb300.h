@@ -426,7 +426,7 @@ int trot_tc_gemm_bf16(const uint16_t* A, const uint16_t* B, float* D, int M, int
  * timing candidates on the caller's workload (trot_gb300.autotune); every
  * setting computes bit-identical results.  No counterpart in the reference.
  *   TROT_TUNE_EXCHANGE_TILES: walker tiles per work item of the exact-slice
- *     exchange kernel (default 16);
+ *     exchange kernel (default 8);
  *   TROT_TUNE_EXCHANGE_GRID: persistent CTAs of that kernel (default 152). */
 typedef enum { TROT_TUNE_EXCHANGE_TILES = 0, TROT_TUNE_EXCHANGE_GRID = 1, TROT_TUNE_COUNT = 2 } trot_tune_knob;
 int trot_set_tuning(int knob, int value);
