@@ -41,7 +41,18 @@ TROT_D ff ff_mul(ff x, ff y) {
   e = fmaf(x.lo, y.hi, e);
   return ff_fast(p, e);
 }
-TROT_D double ff_d(ff x) { return (double)x.hi + (double)x.lo; }
+// float -> double by moving the bits (exact for normal floats; zero, subnormal, inf and
+// NaN take the conversion instruction)
+TROT_D double f2d_bits(float f) {
+  const unsigned v = (unsigned)__float_as_int(f);
+  const unsigned e = (v >> 23) & 0xFFu;
+  if (e == 0u || e == 0xFFu) return (double)f;
+  const unsigned long long d = ((unsigned long long)(v & 0x80000000u) << 32) |
+                               ((unsigned long long)(e - 127u + 1023u) << 52) |
+                               ((unsigned long long)(v & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)d);
+}
+TROT_D double ff_d(ff x) { return f2d_bits(x.hi) + f2d_bits(x.lo); }
 // 2^e as a float for e in [-126, 127] (exact; the exponents here stay far inside)
 TROT_D float pow2f(int e) { return __int_as_float((e + 127) << 23); }
 TROT_D ff ff_shfl_xor(ff x, int o) {
@@ -66,9 +77,25 @@ TROT_D void ff_mad(ff& acc, ff a, ff b) {
 // with the two N x n^2 products in float-float (FP32 pairs, ~2^-44 relative)
 // on the FP32 pipe instead of FP64.  One CTA per walker.
 struct ffc { ff re, im; };
+// Split a double into float-float with integer operations only (conversions and
+// double arithmetic run on the FP64 pipe, a few operations per clock per SM on this
+// GPU): hi = the top 24 significant bits (truncated), lo = the next 29 bits rounded to
+// a float, so hi + lo = x to 2^-48 relative.  Values below 2^-126 give 0; values past
+// the float range give inf; NaN and inf pass through.
 TROT_D ff ff_from_d(double x) {
-  const float h = __double2float_rn(x);
-  return ff{h, __double2float_rn(x - (double)h)};
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
+  const int ex = (int)((u >> 52) & 0x7FF);
+  if (ex == 0x7FF) return ff{__double2float_rn(x), 0.f};
+  const int ef = ex - 1023 + 127;
+  if (ex == 0 || ef <= 0) return ff{__int_as_float((int)sign), 0.f};
+  if (ef >= 255) return ff{__int_as_float((int)(sign | 0x7F800000u)), 0.f};
+  const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
+  const float hi = __int_as_float((int)(sign | ((unsigned)ef << 23) | (unsigned)(m >> 29)));
+  const float r = __uint2float_rn((unsigned)(m & 0x1FFFFFFFull));
+  const int sc = ex - 1075;  // rem * 2^(ex - 1023 - 52)
+  float lo = sc >= -126 ? r * pow2f(sc) : ldexpf(r, sc);
+  return ff{hi, sign ? -lo : lo};
 }
 TROT_D ff ff_fma(ff acc, ff a, ff b) { return ff_add(acc, ff_mul(a, b)); }
 
@@ -87,9 +114,9 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
   ffc* Mif = reinterpret_cast<ffc*>(Mi + nmax * nmax);            // n x n
   ff e1r{0.f, 0.f}, e1i{0.f, 0.f};
   for (int s = 0; s < sp.nspin; ++s) {
-    const int n = sp.n[s];
+    const int n = s ? sp.n[1] : sp.n[0];
     const double2* w = (s == 0 ? wa : wb) + (size_t)b * N * n;
-    const double* C = sp.mo[s];
+    const double* C = s ? sp.mo[1] : sp.mo[0];
     __syncthreads();
     for (int e = tid; e < N * n; e += nt) {
       const double2 x = w[e];
@@ -132,9 +159,9 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
     block_gauss_jordan(Md, n, n, Mi, &piv, red);
     for (int e = tid; e < n * n; e += nt) Mif[e] = ffc{ff_from_d(Mi[e].x), ff_from_d(Mi[e].y)};
     __syncthreads();
-    const double* H = sp.rot_h1[s];
-    double2* gout = green + (size_t)b * sp.ntot * N + (size_t)sp.off[s] * N;
-    const float m = (float)sp.mult[s];
+    const double* H = s ? sp.rot_h1[1] : sp.rot_h1[0];
+    double2* gout = green + (size_t)b * sp.ntot * N + (size_t)(s ? sp.off[1] : 0) * N;
+    const float m = (float)(s ? sp.mult[1] : sp.mult[0]);
     for (int e = tid; e < n * N; e += nt) {
       const int i = e / N, p = e % N;
       ff gr{0.f, 0.f}, gi{0.f, 0.f};
@@ -280,6 +307,27 @@ size_t mixed_workspace_size(const trot_system* s, int op) {
   return carve_mixed(s, sp, c, m, op);
 }
 
+// rint(x 2^s) (round half to even) by integer operations, for |x 2^s| < 2^62; zero and
+// subnormal x give 0 (the callers scale the row maximum to 2^40).
+TROT_D long long rint_scaled(double x, int s) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((u >> 52) & 0x7FF);
+  if (ex == 0 || ex == 0x7FF) return 0;
+  const unsigned long long M = (u & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const int sh = 1075 - ex - s;  // x 2^s = M 2^(ex - 1075 + s)
+  unsigned long long q;
+  if (sh <= 0) {
+    q = M << (-sh);
+  } else if (sh >= 64) {
+    q = 0;
+  } else {
+    q = M >> sh;
+    const unsigned long long r = M & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (r > half || (r == half && (q & 1ull))) ++q;
+  }
+  return (u >> 63) ? -(long long)q : (long long)q;
+}
+
 // ------------------------------------------------------------------ Green's function slices
 // Rows (b, spin, c in {re, im}, j) of the half Green's function over orbitals
 // p, as exact fixed-point bf16 slices: v = round(x 2^(40 - e)) (|v| <= 2^40),
@@ -313,17 +361,16 @@ green_slices_kernel(int N, int n, int n_pad, int WB, int W, int ntot, int off, c
       const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
       mx = t > mx ? t : mx;
     }
+    // e = the smallest integer with max |x| <= 2^e, from the bits of the maximum
+    const int E = (int)((mx >> 52) & 0x7FF);
+    const bool nonfinite = E == 0x7FF;  // the row's slices become NaN, so its products are NaN
     int e = 0;
-    if (mx != 0) {
-      int ex;
-      const double m = frexp(__longlong_as_double((long long)mx), &ex);  // mx = m 2^ex, m in [0.5, 1)
-      e = (m == 0.5) ? ex - 1 : ex;                                       // mx <= 2^e
-    }
+    if (mx != 0 && !nonfinite) e = E == 0 ? -1022 : (E - 1023) + ((mx & 0xFFFFFFFFFFFFFull) != 0 ? 1 : 0);
     if (lane == 0) ge[(size_t)tile * kBN + row] = e;
 #pragma unroll
     for (int k = 0; k < kKP / 32; ++k) {
       const int p = lane + 32 * k;
-      long long v = (long long)rint(ldexp(x[k], 8 * kSlices - e));
+      long long v = rint_scaled(x[k], 8 * kSlices - e);
 #pragma unroll
       for (int t = 0; t < kSlices; ++t) {
         const int sh = 8 * (kSlices - 1 - t);
@@ -332,7 +379,7 @@ green_slices_kernel(int N, int n, int n_pad, int WB, int W, int ntot, int off, c
         v -= d << sh;
         const __nv_bfloat16 h = __int2bfloat16_rn((int)d);
         gq[(((size_t)tile * kSlices + t) * 2 + (p >> 6)) * kBN * kKH + img_idx64(row, p & 63)] =
-            *reinterpret_cast<const uint16_t*>(&h);
+            nonfinite ? (uint16_t)0x7FC0u : *reinterpret_cast<const uint16_t*>(&h);
       }
     }
   }
@@ -1155,7 +1202,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, Tro
             if (j < nc && prow) {
               const int s = j < sp.n[0] ? 0 : 1, n = s ? sp.n[1] : sp.n[0], col = s ? j - sp.off[1] : j;
               (s == 0 ? a.out_a : a.out_b)[((size_t)b * N + p) * n + col] =
-                  make_double2((double)d[2 * jj], (double)d[2 * jj + 1]);
+                  make_double2(f2d_bits(d[2 * jj]), f2d_bits(d[2 * jj + 1]));
             }
           }
           continue;
@@ -1246,9 +1293,9 @@ __global__ void __launch_bounds__(256) overlap_weight_ff_kernel(Spins sp, Trotte
   double2* Md = reinterpret_cast<double2*>(Cf + (size_t)N * nmax + ((N * nmax) & 1));  // n x n
   double2 det_all = cmk(1.0, 0.0);
   for (int s = 0; s < sp.nspin; ++s) {
-    const int n = sp.n[s];
+    const int n = s ? sp.n[1] : sp.n[0];
     const double2* w = (s == 0 ? a.out_a : a.out_b) + (size_t)b * N * n;
-    const double* C = sp.mo[s];
+    const double* C = s ? sp.mo[1] : sp.mo[0];
     __syncthreads();
     for (int e = tid; e < N * n; e += nt) {
       const double2 x = w[e];
@@ -1287,7 +1334,7 @@ __global__ void __launch_bounds__(256) overlap_weight_ff_kernel(Spins sp, Trotte
     }
     __syncthreads();
     const double2 det = block_gauss_jordan(Md, n, n, nullptr, &piv, red);
-    det_all = cmul(det_all, sp.mult[s] == 2 ? cmul(det, det) : det);
+    det_all = cmul(det_all, (s ? sp.mult[1] : sp.mult[0]) == 2 ? cmul(det, det) : det);
   }
   if (tid == 0) phaseless_update(a, b, det_all);
 }
