@@ -13,6 +13,7 @@
 //   local energy: the terms of energy_kernel_rw_rh, see cisd_energy_combine.
 // The l2ci2 quadratic forms 2 sum_g X_g^T ci2 X_g - X_g^T ci2_perm X_g (ci2_perm[(p,u),(q,t)] = ci2[p,t,q,u])
 // = sum_g X_g^T ci2m X_g (X_g = vec(glgp_g)) are one GEMM over all (walker, g) rows.
+#include "ff.cuh"
 #include "kernels.h"
 #include "mixed.h"
 
@@ -261,7 +262,20 @@ cisd_gamma_kernel(int N, int n, int v, int G, const double2* __restrict__ green,
 }
 
 // Same sums as cisd_gamma_kernel with gl = G L and lci2_green = R M2^T in FP32
-// (float2 x float products, FP64 accumulation of the sums); lg1 and its terms stay FP64.
+// (the reference's float32 mixed dtype; sums accumulated in float-float), and lg1 =
+// R G^T, lci1g = lci1^T G^T and their products in float-float (FP32 pairs, ~2^-44
+// relative: FP64-level results on the FP32 pipe; GB300's FP64 pipe runs a few
+// operations per clock per SM).  Double -> float / float-float conversions by integer
+// operations (ff.cuh) for the same reason.
+TROT_D void ffc_mad(ffc& acc, const ffc& a, const ffc& b) {  // acc += a b (complex)
+  ff_mad(acc.re, a.re, b.re);
+  ff_mad(acc.re, ff{-a.im.hi, -a.im.lo}, b.im);
+  ff_mad(acc.im, a.re, b.im);
+  ff_mad(acc.im, a.im, b.re);
+}
+TROT_D ffc ffc_norm(ffc a) { return ffc{ff_fast(a.re.hi, a.re.lo), ff_fast(a.im.hi, a.im.lo)}; }
+TROT_D double2 ffc_d(ffc a) { return make_double2(ff_d(a.re), ff_d(a.im)); }
+
 __global__ void __launch_bounds__(256)
 cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ green, const double* __restrict__ chol,
                       const double* __restrict__ lci1, const double2* __restrict__ m2,
@@ -270,40 +284,53 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
   __shared__ double2 red[32];
   const int chunk = blockIdx.x, b = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
   const int nchunk = gridDim.x;
-  double2* Gs = sm;                                      // n x N (FP64)
-  double2* C1 = Gs + n * N;                              // n x n
-  double2* A = C1 + n * n;                               // n x n  (lg1)
-  double* Rd = reinterpret_cast<double*>(A + n * n);     // n x N  (rows < n of L_g)
-  float2* Gf = reinterpret_cast<float2*>(Rd + n * N);    // n x N
-  float2* M2f = Gf + n * N;                              // N x N
-  float2* GLf = M2f + N * N;                             // n x N
-  float* Lf = reinterpret_cast<float*>(GLf + n * N);     // N x N
+  ffc* Gs = reinterpret_cast<ffc*>(sm);                   // n x N
+  ffc* C1 = Gs + n * N;                                   // n x n
+  ffc* A = C1 + n * n;                                    // n x n  (lg1)
+  ff* Rd = reinterpret_cast<ff*>(A + n * n);              // n x N  (rows < n of L_g)
+  float2* Gf = reinterpret_cast<float2*>(Rd + n * N);     // n x N
+  float2* M2f = Gf + n * N;                               // N x N, transposed
+  float2* GLf = M2f + N * N;                              // n x N
+  float* Lf = reinterpret_cast<float*>(GLf + n * N);      // N x N
+  ff* Lc = reinterpret_cast<ff*>(Lf + N * N + ((N * N) & 1));  // N x n: lci1_g
   for (int e = tid; e < n * N; e += nt) {
     const double2 g = green[(size_t)b * n * N + e];
-    Gs[e] = g;
-    Gf[e] = make_float2((float)g.x, (float)g.y);
+    Gs[e] = ffc{ff_from_d(g.x), ff_from_d(g.y)};
+    Gf[e] = make_float2(d2f_bits(g.x), d2f_bits(g.y));
   }
-  for (int e = tid; e < N * N; e += nt) {
+  for (int e = tid; e < N * N; e += nt) {  // stored transposed: M2f[i][j] = M2[j][i]
     const double2 m = m2[(size_t)b * N * N + e];
-    M2f[e] = make_float2((float)m.x, (float)m.y);
+    const int j = e / N, i = e % N;
+    M2f[i * N + j] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
   }
-  for (int e = tid; e < n * n; e += nt) C1[e] = ci1g1[(size_t)b * n * n + e];
-  double2 s0 = cmk(0.0, 0.0), s1 = cmk(0.0, 0.0), s2 = cmk(0.0, 0.0), s3 = cmk(0.0, 0.0);
+  for (int e = tid; e < n * n; e += nt) {
+    const double2 c = ci1g1[(size_t)b * n * n + e];
+    C1[e] = ffc{ff_from_d(c.x), ff_from_d(c.y)};
+  }
+  const ffc z{{0.f, 0.f}, {0.f, 0.f}};
+  ffc s0 = z, s1 = z, s2 = z, s3 = z;
   const int g0 = chunk * kCisdGChunk, g1 = min(G, g0 + kCisdGChunk);
   for (int gg = g0; gg < g1; ++gg) {
     __syncthreads();
     const double* Lg = chol + (size_t)gg * N * N;
     for (int e = tid; e < N * N; e += nt) {
       const double l = Lg[e];
-      Lf[e] = (float)l;
-      if (e < n * N) Rd[e] = l;
+      Lf[e] = d2f_bits(l);
+      if (e < n * N) Rd[e] = ff_from_d(l);
     }
+    const double* lc = lci1 + (size_t)gg * N * n;
+    for (int e = tid; e < N * n; e += nt) Lc[e] = ff_from_d(lc[e]);
     __syncthreads();
-    for (int e = tid; e < n * n; e += nt) {
+    for (int e = tid; e < n * n; e += nt) {  // lg1[p][q] = sum_j R[p][j] G[q][j]
       const int p = e / n, q = e % n;
-      double2 a = cmk(0.0, 0.0);
-      for (int j = 0; j < N; ++j) crfma(a, Rd[p * N + j], Gs[q * N + j]);
-      A[e] = a;
+      ffc a = z;
+      for (int j = 0; j < N; ++j) {
+        const ff r = Rd[p * N + j];
+        const ffc g = Gs[q * N + j];
+        ff_mad(a.re, r, g.re);
+        ff_mad(a.im, r, g.im);
+      }
+      A[e] = ffc_norm(a);
     }
     for (int e = tid; e < n * N; e += nt) {
       const int p = e / N, i = e % N;
@@ -317,30 +344,38 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
       GLf[e] = make_float2(ar, ai);
     }
     __syncthreads();
-    const double* lc = lci1 + (size_t)gg * N * n;
     for (int e = tid; e < n * n; e += nt) {
       const int p = e / n, q = e % n;
-      cfma(s0, A[p * n + q], A[q * n + p]);
-      double2 t = cmk(0.0, 0.0);
-      for (int a2 = 0; a2 < n; ++a2) cfma(t, A[q * n + a2], C1[a2 * n + p]);
-      cfma(s1, A[p * n + q], t);
-      double2 bq = cmk(0.0, 0.0);
-      for (int i = 0; i < N; ++i) crfma(bq, lc[i * n + q], Gs[p * N + i]);
-      cfma(s2, bq, A[p * n + q]);
+      const ffc apq = A[p * n + q];
+      ffc_mad(s0, apq, A[q * n + p]);
+      ffc t = z;
+      for (int a2 = 0; a2 < n; ++a2) ffc_mad(t, A[q * n + a2], C1[a2 * n + p]);
+      ffc_mad(s1, apq, ffc_norm(t));
+      ffc bq = z;  // lci1g[q][p] = sum_i lci1[i][q] G[p][i]
+      for (int i = 0; i < N; ++i) {
+        const ff l = Lc[i * n + q];
+        const ffc g = Gs[p * N + i];
+        ff_mad(bq.re, l, g.re);
+        ff_mad(bq.im, l, g.im);
+      }
+      ffc_mad(s2, ffc_norm(bq), apq);
     }
     for (int e = tid; e < n * N; e += nt) {
       const int p = e / N, j = e % N;
       float ar = 0.f, ai = 0.f;
       for (int i = 0; i < N; ++i) {
         const float l = Lf[p * N + i];
-        const float2 m = M2f[j * N + i];
+        const float2 m = M2f[i * N + j];  // consecutive j across the warp
         ar = fmaf(l, m.x, ar);
         ai = fmaf(l, m.y, ai);
       }
       const float2 gl = GLf[e];
-      s3.x += (double)gl.x * ar - (double)gl.y * ai;
-      s3.y += (double)gl.x * ai + (double)gl.y * ar;
+      ffc_mad(s3, ffc{ff{gl.x, 0.f}, ff{gl.y, 0.f}}, ffc{ff{ar, 0.f}, ff{ai, 0.f}});
     }
+    s0 = ffc_norm(s0);
+    s1 = ffc_norm(s1);
+    s2 = ffc_norm(s2);
+    s3 = ffc_norm(s3);
     double2* xo = xg + ((size_t)b * G + gg) * n * v;
     for (int e = tid; e < n * v; e += nt) {
       const int p = e / v, t = e % v;
@@ -351,16 +386,16 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
         ar = fmaf(a.x, x.x, fmaf(-a.y, x.y, ar));
         ai = fmaf(a.x, x.y, fmaf(a.y, x.x, ai));
       }
-      xo[e] = cmk(ar, ai);
+      xo[e] = make_double2(f2d_bits(ar), f2d_bits(ai));
     }
   }
-  s0 = block_sum2(s0, red);
-  s1 = block_sum2(s1, red);
-  s2 = block_sum2(s2, red);
-  s3 = block_sum2(s3, red);
+  double2 d0 = block_sum2(ffc_d(s0), red);
+  double2 d1 = block_sum2(ffc_d(s1), red);
+  double2 d2 = block_sum2(ffc_d(s2), red);
+  double2 d3 = block_sum2(ffc_d(s3), red);
   if (tid == 0) {
     double2* o = gpart + ((size_t)b * nchunk + chunk) * 4;
-    o[0] = s0; o[1] = s1; o[2] = s2; o[3] = s3;
+    o[0] = d0; o[1] = d1; o[2] = d2; o[3] = d3;
   }
 }
 
@@ -511,7 +546,8 @@ static size_t cisd_gamma_smem(int N, int n) {
 
 static size_t cisd_gamma_f32_smem(int N, int n) {
   return (size_t)(n * N + 2 * n * n) * sizeof(double2) + (size_t)n * N * sizeof(double) +
-         (size_t)(2 * n * N + N * N) * sizeof(float2) + (size_t)N * N * sizeof(float);
+         (size_t)(2 * n * N + N * N) * sizeof(float2) + (size_t)(N * N + ((N * N) & 1)) * sizeof(float) +
+         (size_t)N * n * 8;  // + lci1_g in float-float
 }
 
 // need_ham: the force bias / energy / step also read h1, chol and lci1

@@ -10,6 +10,7 @@
 
 #include <algorithm>
 
+#include "ff.cuh"
 #include "mixed.h"
 #include "profile.h"
 #include "step_tail.cuh"
@@ -17,88 +18,11 @@
 
 namespace trot {
 
-// ------------------------------------------------------------------ float-float
-struct ff { float hi, lo; };
-// The error-free transformations below rely on the rounded value of every sum and
-// product, so they use the _rn intrinsics, which the compiler never contracts into FMAs.
-TROT_D ff ff_two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
-  return ff{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
-}
-TROT_D ff ff_fast(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  return ff{s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-TROT_D ff ff_add(ff x, ff y) {
-  ff s = ff_two_sum(x.hi, y.hi);
-  return ff_fast(s.hi, __fadd_rn(__fadd_rn(s.lo, x.lo), y.lo));
-}
-TROT_D ff ff_sub(ff x, ff y) { return ff_add(x, ff{-y.hi, -y.lo}); }
-TROT_D ff ff_mul(ff x, ff y) {
-  const float p = __fmul_rn(x.hi, y.hi);
-  float e = fmaf(x.hi, y.hi, -p);
-  e = fmaf(x.hi, y.lo, e);
-  e = fmaf(x.lo, y.hi, e);
-  return ff_fast(p, e);
-}
-// float -> double by moving the bits (exact for normal floats; zero, subnormal, inf and
-// NaN take the conversion instruction)
-TROT_D double f2d_bits(float f) {
-  const unsigned v = (unsigned)__float_as_int(f);
-  const unsigned e = (v >> 23) & 0xFFu;
-  if (e == 0u || e == 0xFFu) return (double)f;
-  const unsigned long long d = ((unsigned long long)(v & 0x80000000u) << 32) |
-                               ((unsigned long long)(e - 127u + 1023u) << 52) |
-                               ((unsigned long long)(v & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)d);
-}
-TROT_D double ff_d(ff x) { return f2d_bits(x.hi) + f2d_bits(x.lo); }
-// 2^e as a float for e in [-126, 127] (exact; the exponents here stay far inside)
-TROT_D float pow2f(int e) { return __int_as_float((e + 127) << 23); }
-TROT_D ff ff_shfl_xor(ff x, int o) {
-  return ff{__shfl_xor_sync(0xffffffffu, x.hi, o), __shfl_xor_sync(0xffffffffu, x.lo, o)};
-}
-// acc += a b (float-float operands): exact product of the high parts (TwoProd) plus
-// the cross terms; the high parts are summed with TwoSum and the low parts in plain
-// FP32, renormalised once by the caller (ff_fast) after at most a few dozen terms.
-TROT_D void ff_mad(ff& acc, ff a, ff b) {
-  const float p = __fmul_rn(a.hi, b.hi);
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, e);
-  e = fmaf(a.lo, b.hi, e);
-  const ff t = ff_two_sum(acc.hi, p);
-  acc.hi = t.hi;
-  acc.lo = __fadd_rn(acc.lo, __fadd_rn(t.lo, e));
-}
-
 // ------------------------------------------------------------------ Green's functions in float-float
 // Same quantities as green_kernel (green.cu): M_s = C_s^T w_s, M_s^{-1} by
 // FP64 Gauss-Jordan, G_s = (w_s M_s^{-1})^T and e1 = sum_s mult_s sum G_s o rot_h1_s,
 // with the two N x n^2 products in float-float (FP32 pairs, ~2^-44 relative)
 // on the FP32 pipe instead of FP64.  One CTA per walker.
-struct ffc { ff re, im; };
-// Split a double into float-float with integer operations only (conversions and
-// double arithmetic run on the FP64 pipe, a few operations per clock per SM on this
-// GPU): hi = the top 24 significant bits (truncated), lo = the next 29 bits rounded to
-// a float, so hi + lo = x to 2^-48 relative.  Values below 2^-126 give 0; values past
-// the float range give inf; NaN and inf pass through.
-TROT_D ff ff_from_d(double x) {
-  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
-  const unsigned sign = (unsigned)(u >> 32) & 0x80000000u;
-  const int ex = (int)((u >> 52) & 0x7FF);
-  if (ex == 0x7FF) return ff{__double2float_rn(x), 0.f};
-  const int ef = ex - 1023 + 127;
-  if (ex == 0 || ef <= 0) return ff{__int_as_float((int)sign), 0.f};
-  if (ef >= 255) return ff{__int_as_float((int)(sign | 0x7F800000u)), 0.f};
-  const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
-  const float hi = __int_as_float((int)(sign | ((unsigned)ef << 23) | (unsigned)(m >> 29)));
-  const float r = __uint2float_rn((unsigned)(m & 0x1FFFFFFFull));
-  const int sc = ex - 1075;  // rem * 2^(ex - 1023 - 52)
-  float lo = sc >= -126 ? r * pow2f(sc) : ldexpf(r, sc);
-  return ff{hi, sign ? -lo : lo};
-}
-TROT_D ff ff_fma(ff acc, ff a, ff b) { return ff_add(acc, ff_mul(a, b)); }
-
 __global__ void __launch_bounds__(256)
 green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* __restrict__ wb,
                 double2* __restrict__ green, double2* __restrict__ e1_out) {
