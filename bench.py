@@ -359,7 +359,8 @@ def adjoint_leg(chol_scale=0.1, seed=11):
     params = tg.QmcParams(dt=dt, n_exp_terms=6, n_prop_steps=spb, n_walkers=W)
     trial = tg.RhfTrial(mo)
     one = adjoint.as_problem(h0, chol, trial, params, fields[:, :1].contiguous(), steps_per_block=spb)
-    e0 = float(adjoint.LocalEnergy.apply(one.walkers0, torch.as_tensor(h1).cuda(), one)[0])
+    e0 = float(adjoint.LocalEnergy.apply(one.walkers0, torch.empty(0, dtype=torch.complex128, device="cuda"),
+                                         torch.as_tensor(h1).cuda(), one)[0])
     prob = adjoint.as_problem(h0, chol, trial, params, fields, e_estimate0=e0, steps_per_block=spb)
     adjoint.energy(h1, prob)  # warm-up (first launches, workspaces)
     torch.cuda.synchronize()

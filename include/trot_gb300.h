@@ -368,40 +368,46 @@ int trot_cisd_lci1(int norb, int nchol, int nocc, const double* ci1, const doubl
                    void* stream);
 
 /* ---------------------------------------------------------------- adjoint (reverse mode)
- * Hand-written vector-Jacobian products for an RHF trial with restricted
- * walkers (TROT_RHF_R) in FP64; other kinds return TROT_ERR_UNSUPPORTED.  The
- * reference has no adjoint: these differentiate its forward formulas
- * (trot/prop/afqmc.py:91-144, trot/meas/rhf.py:21-60,128-138,
- * trot/trial/rhf.py:45-47, trot/walkers.py:137-179) so that gradients of an
- * energy estimator with respect to h1 come out of one run.  Cotangents of a
- * real objective J: g_z = dJ/dRe z + i dJ/dIm z for complex z (complex128
- * arrays), dJ/dz for real z.  Workspace: trot_vjp_workspace_size(sys, op)
- * with op TROT_OP_PROP_STEP, TROT_OP_LOCAL_ENERGY or TROT_OP_OVERLAP.
+ * Hand-written vector-Jacobian products in FP64 for TROT_RHF_R, TROT_RHF_U and
+ * TROT_UHF_U (precision TROT_MIXED returns TROT_ERR_UNSUPPORTED).  The reference
+ * has no adjoint: these differentiate its forward formulas
+ * (trot/prop/afqmc.py:91-144, trot/meas/rhf.py:21-60,128-172,
+ * trot/meas/uhf.py:205-231, trot/trial/rhf.py:45-54, trot/trial/uhf.py:54-58,
+ * trot/walkers.py:137-179) so that gradients of an energy estimator with
+ * respect to h1 come out of one run.  Cotangents of a real objective J:
+ * g_z = dJ/dRe z + i dJ/dIm z for complex z (complex128 arrays laid out like
+ * z), dJ/dz for real z; *_b arguments are ignored for TROT_RHF_R.  Workspace:
+ * trot_vjp_workspace_size(sys, op) with op TROT_OP_PROP_STEP,
+ * TROT_OP_LOCAL_ENERGY or TROT_OP_OVERLAP.
  *
- * trot_prop_step_vjp: given the state BEFORE the step (in), the step's fields
- * and the cotangents of the state after it (walkers, weights (may be NULL),
- * overlaps (may be NULL), scalars [E_shift, e_estimate]), writes the
+ * trot_prop_step_vjp: given the state BEFORE the step (state_in), the step's
+ * fields and the cotangents of the state after it (walkers, weights (may be
+ * NULL), overlaps (may be NULL), scalars [E_shift, e_estimate]), writes the
  * cotangents of the state before it and adds dJ/d exp_h1_half (N x N) into
- * g_exp_h1_half.  The forward step is recomputed inside; weights that the
- * step's floor / cap / non-finite guards set to zero pass no gradient.
+ * g_exp_h1_half.  The forward step is recomputed inside; walkers that the
+ * step's floor / cap / non-finite guards (or a zero weight) remove from the
+ * objective get exactly zero cotangents.
  * trot_local_energy_vjp: adds g_energy[b] * d Re E_L[b] / d walkers into
  * g_walkers and sum_b g_energy[b] d Re E_L[b] / d h1 (through rot_h1 = C^T h1)
  * into g_h1 (N x N).
- * trot_overlap_vjp: adds the cotangent of det(C^T w)^2 into g_walkers.
- * trot_orthonormalize_vjp: g_walkers = g_q (w^H q)^-1 for q the orthonormalised
+ * trot_overlap_vjp: adds the cotangent of prod_s det(C_s^T w_s)^mult_s into g_walkers.
+ * trot_orthonormalize_vjp: g_w = g_q (w^H q)^-1 per spin for q the orthonormalised
  * walkers (everything downstream is invariant under q -> q M). */
 size_t trot_vjp_workspace_size(const trot_system* sys, int op);
 int trot_prop_step_vjp(const trot_system* sys, const trot_state* state_in, const double* fields,
-                       const double* g_walkers_out, const double* g_weights_out, const double* g_overlaps_out,
-                       const double* g_scalars_out, double* g_walkers_in, double* g_weights_in,
-                       double* g_overlaps_in, double* g_scalars_in, double* g_exp_h1_half, void* workspace,
-                       size_t workspace_bytes, void* stream);
-int trot_local_energy_vjp(const trot_system* sys, const double* walkers, const double* g_energy,
-                          double* g_walkers, double* g_h1, void* workspace, size_t workspace_bytes, void* stream);
-int trot_overlap_vjp(const trot_system* sys, const double* walkers, const double* g_overlaps, double* g_walkers,
-                     void* workspace, size_t workspace_bytes, void* stream);
-int trot_orthonormalize_vjp(const trot_system* sys, const double* walkers, const double* walkers_q,
-                            const double* g_q, double* g_walkers, void* stream);
+                       const double* g_walkers_out_a, const double* g_walkers_out_b, const double* g_weights_out,
+                       const double* g_overlaps_out, const double* g_scalars_out, double* g_walkers_in_a,
+                       double* g_walkers_in_b, double* g_weights_in, double* g_overlaps_in, double* g_scalars_in,
+                       double* g_exp_h1_half, void* workspace, size_t workspace_bytes, void* stream);
+int trot_local_energy_vjp(const trot_system* sys, const double* walkers_a, const double* walkers_b,
+                          const double* g_energy, double* g_walkers_a, double* g_walkers_b, double* g_h1,
+                          void* workspace, size_t workspace_bytes, void* stream);
+int trot_overlap_vjp(const trot_system* sys, const double* walkers_a, const double* walkers_b,
+                     const double* g_overlaps, double* g_walkers_a, double* g_walkers_b, void* workspace,
+                     size_t workspace_bytes, void* stream);
+int trot_orthonormalize_vjp(const trot_system* sys, const double* walkers_a, const double* walkers_b,
+                            const double* q_a, const double* q_b, const double* g_q_a, const double* g_q_b,
+                            double* g_walkers_a, double* g_walkers_b, void* stream);
 
 /* Adjoint of the propagation context's exp(-dt/2 h1_eff) with respect to h1:
  * adds the Frechet-derivative adjoint of expm applied to g_exp_h1_half, times

@@ -21,17 +21,28 @@ def _cuda():
         pytest.skip("no CUDA device")
 
 
-def _problem(N=12, n=3, G=20, W=6, T=8, spb=4, dt=0.01, noise=0.05, seed=4):
+def _problem(N=12, n=3, G=20, W=6, T=8, spb=4, dt=0.01, noise=0.05, seed=4, kind="rhf_r", nb=None):
+    """A small system; kind rhf_r (walkers (W, N, n)), rhf_u or uhf_u (walkers (wa, wb))."""
     import trot_gb300 as tg
     from trot_gb300 import adjoint, synthetic
 
-    ss = synthetic.make_system(N, (n, n), G, decay=30.0, seed=seed, h0=0.3)
+    nb = n if nb is None else nb
+    ss = synthetic.make_system(N, (n, nb if kind == "uhf_u" else n), G, decay=30.0, seed=seed, h0=0.3)
     rng = np.random.default_rng(seed + 1)
     fields = rng.standard_normal((T, W, G))
-    w0 = synthetic.perturbed_walkers(ss.mo_a, W, noise, seed + 2)
     params = tg.QmcParams(dt=dt, n_exp_terms=6, n_prop_steps=spb, n_walkers=W)
-    prob = adjoint.as_problem(ss.h0, ss.chol, tg.RhfTrial(ss.mo_a), params, torch.as_tensor(fields).cuda(),
-                              walkers0=torch.as_tensor(w0).cuda(), e_estimate0=-2.0, steps_per_block=spb)
+    if kind == "rhf_r":
+        w0 = synthetic.perturbed_walkers(ss.mo_a, W, noise, seed + 2)
+        trial, walkers = tg.RhfTrial(ss.mo_a), torch.as_tensor(w0).cuda()
+    else:
+        mo_b = ss.mo_b if kind == "uhf_u" else ss.mo_a
+        w0 = (synthetic.perturbed_walkers(ss.mo_a, W, noise, seed + 2),
+              synthetic.perturbed_walkers(mo_b, W, noise, seed + 3))
+        trial = tg.UhfTrial(ss.mo_a, mo_b) if kind == "uhf_u" else tg.RhfTrial(ss.mo_a)
+        walkers = (torch.as_tensor(w0[0]).cuda(), torch.as_tensor(w0[1]).cuda())
+    prob = adjoint.as_problem(ss.h0, ss.chol, trial, params, torch.as_tensor(fields).cuda(), walkers0=walkers,
+                              e_estimate0=-2.0, steps_per_block=spb,
+                              walker_kind="restricted" if kind == "rhf_r" else "unrestricted")
     return ss, fields, w0, prob
 
 
@@ -69,13 +80,15 @@ def test_step_vjp():
     W = w0.shape[0]
     dev = lambda x: x.cuda().requires_grad_(True)
     w = dev(_c(w0))
+    wb = torch.empty(0, dtype=torch.complex128, device="cuda", requires_grad=True)
     wt = dev(torch.linspace(0.5, 1.5, W, dtype=torch.float64))
     ov = dev(twin.overlap(_c(w0), _c(ss.mo_a)).detach())
     scal = dev(torch.tensor([-1.7, -2.1], dtype=torch.float64))
     h1 = torch.as_tensor(ss.h1).cuda()
     eh = dev(adjoint.ExpH1Half.apply(h1, prob).detach())
     x = torch.as_tensor(fields[0]).cuda()
-    outs = adjoint.Step.apply(w, wt, ov, scal, eh, x, prob)
+    wa_o, _, wt_o, ov_o, sc_o = adjoint.Step.apply(w, wb, wt, ov, scal, eh, x, prob)
+    outs = (wa_o, wt_o, ov_o, sc_o)
     gs = [_rand_like(o.detach().cpu(), 10 + i) for i, o in enumerate(outs)]
     grads = torch.autograd.grad(outs, (w, wt, ov, scal, eh), [g.cuda() for g in gs])
 
@@ -102,14 +115,56 @@ def test_step_vjp():
     assert rel(grads[4].cpu().numpy(), ref[5].numpy()) < 1e-9
 
 
+@pytest.mark.parametrize("kind", ["rhf_u", "uhf_u"])
+def test_step_vjp_unrestricted(kind):
+    from trot_gb300 import adjoint
+
+    ss, fields, w0, prob = _problem(kind=kind, nb=2)
+    W = w0[0].shape[0]
+    dev = lambda x: x.cuda().requires_grad_(True)
+    wa, wb = dev(_c(w0[0])), dev(_c(w0[1]))
+    mo = (_c(prob.mo[0].cpu()), _c(prob.mo[1].cpu()))
+    kind_t = kind
+    mo_t = mo if kind == "uhf_u" else mo[0]
+    ov0 = twin._overlap_k((_c(w0[0]), _c(w0[1])), mo_t, kind_t).detach()
+    wt = dev(torch.linspace(0.5, 1.5, W, dtype=torch.float64))
+    ov = dev(ov0)
+    scal = dev(torch.tensor([-1.7, -2.1], dtype=torch.float64))
+    eh = dev(adjoint.ExpH1Half.apply(torch.as_tensor(ss.h1).cuda(), prob).detach())
+    x = torch.as_tensor(fields[0]).cuda()
+    outs = adjoint.Step.apply(wa, wb, wt, ov, scal, eh, x, prob)
+    gs = [_rand_like(o.detach().cpu(), 20 + i) for i, o in enumerate(outs)]
+    grads = torch.autograd.grad(outs, (wa, wb, wt, ov, scal, eh), [g.cuda() for g in gs])
+    cwa, cwb = _c(w0[0]).requires_grad_(True), _c(w0[1]).requires_grad_(True)
+    cwt, cov = wt.detach().cpu().requires_grad_(True), ov0.clone().requires_grad_(True)
+    ces = torch.tensor(-1.7, dtype=torch.float64, requires_grad=True)
+    cee = torch.tensor(-2.1, dtype=torch.float64, requires_grad=True)
+    ceh = eh.detach().cpu().requires_grad_(True)
+    rot = lambda m: torch.einsum("pi,gpj->gij", m, _c(ss.chol))
+    rot_chol = (rot(mo[0]), rot(mo[1])) if kind == "uhf_u" else rot(mo[0])
+    wn, wtn, ovn, esn = twin.step((cwa, cwb), cwt, cov, ces, cee, _c(fields[0]), mo=mo_t, rot_chol=rot_chol,
+                                  chol=_c(ss.chol), mf_im=prob.mf_im.cpu(), h0_prop=prob.h0_prop, eh=ceh,
+                                  dt=prob.params.dt, n_terms=6, kind=kind)
+    assert rel(outs[0].detach().cpu().numpy(), wn[0].detach().numpy()) < 1e-12
+    assert rel(outs[1].detach().cpu().numpy(), wn[1].detach().numpy()) < 1e-12
+    loss = sum(torch.sum((g.conj() * o).real) if o.is_complex() else torch.sum(g * o)
+               for g, o in zip(gs, (wn[0], wn[1], wtn, ovn, torch.stack([esn, cee]))))
+    ref = torch.autograd.grad(loss, (cwa, cwb, cwt, cov, ces, cee, ceh))
+    for k in range(4):
+        assert rel(grads[k].cpu().numpy(), ref[k].numpy()) < 1e-9, k
+    assert rel(grads[4].cpu().numpy(), np.array([ref[4].item(), ref[5].item()])) < 1e-9
+    assert rel(grads[5].cpu().numpy(), ref[6].numpy()) < 1e-9
+
+
 def test_local_energy_overlap_qr_vjp():
     from trot_gb300 import adjoint
 
     ss, _, w0, prob = _problem(N=14, n=4, G=24, W=5)
     w = torch.as_tensor(w0).cuda().requires_grad_(True)
     h1 = torch.as_tensor(ss.h1).cuda().requires_grad_(True)
-    e = adjoint.LocalEnergy.apply(w, h1, prob)
-    ov = adjoint.Overlap.apply(w, prob)
+    e0 = torch.empty(0, dtype=torch.complex128, device="cuda")
+    e = adjoint.LocalEnergy.apply(w, e0, h1, prob)
+    ov = adjoint.Overlap.apply(w, e0, prob)
     ge = _rand_like(e.detach().cpu(), 3)
     gov = _rand_like(ov.detach().cpu(), 4)
     gw, gh1 = torch.autograd.grad((e, ov), (w, h1), (ge.cuda(), gov.cuda()))
@@ -125,23 +180,26 @@ def test_local_energy_overlap_qr_vjp():
     assert rel(gh1.cpu().numpy(), rh1.numpy()) < 1e-9
     # QR: the energy is invariant under w -> w R, so E(qr(w)) has the gradient of E(w)
     w2 = torch.as_tensor(w0).cuda().requires_grad_(True)
-    e2 = adjoint.LocalEnergy.apply(adjoint.Orthonormalize.apply(w2, prob), h1.detach(), prob)
+    q2, _ = adjoint.Orthonormalize.apply(w2, e0, prob)
+    e2 = adjoint.LocalEnergy.apply(q2, e0, h1.detach(), prob)
     (gq,) = torch.autograd.grad(e2, w2, ge.cuda())
     w3 = torch.as_tensor(w0).cuda().requires_grad_(True)
-    e3 = adjoint.LocalEnergy.apply(w3, h1.detach(), prob)
+    e3 = adjoint.LocalEnergy.apply(w3, e0, h1.detach(), prob)
     (gd,) = torch.autograd.grad(e3, w3, ge.cuda())
     assert rel(gq.cpu().numpy(), gd.cpu().numpy()) < 1e-9
 
 
-@pytest.mark.parametrize("spb,T", [(4, 8), (3, 9)])
-def test_mixed_energy_gradient(spb, T):
+@pytest.mark.parametrize("kind,spb,T", [("rhf_r", 4, 8), ("rhf_r", 3, 9), ("rhf_u", 4, 8), ("uhf_u", 4, 8)])
+def test_mixed_energy_gradient(kind, spb, T):
     """Whole run (steps, QR, overlaps, energies, clamps, e_estimate updates, checkpointed blocks)."""
     from trot_gb300 import adjoint
 
-    ss, fields, w0, prob = _problem(T=T, spb=spb)
+    ss, fields, w0, prob = _problem(T=T, spb=spb, kind=kind, nb=2)
     J, g = adjoint.energy_and_grad(ss.h1, prob)
-    kw = dict(h0=ss.h0, chol=_c(ss.chol), mo=_c(ss.mo_a), rdm1=prob.rdm1.cpu(), fields=_c(fields),
-              walkers0=_c(w0), e_estimate0=-2.0, steps_per_block=spb, dt=prob.params.dt, n_terms=6)
+    mo = (_c(prob.mo[0].cpu()), _c(prob.mo[1].cpu()))
+    kw = dict(h0=ss.h0, chol=_c(ss.chol), mo=mo if kind == "uhf_u" else mo[0], rdm1=prob.rdm1.cpu(),
+              fields=_c(fields), walkers0=(_c(w0[0]), _c(w0[1])) if kind != "rhf_r" else _c(w0), e_estimate0=-2.0,
+              steps_per_block=spb, dt=prob.params.dt, n_terms=6, kind=kind)
     h1c = _c(ss.h1).clone().requires_grad_(True)
     Jc = twin.mixed_energy(h1c, **kw)
     (gc,) = torch.autograd.grad(Jc, h1c)
@@ -165,16 +223,16 @@ def test_checkpointing_is_exact():
     assert torch.equal(g1, g2)
 
 
-def test_adjoint_rejects_other_kinds():
+def test_adjoint_rejects_mixed_precision():
     import ctypes
 
     from trot_gb300 import _lib
 
     _, _, _, prob = _problem()
     s = prob.system()
-    s.kind = _lib.UHF_U
+    s.precision = _lib.MIXED
     assert _lib.load().trot_vjp_workspace_size(ctypes.byref(s), _lib.OP_PROP_STEP) == 0
-    assert b"restricted" in _lib.load().trot_last_error()
+    assert b"FP64" in _lib.load().trot_last_error()
 
 
 def test_dead_walkers_pass_no_gradient():

@@ -116,10 +116,10 @@ _SIGNATURES = {
     "trot_cisd_lci1": (_i, [_i, _i, _i, _p, _p, _p, _p]),
     "trot_vjp_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(TrotSystem), _i]),
     "trot_prop_step_vjp": (_i, [ctypes.POINTER(TrotSystem), ctypes.POINTER(TrotState), _p, _p, _p, _p, _p, _p, _p,
-                                _p, _p, _p, _p, ctypes.c_size_t, _p]),
-    "trot_local_energy_vjp": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
-    "trot_overlap_vjp": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p, ctypes.c_size_t, _p]),
-    "trot_orthonormalize_vjp": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p, _p]),
+                                _p, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
+    "trot_local_energy_vjp": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
+    "trot_overlap_vjp": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
+    "trot_orthonormalize_vjp": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p, _p, _p, _p, _p, _p]),
     "trot_prop_ctx_vjp_workspace_size": (ctypes.c_size_t, [_i, _i]),
     "trot_prop_ctx_vjp": (_i, [_i, _i, _d, _p, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
     "trot_set_tuning": (_i, [_i, _i]),

@@ -20,6 +20,8 @@
 //             g_V = sum_l s_l (V^l x)^H,  s_l = sum_{j <= K-1-l} conj(c_{j+l+1}) (V^H)^j g_y
 //   weights:  imp_ph = exp(Re q) Re(rho e^{ic}), rho = ov'/ov,
 //             q = -sqrt(dt) st + ft + dt (E_shift + h0_prop), c = -sqrt(dt) Re(sum xs m)
+#include <algorithm>
+
 #include "kernels.h"
 
 namespace trot {
@@ -127,11 +129,13 @@ __global__ void adj_green_kernel(int N, int n, const double* __restrict__ C, con
   if (tid == 0) det[b] = d;
 }
 
-// g_w[p][j] += kappa_b sum_i C[p][i] conj(P[j][i])   (overlap det(O)^2, kappa = 2 conj(ov) g_ov)
-__global__ void adj_overlap_kernel(int N, int n, const double* __restrict__ C, const double2* __restrict__ P,
-                                   const double2* __restrict__ kappa, double2* __restrict__ gw) {
+// g_w[p][j] += mult kappa_b sum_i C[p][i] conj(P[j][i]) for ov = prod_s det(O_s)^mult_s,
+// kappa = conj(ov) g_ov (d ov / d w_s = mult_s ov (C_s P_s^T))
+__global__ void adj_overlap_kernel(int N, int n, double mult, const double* __restrict__ C,
+                                   const double2* __restrict__ P, const double2* __restrict__ kappa,
+                                   double2* __restrict__ gw) {
   const int b = blockIdx.x;
-  const double2 kb = kappa[b];
+  const double2 kb = cscale(kappa[b], mult);
   const double2* Pb = P + (size_t)b * n * n;
   for (int e = threadIdx.x; e < N * n; e += blockDim.x) {
     const int p = e / n, j = e % n;
@@ -145,14 +149,24 @@ __global__ void adj_overlap_kernel(int N, int n, const double* __restrict__ C, c
   }
 }
 
-// kappa_b = 2 conj(ov_b) g_ov_b with ov = det^2
-__global__ void adj_kappa_kernel(int W, const double2* __restrict__ det, const double2* __restrict__ gov,
+// kappa_b = conj(ov_b) g_ov_b (zero for a zero cotangent)
+__global__ void adj_kappa_kernel(int W, const double2* __restrict__ ov, const double2* __restrict__ gov,
                                  double2* __restrict__ kappa) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= W) return;
-  const double2 ov = cmul(det[b], det[b]);
-  const double2 g = gov[b];
-  kappa[b] = (g.x == 0.0 && g.y == 0.0) ? cmk(0.0, 0.0) : cscale(cmul(cmk(ov.x, -ov.y), g), 2.0);
+  const double2 o = ov[b], g = gov[b];
+  kappa[b] = (g.x == 0.0 && g.y == 0.0) ? cmk(0.0, 0.0) : cmul(cmk(o.x, -o.y), g);
+}
+
+// ov = prod_s det_s^mult_s (up to two spins; det1 may be null)
+__global__ void adj_ov_kernel(int W, const double2* __restrict__ det0, int m0, const double2* __restrict__ det1, int m1,
+                              double2* __restrict__ ov) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= W) return;
+  double2 o = det0[b];
+  if (m0 == 2) o = cmul(o, o);
+  if (det1) o = cmul(o, m1 == 2 ? cmul(det1[b], det1[b]) : det1[b]);
+  ov[b] = o;
 }
 
 // g_w += (g_Gt - C X) P^H with X = Gt^H g_Gt (n x n); Gt = G^T, g_Gt = g_G^T.
@@ -334,15 +348,14 @@ __device__ __forceinline__ double imp_forward(const StepScalars& s, double* E_ou
 }
 
 // weights after the step (for the population-control mean)
-__global__ void adj_step_fwd_kernel(int W, const double2* __restrict__ ov_old, const double2* __restrict__ det_new,
+__global__ void adj_step_fwd_kernel(int W, const double2* __restrict__ ov_old, const double2* __restrict__ ov_new,
                                     const double2* __restrict__ st, const double2* __restrict__ ft,
                                     const double* __restrict__ wt, const double* __restrict__ scal, double dt,
                                     double sqrt_dt, double h0_prop, double w_floor, double w_cap,
                                     double* __restrict__ wt_new, int* __restrict__ act) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= W) return;
-  StepScalars s{ov_old[b], cmul(det_new[b], det_new[b]), st[b], ft[b], wt[b], scal[0], dt, sqrt_dt, h0_prop,
-                w_floor, w_cap};
+  StepScalars s{ov_old[b], ov_new[b], st[b], ft[b], wt[b], scal[0], dt, sqrt_dt, h0_prop, w_floor, w_cap};
   double E;
   double2 r;
   bool live;
@@ -366,7 +379,7 @@ __global__ void adj_scalar_tail_kernel(const double* __restrict__ g_out, double*
 
 // Per-walker backward of the weight update.  In: g_wt', g_ov', g_scalars' = [g_Es', g_ee'], sum of wt'.
 // Out: g_wt, g_ov (old), kappa' = 2 conj(ov') g_ov'_total, per-walker g_st (real), g_c, g_Req, dt g_Req (for g_Es).
-__global__ void adj_step_bwd_kernel(int W, const double2* __restrict__ ov_old, const double2* __restrict__ det_new,
+__global__ void adj_step_bwd_kernel(int W, const double2* __restrict__ ov_old, const double2* __restrict__ ov_new,
                                     const double2* __restrict__ st, const double2* __restrict__ ft,
                                     const double* __restrict__ wt, const double* __restrict__ scal, double dt,
                                     double sqrt_dt, double h0_prop, double w_floor, double w_cap, double damping,
@@ -376,7 +389,7 @@ __global__ void adj_step_bwd_kernel(int W, const double2* __restrict__ ov_old, c
                                     double* __restrict__ g_req, double* __restrict__ g_c, double* __restrict__ g_es) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= W) return;
-  const double2 ovn = cmul(det_new[b], det_new[b]);
+  const double2 ovn = ov_new[b];
   StepScalars s{ov_old[b], ovn, st[b], ft[b], wt[b], scal[0], dt, sqrt_dt, h0_prop, w_floor, w_cap};
   double E;
   double2 r;
@@ -401,7 +414,7 @@ __global__ void adj_step_bwd_kernel(int W, const double2* __restrict__ ov_old, c
   const double2 rq = cmul(rho, inv_old);
   const bool active = live && wt[b] != 0.0;
   g_ov[b] = active ? cscale(cmul(cmk(rq.x, -rq.y), grho), -1.0) : cmk(0.0, 0.0);
-  kappa[b] = active ? cscale(cmul(cmk(ovn.x, -ovn.y), gov_new), 2.0) : cmk(0.0, 0.0);
+  kappa[b] = active ? cmul(cmk(ovn.x, -ovn.y), gov_new) : cmk(0.0, 0.0);  // times mult_s per spin
   g_req[b] = active ? greq : 0.0;
   g_c[b] = active ? gc : 0.0;
   g_es[b] = active ? dt * greq : 0.0;
@@ -452,15 +465,15 @@ __global__ void adj_block_transpose_kernel(int W, int G, int n, const double2* _
   }
 }
 
-// g_G[b][i][p] = g_E[b] conj(2 rot_h1[i][p] + D[b][i][p])
-__global__ void adj_energy_green_kernel(int W, int n, int N, const double* __restrict__ rot_h1,
+// g_G[b][i][p] = g_E[b] conj(mult rot_h1[i][p] + D[b][i][p])
+__global__ void adj_energy_green_kernel(int W, int n, int N, double mult, const double* __restrict__ rot_h1,
                                         const double2* __restrict__ D, const double* __restrict__ gE,
                                         double2* __restrict__ gG) {
   const size_t per = (size_t)n * N, total = (size_t)W * per;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
     const size_t b = e / per, k = e % per;
     const double2 d = D[e];
-    gG[e] = cscale(cmk(2.0 * rot_h1[k] + d.x, -d.y), gE[b]);
+    gG[e] = cscale(cmk(mult * rot_h1[k] + d.x, -d.y), gE[b]);
   }
 }
 
@@ -475,14 +488,14 @@ __global__ void adj_weighted_green_kernel(int W, int n, int N, const double2* __
   }
 }
 
-// g_h1[q][p] += 2 Re sum_i C[q][i] H[i][p]
-__global__ void adj_h1_direct_kernel(int N, int n, const double* __restrict__ C, const double2* __restrict__ H,
-                                     double* __restrict__ gh1) {
+// g_h1[q][p] += mult Re sum_i C[q][i] H[i][p]
+__global__ void adj_h1_direct_kernel(int N, int n, double mult, const double* __restrict__ C,
+                                     const double2* __restrict__ H, double* __restrict__ gh1) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)N * N; e += (size_t)gridDim.x * blockDim.x) {
     const int q = (int)(e / N), p = (int)(e % N);
     double acc = 0.0;
     for (int i = 0; i < n; ++i) acc += C[(size_t)q * n + i] * H[(size_t)i * N + p].x;
-    gh1[e] += 2.0 * acc;
+    gh1[e] += mult * acc;
   }
 }
 
@@ -495,110 +508,156 @@ __global__ void adj_to_complex_kernel(size_t len, const double* __restrict__ x, 
 static int grid_of(size_t len) { return (int)((len + 255) / 256 < 4096 ? (len + 255) / 256 : 4096); }
 
 // ---------------------------------------------------------------- workspace layouts
+// Spins: TROT_RHF_R has one spin with multiplicity 2; TROT_RHF_U and TROT_UHF_U two spins
+// with multiplicity 1 (RHF_U uses the alpha trial and rotated integrals for both).
 struct AdjCommon {
-  int W, N, n, G, K;
-  size_t wn, nN;
+  int W, N, G, K, nspin;
+  int n[2], mult[2];
+  size_t wn[2], nN[2];
+  const double* mo[2];
+  const double* rot_h1[2];
+  const double* rot_chol[2];
 };
 
 static int check_adj(const trot_system* s) {
   if (!s) { set_error("null system"); return TROT_ERR_NULL_PTR; }
-  if (s->kind != TROT_RHF_R) { set_error("the adjoint supports RHF trials with restricted walkers"); return TROT_ERR_UNSUPPORTED; }
+  if (s->kind != TROT_RHF_R && s->kind != TROT_RHF_U && s->kind != TROT_UHF_U) {
+    set_error("bad kind %d", s->kind);
+    return TROT_ERR_BAD_SHAPE;
+  }
   if (s->precision != TROT_FP64) { set_error("the adjoint runs in FP64"); return TROT_ERR_UNSUPPORTED; }
+  const int nb = s->kind == TROT_RHF_R ? s->nocc_a : s->nocc_b;
   if (s->n_walkers < 1 || s->n_walkers > 65535 || s->norb < 1 || s->nchol < 1 || s->nocc_a < 1 || s->nocc_a > 32 ||
-      s->nocc_a > s->norb) {
-    set_error("bad shape: W %d (<= 65535), N %d, G %d, n %d (n <= 32)", s->n_walkers, s->norb, s->nchol, s->nocc_a);
+      s->nocc_a > s->norb || nb < 1 || nb > 32 || nb > s->norb) {
+    set_error("bad shape: W %d (<= 65535), N %d, G %d, n %d / %d (<= 32)", s->n_walkers, s->norb, s->nchol, s->nocc_a,
+              nb);
     return TROT_ERR_BAD_SHAPE;
   }
   if (s->n_exp_terms < 1 || s->n_exp_terms > 7) { set_error("n_exp_terms %d outside 1..7", s->n_exp_terms); return TROT_ERR_BAD_SHAPE; }
-  if (!s->mo_a) { set_error("null trial"); return TROT_ERR_NULL_PTR; }
+  if (!s->mo_a || (s->kind == TROT_UHF_U && !s->mo_b)) { set_error("null trial"); return TROT_ERR_NULL_PTR; }
   return TROT_OK;
 }
 
 static AdjCommon common_of(const trot_system* s) {
-  AdjCommon a;
-  a.W = s->n_walkers; a.N = s->norb; a.n = s->nocc_a; a.G = s->nchol; a.K = s->n_exp_terms;
-  a.wn = (size_t)a.W * a.N * a.n;
-  a.nN = (size_t)a.n * a.N;
+  AdjCommon a{};
+  a.W = s->n_walkers; a.N = s->norb; a.G = s->nchol; a.K = s->n_exp_terms;
+  const bool uhf = s->kind == TROT_UHF_U;
+  a.nspin = s->kind == TROT_RHF_R ? 1 : 2;
+  for (int q = 0; q < a.nspin; ++q) {
+    a.n[q] = q == 0 ? s->nocc_a : s->nocc_b;
+    a.mult[q] = a.nspin == 1 ? 2 : 1;
+    a.wn[q] = (size_t)a.W * a.N * a.n[q];
+    a.nN[q] = (size_t)a.n[q] * a.N;
+    a.mo[q] = (q == 1 && uhf) ? s->mo_b : s->mo_a;
+    a.rot_h1[q] = (q == 1 && uhf) ? s->rot_h1_b : s->rot_h1_a;
+    a.rot_chol[q] = (q == 1 && uhf) ? s->rot_chol_b : s->rot_chol_a;
+  }
   return a;
 }
 
+struct SpinWs {  // per-spin buffers of the step adjoint
+  double2 *green, *P, *det, *U, *w2, *wnew, *greenn, *Pn, *detn, *gwn, *gw2, *Vv, *S, *gG, *gw1, *wz;
+};
 struct StepWs {
-  double2 *green, *P, *det, *fb, *xs, *st, *ft, *V, *U, *w2, *wnew, *greenn, *Pn, *detn, *Bc;
-  double2 *gwn, *gw2, *Vv, *S, *gV, *gxsv, *gfb, *gG, *gw1, *kappa, *gov_tmp;
+  SpinWs sp[2];
+  double2 *fb, *xs, *st, *ft, *V, *Bc, *gV, *gxsv, *gfb, *kappa, *ov_new;
   double *wt_new, *wsum, *g_req, *g_c, *g_es;
   int* act;
-  double2* wz;
 };
 
 static void carve_step(const AdjCommon& a, Carver& c, StepWs& b) {
   const size_t W = a.W, G = a.G, NN = (size_t)a.N * a.N;
-  b.green = c.take<double2>(W * a.nN);
-  b.P = c.take<double2>(W * a.n * a.n);
-  b.det = c.take<double2>(W);
+  b = StepWs{};
+  for (int q = 0; q < a.nspin; ++q) {
+    SpinWs& x = b.sp[q];
+    const size_t wn = a.wn[q], n = a.n[q];
+    x.green = c.take<double2>(W * a.nN[q]);
+    x.P = c.take<double2>(W * n * n);
+    x.det = c.take<double2>(W);
+    x.U = c.take<double2>((size_t)(a.K + 1) * wn);
+    x.w2 = c.take<double2>(wn);
+    x.wnew = c.take<double2>(wn);
+    x.greenn = c.take<double2>(W * a.nN[q]);
+    x.Pn = c.take<double2>(W * n * n);
+    x.detn = c.take<double2>(W);
+    x.gwn = c.take<double2>(wn);
+    x.gw2 = c.take<double2>(wn);
+    x.Vv = c.take<double2>((size_t)(a.K + 1) * wn);
+    x.S = c.take<double2>((size_t)a.K * wn);
+    x.gG = c.take<double2>(W * a.nN[q]);
+    x.gw1 = c.take<double2>(wn);
+    x.wz = c.take<double2>(wn);
+  }
   b.fb = c.take<double2>(W * G);
   b.xs = c.take<double2>(W * G);
   b.st = c.take<double2>(W);
   b.ft = c.take<double2>(W);
   b.V = c.take<double2>(W * NN);
-  b.U = c.take<double2>((size_t)(a.K + 1) * a.wn);
-  b.w2 = c.take<double2>(a.wn);
-  b.wnew = c.take<double2>(a.wn);
-  b.greenn = c.take<double2>(W * a.nN);
-  b.Pn = c.take<double2>(W * a.n * a.n);
-  b.detn = c.take<double2>(W);
   b.Bc = c.take<double2>(NN);
-  b.gwn = c.take<double2>(a.wn);
-  b.gw2 = c.take<double2>(a.wn);
-  b.Vv = c.take<double2>((size_t)(a.K + 1) * a.wn);
-  b.S = c.take<double2>((size_t)a.K * a.wn);
   b.gV = c.take<double2>(W * NN);
   b.gxsv = c.take<double2>(W * G);
   b.gfb = c.take<double2>(W * G);
-  b.gG = c.take<double2>(W * a.nN);
-  b.gw1 = c.take<double2>(a.wn);
   b.kappa = c.take<double2>(W);
-  b.gov_tmp = c.take<double2>(W);
+  b.ov_new = c.take<double2>(W);
   b.wt_new = c.take<double>(W);
   b.wsum = c.take<double>(1);
   b.g_req = c.take<double>(W);
   b.g_c = c.take<double>(W);
   b.g_es = c.take<double>(W);
   b.act = c.take<int>(W);
-  b.wz = c.take<double2>(a.wn);
 }
 
 struct EnergyWs {
-  double2 *green, *P, *det, *F, *Ft, *c, *D, *gG, *H;
+  double2 *green[2], *P[2], *det, *F, *Ft, *c[2], *ctot, *D, *gG, *H;
   int* act;
 };
 
 static void carve_energy(const AdjCommon& a, Carver& c, EnergyWs& b) {
   const size_t W = a.W, G = a.G;
-  b.green = c.take<double2>(W * a.nN);
-  b.P = c.take<double2>(W * a.n * a.n);
+  b = EnergyWs{};
+  size_t nmax = 0, nNmax = 0;
+  for (int q = 0; q < a.nspin; ++q) {
+    b.green[q] = c.take<double2>(W * a.nN[q]);
+    b.P[q] = c.take<double2>(W * a.n[q] * a.n[q]);
+    b.c[q] = c.take<double2>(W * G);
+    nmax = std::max(nmax, (size_t)a.n[q]);
+    nNmax = std::max(nNmax, a.nN[q]);
+  }
   b.det = c.take<double2>(W);
-  b.F = c.take<double2>(W * a.n * G * a.n);
-  b.Ft = c.take<double2>(W * a.n * G * a.n);
-  b.c = c.take<double2>(W * G);
-  b.D = c.take<double2>(W * a.nN);
-  b.gG = c.take<double2>(W * a.nN);
-  b.H = c.take<double2>(a.nN);
+  b.F = c.take<double2>(W * nmax * G * nmax);
+  b.Ft = c.take<double2>(W * nmax * G * nmax);
+  b.ctot = c.take<double2>(W * G);
+  b.D = c.take<double2>(W * nNmax);
+  b.gG = c.take<double2>(W * nNmax);
+  b.H = c.take<double2>(nNmax);
   b.act = c.take<int>(W);
 }
 
-static int green_launch(const AdjCommon& a, const double* C, const double2* w, double2* green, double2* P,
-                        double2* det, cudaStream_t st) {
-  adj_green_kernel<<<a.W, 256, 0, st>>>(a.N, a.n, C, w, green, P, det);
+static int green_launch(const AdjCommon& a, int q, const double2* w, double2* green, double2* P, double2* det,
+                        cudaStream_t st) {
+  adj_green_kernel<<<a.W, 256, 0, st>>>(a.N, a.n[q], a.mo[q], w, green, P, det);
   TROT_CHECK_LAUNCH("adj_green_kernel");
   return TROT_OK;
 }
 
-static int green_vjp_launch(const AdjCommon& a, const double* C, const double2* green, const double2* ggreen,
-                            const double2* P, double2* gw, cudaStream_t st) {
-  const size_t smem = (size_t)2 * a.n * a.n * sizeof(double2);
-  adj_green_vjp_kernel<<<a.W, 256, smem, st>>>(a.N, a.n, C, green, ggreen, P, gw);
+static int green_vjp_launch(const AdjCommon& a, int q, const double2* green, const double2* ggreen, const double2* P,
+                            double2* gw, cudaStream_t st) {
+  const size_t smem = (size_t)2 * a.n[q] * a.n[q] * sizeof(double2);
+  adj_green_vjp_kernel<<<a.W, 256, smem, st>>>(a.N, a.n[q], a.mo[q], green, ggreen, P, gw);
   TROT_CHECK_LAUNCH("adj_green_vjp_kernel");
   return TROT_OK;
+}
+
+static int ov_launch(const AdjCommon& a, const double2* d0, const double2* d1, double2* ov, cudaStream_t st) {
+  adj_ov_kernel<<<(a.W + 127) / 128, 128, 0, st>>>(a.W, d0, a.mult[0], a.nspin == 2 ? d1 : nullptr,
+                                                    a.nspin == 2 ? a.mult[1] : 0, ov);
+  TROT_CHECK_LAUNCH("adj_ov_kernel");
+  return TROT_OK;
+}
+
+static int dcopy(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
+  return e == cudaSuccess ? TROT_OK : cuda_status(e, "adjoint copy");
 }
 
 }  // namespace trot
@@ -618,10 +677,12 @@ size_t trot_vjp_workspace_size(const trot_system* s, int op) {
     EnergyWs b;
     carve_energy(a, c, b);
   } else if (op == TROT_OP_OVERLAP) {
-    c.take<double2>(a.W * a.nN);
-    c.take<double2>((size_t)a.W * a.n * a.n);
-    c.take<double2>(a.W);
-    c.take<double2>((size_t)2 * a.W);
+    for (int q = 0; q < a.nspin; ++q) {
+      c.take<double2>(a.W * a.nN[q]);
+      c.take<double2>((size_t)a.W * a.n[q] * a.n[q]);
+      c.take<double2>(a.W);
+    }
+    c.take<double2>((size_t)3 * a.W);  // ov, kappa, walker flags
   } else if (op == TROT_OP_QR) {
     return 256;
   } else {
@@ -631,43 +692,46 @@ size_t trot_vjp_workspace_size(const trot_system* s, int op) {
   return c.used + 256;
 }
 
-int trot_prop_step_vjp(const trot_system* s, const trot_state* in, const double* fields, const double* g_walkers_out,
-                       const double* g_weights_out, const double* g_overlaps_out, const double* g_scalars_out,
-                       double* g_walkers_in, double* g_weights_in, double* g_overlaps_in, double* g_scalars_in,
-                       double* g_exp_h1_half, void* ws, size_t ws_bytes, void* stream) {
+int trot_prop_step_vjp(const trot_system* s, const trot_state* in, const double* fields, const double* g_walkers_out_a,
+                       const double* g_walkers_out_b, const double* g_weights_out, const double* g_overlaps_out,
+                       const double* g_scalars_out, double* g_walkers_in_a, double* g_walkers_in_b,
+                       double* g_weights_in, double* g_overlaps_in, double* g_scalars_in, double* g_exp_h1_half,
+                       void* ws, size_t ws_bytes, void* stream) {
   TROT_TRY(check_adj(s));
-  if (!in || !in->walkers_a || !in->weights || !in->overlaps || !in->scalars || !fields || !g_walkers_out ||
-      !g_scalars_out || !g_walkers_in || !g_weights_in || !g_overlaps_in || !g_scalars_in || !g_exp_h1_half || !ws) {
+  const AdjCommon a = common_of(s);
+  const bool two = a.nspin == 2;
+  if (!in || !in->walkers_a || (two && !in->walkers_b) || !in->weights || !in->overlaps || !in->scalars || !fields ||
+      !g_walkers_out_a || (two && !g_walkers_out_b) || !g_scalars_out || !g_walkers_in_a ||
+      (two && !g_walkers_in_b) || !g_weights_in || !g_overlaps_in || !g_scalars_in || !g_exp_h1_half || !ws) {
     set_error("null state, fields, cotangent or workspace");
     return TROT_ERR_NULL_PTR;
   }
-  if (!s->rot_chol_a || !s->exp_h1_half || !s->chol_flat || !s->mf_shifts_im) {
+  if (!a.rot_chol[0] || (two && !a.rot_chol[1]) || !s->exp_h1_half || !s->chol_flat || !s->mf_shifts_im) {
     set_error("null measurement or propagation context");
     return TROT_ERR_NULL_PTR;
   }
-  const AdjCommon a = common_of(s);
   Carver c(ws, ws_bytes);
   StepWs b;
   carve_step(a, c, b);
   if (!c.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, c.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
   cudaStream_t st = (cudaStream_t)stream;
-  const int W = a.W, N = a.N, n = a.n, G = a.G, K = a.K;
+  const int W = a.W, N = a.N, G = a.G, K = a.K;
   const size_t NN = (size_t)N * N;
   const double2 one = cmk(1.0, 0.0), zero = cmk(0.0, 0.0);
-  const double2* w = (const double2*)in->walkers_a;
+  const double2* w[2] = {(const double2*)in->walkers_a, (const double2*)in->walkers_b};
+  const double2* gout[2] = {(const double2*)g_walkers_out_a, (const double2*)g_walkers_out_b};
+  double2* gin[2] = {(double2*)g_walkers_in_a, (double2*)g_walkers_in_b};
   // ---------------- forward recompute
-  TROT_TRY(green_launch(a, s->mo_a, w, b.green, b.P, b.det, st));
-  TROT_TRY(launch_zgemm_cr(W, G, (int)a.nN, 2.0, b.green, (int)a.nN, s->rot_chol_a, (int)a.nN, true, b.fb, G, false,
-                           st));
+  for (int q = 0; q < a.nspin; ++q) {
+    TROT_TRY(green_launch(a, q, w[q], b.sp[q].green, b.sp[q].P, b.sp[q].det, st));
+    // fb = sum_s mult_s R_s . G_s
+    TROT_TRY(launch_zgemm_cr(W, G, (int)a.nN[q], (double)a.mult[q], b.sp[q].green, (int)a.nN[q], a.rot_chol[q],
+                             (int)a.nN[q], true, b.fb, G, q > 0, st));
+  }
   TROT_TRY(launch_fields(W, G, s->sqrt_dt, b.fb, s->mf_shifts_im, fields, b.xs, b.st, b.ft, st));
   TROT_TRY(launch_zgemm_cr(W, (int)NN, G, 1.0, b.xs, G, s->chol_flat, (int)NN, false, b.V, (int)NN, false, st));
   adj_to_complex_kernel<<<grid_of(NN), 256, 0, st>>>(NN, s->exp_h1_half, b.Bc);
   TROT_CHECK_LAUNCH("adj_to_complex_kernel");
-  // u_0 = B w, u_{l+1} = V u_l
-  TROT_TRY(zgemm_batched(W, N, n, N, one, b.Bc, 0, N, 0, w, (long long)N * n, n, 0, zero, b.U, (long long)N * n, n, st));
-  for (int l = 0; l < K; ++l)
-    TROT_TRY(zgemm_batched(W, N, n, N, one, b.V, (long long)NN, N, 0, b.U + (size_t)l * a.wn, (long long)N * n, n, 0,
-                           zero, b.U + (size_t)(l + 1) * a.wn, (long long)N * n, n, st));
   double2 ck[8];
   {  // c_k = (i sqrt(dt))^k / k!
     double2 t = one;
@@ -677,35 +741,46 @@ int trot_prop_step_vjp(const trot_system* s, const trot_state* in, const double*
       ck[k] = t;
     }
   }
-  Comb cb{};
-  cb.nx = K + 1;
-  for (int k = 0; k <= K; ++k) { cb.coef[k] = ck[k]; cb.x[k] = b.U + (size_t)k * a.wn; }
-  TROT_TRY(combine(a.wn, cb, b.w2, false, st));
-  TROT_TRY(zgemm_batched(W, N, n, N, one, b.Bc, 0, N, 0, b.w2, (long long)N * n, n, 0, zero, b.wnew, (long long)N * n,
-                         n, st));
-  TROT_TRY(green_launch(a, s->mo_a, b.wnew, b.greenn, b.Pn, b.detn, st));
+  for (int q = 0; q < a.nspin; ++q) {
+    SpinWs& x = b.sp[q];
+    const int n = a.n[q];
+    const long long sw = (long long)N * n;
+    // u_0 = B w, u_{l+1} = V u_l, w2 = sum_k c_k u_k, w' = B w2
+    TROT_TRY(zgemm_batched(W, N, n, N, one, b.Bc, 0, N, 0, w[q], sw, n, 0, zero, x.U, sw, n, st));
+    for (int l = 0; l < K; ++l)
+      TROT_TRY(zgemm_batched(W, N, n, N, one, b.V, (long long)NN, N, 0, x.U + (size_t)l * a.wn[q], sw, n, 0, zero,
+                             x.U + (size_t)(l + 1) * a.wn[q], sw, n, st));
+    Comb cb{};
+    cb.nx = K + 1;
+    for (int k = 0; k <= K; ++k) { cb.coef[k] = ck[k]; cb.x[k] = x.U + (size_t)k * a.wn[q]; }
+    TROT_TRY(combine(a.wn[q], cb, x.w2, false, st));
+    TROT_TRY(zgemm_batched(W, N, n, N, one, b.Bc, 0, N, 0, x.w2, sw, n, 0, zero, x.wnew, sw, n, st));
+    TROT_TRY(green_launch(a, q, x.wnew, x.greenn, x.Pn, x.detn, st));
+  }
+  TROT_TRY(ov_launch(a, b.sp[0].detn, b.sp[1].detn, b.ov_new, st));
   const int wb = (W + 127) / 128;
-  adj_step_fwd_kernel<<<wb, 128, 0, st>>>(W, (const double2*)in->overlaps, b.detn, b.st, b.ft, in->weights,
+  adj_step_fwd_kernel<<<wb, 128, 0, st>>>(W, (const double2*)in->overlaps, b.ov_new, b.st, b.ft, in->weights,
                                            in->scalars, s->dt, s->sqrt_dt, s->h0_prop, s->weight_floor, s->weight_cap,
                                            b.wt_new, b.act);
   TROT_CHECK_LAUNCH("adj_step_fwd_kernel");
   adj_sum_kernel<<<1, 256, 0, st>>>(W, b.wt_new, b.wsum);
   TROT_CHECK_LAUNCH("adj_sum_kernel");
   // inactive walkers: zero their recomputed data (see adj_zero_inactive_kernel)
-  {
-    cudaError_t e0 = cudaMemcpyAsync(b.wz, w, a.wn * sizeof(double2), cudaMemcpyDeviceToDevice, st);
-    if (e0 != cudaSuccess) return cuda_status(e0, "trot_prop_step_vjp copy");
-    TROT_TRY(zero_inactive(W, (size_t)N * n, b.act, b.wz, st));
-    for (int l = 0; l <= K; ++l) TROT_TRY(zero_inactive(W, (size_t)N * n, b.act, b.U + (size_t)l * a.wn, st));
-    TROT_TRY(zero_inactive(W, (size_t)N * n, b.act, b.w2, st));
-    TROT_TRY(zero_inactive(W, NN, b.act, b.V, st));
-    TROT_TRY(zero_inactive(W, a.nN, b.act, b.green, st));
-    TROT_TRY(zero_inactive(W, (size_t)n * n, b.act, b.P, st));
-    TROT_TRY(zero_inactive(W, (size_t)n * n, b.act, b.Pn, st));
-    TROT_TRY(zero_inactive(W, G, b.act, b.xs, st));
+  for (int q = 0; q < a.nspin; ++q) {
+    SpinWs& x = b.sp[q];
+    const size_t per = (size_t)N * a.n[q], nn = (size_t)a.n[q] * a.n[q];
+    TROT_TRY(dcopy(x.wz, w[q], a.wn[q] * sizeof(double2), st));
+    TROT_TRY(zero_inactive(W, per, b.act, x.wz, st));
+    for (int l = 0; l <= K; ++l) TROT_TRY(zero_inactive(W, per, b.act, x.U + (size_t)l * a.wn[q], st));
+    TROT_TRY(zero_inactive(W, per, b.act, x.w2, st));
+    TROT_TRY(zero_inactive(W, a.nN[q], b.act, x.green, st));
+    TROT_TRY(zero_inactive(W, nn, b.act, x.P, st));
+    TROT_TRY(zero_inactive(W, nn, b.act, x.Pn, st));
   }
+  TROT_TRY(zero_inactive(W, NN, b.act, b.V, st));
+  TROT_TRY(zero_inactive(W, G, b.act, b.xs, st));
   // ---------------- backward
-  adj_step_bwd_kernel<<<wb, 128, 0, st>>>(W, (const double2*)in->overlaps, b.detn, b.st, b.ft, in->weights,
+  adj_step_bwd_kernel<<<wb, 128, 0, st>>>(W, (const double2*)in->overlaps, b.ov_new, b.st, b.ft, in->weights,
                                            in->scalars, s->dt, s->sqrt_dt, s->h0_prop, s->weight_floor, s->weight_cap,
                                            s->pop_control_damping, b.wsum, g_weights_out,
                                            (const double2*)g_overlaps_out, g_scalars_out, g_weights_in,
@@ -716,124 +791,173 @@ int trot_prop_step_vjp(const trot_system* s, const trot_state* in, const double*
   TROT_CHECK_LAUNCH("adj_scalar_tail_kernel");
   adj_sum_kernel<<<1, 256, 0, st>>>(W, b.g_es, g_scalars_in);
   TROT_CHECK_LAUNCH("adj_sum_kernel");
-  // g_w' (incoming) + overlap term
-  cudaError_t e = cudaMemcpyAsync(b.gwn, g_walkers_out, a.wn * sizeof(double2), cudaMemcpyDeviceToDevice, st);
-  if (e != cudaSuccess) return cuda_status(e, "trot_prop_step_vjp copy");
-  TROT_TRY(zero_inactive(W, (size_t)N * n, b.act, b.gwn, st));
-  adj_overlap_kernel<<<W, 256, 0, st>>>(N, n, s->mo_a, b.Pn, b.kappa, b.gwn);
-  TROT_CHECK_LAUNCH("adj_overlap_kernel");
-  // w' = B w2: g_B += Re sum g_w' w2^H; g_w2 = B^T g_w'
-  adj_outer_sum_kernel<<<dim3((N + 31) / 32, (N + 31) / 32), 256, 0, st>>>(W, N, n, b.gwn, b.w2, g_exp_h1_half);
-  TROT_CHECK_LAUNCH("adj_outer_sum_kernel");
-  TROT_TRY(zgemm_batched(W, N, n, N, one, b.Bc, 0, N, 1, b.gwn, (long long)N * n, n, 0, zero, b.gw2, (long long)N * n,
-                         n, st));
-  // v_0 = g_w2, v_{j+1} = V^H v_j
-  e = cudaMemcpyAsync(b.Vv, b.gw2, a.wn * sizeof(double2), cudaMemcpyDeviceToDevice, st);
-  if (e != cudaSuccess) return cuda_status(e, "trot_prop_step_vjp copy");
-  for (int j = 0; j < K; ++j)
-    TROT_TRY(zgemm_batched(W, N, n, N, one, b.V, (long long)NN, N, 2, b.Vv + (size_t)j * a.wn, (long long)N * n, n, 0,
-                           zero, b.Vv + (size_t)(j + 1) * a.wn, (long long)N * n, n, st));
-  // g_w1 = sum_k conj(c_k) v_k
-  cb.nx = K + 1;
-  for (int k = 0; k <= K; ++k) { cb.coef[k] = cmk(ck[k].x, -ck[k].y); cb.x[k] = b.Vv + (size_t)k * a.wn; }
-  TROT_TRY(combine(a.wn, cb, b.gw1, false, st));
-  // s_l = sum_{j <= K-1-l} conj(c_{j+l+1}) v_j;  g_V = sum_l s_l u_l^H
-  for (int l = 0; l < K; ++l) {
-    Comb cs{};
-    cs.nx = K - l;
-    for (int j = 0; j < K - l; ++j) { cs.coef[j] = cmk(ck[j + l + 1].x, -ck[j + l + 1].y); cs.x[j] = b.Vv + (size_t)j * a.wn; }
-    TROT_TRY(combine(a.wn, cs, b.S + (size_t)l * a.wn, false, st));
-    TROT_TRY(zgemm_batched(W, N, N, n, one, b.S + (size_t)l * a.wn, (long long)N * n, n, 0, b.U + (size_t)l * a.wn,
-                           (long long)N * n, n, 2, l == 0 ? zero : one, b.gV, (long long)NN, N, st));
+  for (int q = 0; q < a.nspin; ++q) {
+    SpinWs& x = b.sp[q];
+    const int n = a.n[q];
+    const long long sw = (long long)N * n;
+    const size_t per = (size_t)N * n;
+    // g_w' (incoming) + overlap term
+    TROT_TRY(dcopy(x.gwn, gout[q], a.wn[q] * sizeof(double2), st));
+    TROT_TRY(zero_inactive(W, per, b.act, x.gwn, st));
+    adj_overlap_kernel<<<W, 256, 0, st>>>(N, n, (double)a.mult[q], a.mo[q], x.Pn, b.kappa, x.gwn);
+    TROT_CHECK_LAUNCH("adj_overlap_kernel");
+    // w' = B w2: g_B += Re sum g_w' w2^H; g_w2 = B^T g_w'
+    adj_outer_sum_kernel<<<dim3((N + 31) / 32, (N + 31) / 32), 256, 0, st>>>(W, N, n, x.gwn, x.w2, g_exp_h1_half);
+    TROT_CHECK_LAUNCH("adj_outer_sum_kernel");
+    TROT_TRY(zgemm_batched(W, N, n, N, one, b.Bc, 0, N, 1, x.gwn, sw, n, 0, zero, x.gw2, sw, n, st));
+    // v_0 = g_w2, v_{j+1} = V^H v_j
+    TROT_TRY(dcopy(x.Vv, x.gw2, a.wn[q] * sizeof(double2), st));
+    for (int j = 0; j < K; ++j)
+      TROT_TRY(zgemm_batched(W, N, n, N, one, b.V, (long long)NN, N, 2, x.Vv + (size_t)j * a.wn[q], sw, n, 0, zero,
+                             x.Vv + (size_t)(j + 1) * a.wn[q], sw, n, st));
+    // g_w1 = sum_k conj(c_k) v_k
+    Comb cb{};
+    cb.nx = K + 1;
+    for (int k = 0; k <= K; ++k) { cb.coef[k] = cmk(ck[k].x, -ck[k].y); cb.x[k] = x.Vv + (size_t)k * a.wn[q]; }
+    TROT_TRY(combine(a.wn[q], cb, x.gw1, false, st));
+    // s_l = sum_{j <= K-1-l} conj(c_{j+l+1}) v_j;  g_V += sum_l s_l u_l^H (both spins share V)
+    for (int l = 0; l < K; ++l) {
+      Comb cs{};
+      cs.nx = K - l;
+      for (int j = 0; j < K - l; ++j) { cs.coef[j] = cmk(ck[j + l + 1].x, -ck[j + l + 1].y); cs.x[j] = x.Vv + (size_t)j * a.wn[q]; }
+      TROT_TRY(combine(a.wn[q], cs, x.S + (size_t)l * a.wn[q], false, st));
+      TROT_TRY(zgemm_batched(W, N, N, n, one, x.S + (size_t)l * a.wn[q], sw, n, 0, x.U + (size_t)l * a.wn[q], sw, n,
+                             2, (q == 0 && l == 0) ? zero : one, b.gV, (long long)NN, N, st));
+    }
+    // w1 = B w: g_B += Re sum g_w1 w^H; g_w = B^T g_w1 (the Green's-function term is added below)
+    adj_outer_sum_kernel<<<dim3((N + 31) / 32, (N + 31) / 32), 256, 0, st>>>(W, N, n, x.gw1, x.wz, g_exp_h1_half);
+    TROT_CHECK_LAUNCH("adj_outer_sum_kernel");
+    TROT_TRY(zgemm_batched(W, N, n, N, one, b.Bc, 0, N, 1, x.gw1, sw, n, 0, zero, gin[q], sw, n, st));
   }
   // V = sum_g xs_g L_g: g_xs^V[b][g] = sum_pq L_g[pq] g_V[b][pq]
   TROT_TRY(launch_zgemm_cr(W, G, (int)NN, 1.0, b.gV, (int)NN, s->chol_flat, (int)NN, true, b.gxsv, G, false, st));
   adj_fields_kernel<<<grid_of((size_t)W * G), 256, 0, st>>>(W, G, s->sqrt_dt, s->mf_shifts_im, b.xs, b.gxsv, b.g_req,
                                                              b.g_c, b.gfb);
   TROT_CHECK_LAUNCH("adj_fields_kernel");
-  // fb = 2 G R^T: g_G = 2 g_fb R
-  TROT_TRY(launch_zgemm_cr(W, (int)a.nN, G, 2.0, b.gfb, G, s->rot_chol_a, (int)a.nN, false, b.gG, (int)a.nN, false, st));
-  // w1 = B w: g_B += Re sum g_w1 w^H; g_w = B^T g_w1 + G-term
-  adj_outer_sum_kernel<<<dim3((N + 31) / 32, (N + 31) / 32), 256, 0, st>>>(W, N, n, b.gw1, b.wz, g_exp_h1_half);
-  TROT_CHECK_LAUNCH("adj_outer_sum_kernel");
-  TROT_TRY(zgemm_batched(W, N, n, N, one, b.Bc, 0, N, 1, b.gw1, (long long)N * n, n, 0, zero, (double2*)g_walkers_in,
-                         (long long)N * n, n, st));
-  TROT_TRY(green_vjp_launch(a, s->mo_a, b.green, b.gG, b.P, (double2*)g_walkers_in, st));
+  for (int q = 0; q < a.nspin; ++q) {
+    SpinWs& x = b.sp[q];
+    // fb = sum_s mult_s G_s R_s^T: g_G_s = mult_s g_fb R_s
+    TROT_TRY(launch_zgemm_cr(W, (int)a.nN[q], G, (double)a.mult[q], b.gfb, G, a.rot_chol[q], (int)a.nN[q], false,
+                             x.gG, (int)a.nN[q], false, st));
+    TROT_TRY(green_vjp_launch(a, q, x.green, x.gG, x.P, gin[q], st));
+  }
   return TROT_OK;
 }
 
-int trot_local_energy_vjp(const trot_system* s, const double* walkers, const double* g_energy, double* g_walkers,
-                          double* g_h1, void* ws, size_t ws_bytes, void* stream) {
+int trot_local_energy_vjp(const trot_system* s, const double* walkers_a, const double* walkers_b,
+                          const double* g_energy, double* g_walkers_a, double* g_walkers_b, double* g_h1, void* ws,
+                          size_t ws_bytes, void* stream) {
   TROT_TRY(check_adj(s));
-  if (!walkers || !g_energy || !g_walkers || !g_h1 || !ws) {
+  const AdjCommon a = common_of(s);
+  if (!walkers_a || !g_energy || !g_walkers_a || !g_h1 || !ws ||
+      (a.nspin == 2 && (!walkers_b || !g_walkers_b))) {
     set_error("null walkers, cotangent or workspace");
     return TROT_ERR_NULL_PTR;
   }
-  if (!s->rot_chol_a || !s->rot_h1_a) { set_error("null measurement context"); return TROT_ERR_NULL_PTR; }
-  const AdjCommon a = common_of(s);
+  for (int q = 0; q < a.nspin; ++q)
+    if (!a.rot_chol[q] || !a.rot_h1[q]) { set_error("null measurement context"); return TROT_ERR_NULL_PTR; }
   Carver c(ws, ws_bytes);
   EnergyWs b;
   carve_energy(a, c, b);
   if (!c.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, c.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
   cudaStream_t st = (cudaStream_t)stream;
-  const int W = a.W, N = a.N, n = a.n, G = a.G;
-  const double2* w = (const double2*)walkers;
-  TROT_TRY(green_launch(a, s->mo_a, w, b.green, b.P, b.det, st));
+  const int W = a.W, N = a.N, G = a.G;
+  const double2* w[2] = {(const double2*)walkers_a, (const double2*)walkers_b};
+  double2* gw[2] = {(double2*)g_walkers_a, (double2*)g_walkers_b};
   adj_act_from_cotangent_kernel<<<(W + 127) / 128, 128, 0, st>>>(W, g_energy, 0, b.act);
   TROT_CHECK_LAUNCH("adj_act_from_cotangent_kernel");
-  TROT_TRY(zero_inactive(W, a.nN, b.act, b.green, st));
-  TROT_TRY(zero_inactive(W, (size_t)n * n, b.act, b.P, st));
-  // F[b n + j][g n + i] = f_g[i][j] = sum_p R_g[i][p] G[j][p]
-  TROT_TRY(launch_zgemm_cr(W * n, G * n, N, 1.0, b.green, N, s->rot_chol_a, N, true, b.F, G * n, false, st));
-  adj_trace_kernel<<<grid_of((size_t)W * G), 256, 0, st>>>(W, G, n, b.F, b.c);
-  TROT_CHECK_LAUNCH("adj_trace_kernel");
-  adj_block_transpose_kernel<<<grid_of((size_t)W * n * G * n), 256, 0, st>>>(W, G, n, b.F, b.Ft);
-  TROT_CHECK_LAUNCH("adj_block_transpose_kernel");
-  // D = 4 sum_g c_g R_g - 2 sum_g f_g R_g
-  TROT_TRY(launch_zgemm_cr(W * n, N, G * n, -2.0, b.Ft, G * n, s->rot_chol_a, N, false, b.D, N, false, st));
-  TROT_TRY(launch_zgemm_cr(W, (int)a.nN, G, 4.0, b.c, G, s->rot_chol_a, (int)a.nN, false, b.D, (int)a.nN, true, st));
-  adj_energy_green_kernel<<<grid_of((size_t)W * a.nN), 256, 0, st>>>(W, n, N, s->rot_h1_a, b.D, g_energy, b.gG);
-  TROT_CHECK_LAUNCH("adj_energy_green_kernel");
-  TROT_TRY(green_vjp_launch(a, s->mo_a, b.green, b.gG, b.P, (double2*)g_walkers, st));
-  adj_weighted_green_kernel<<<grid_of(a.nN), 256, 0, st>>>(W, n, N, b.green, g_energy, b.H);
-  TROT_CHECK_LAUNCH("adj_weighted_green_kernel");
-  adj_h1_direct_kernel<<<grid_of((size_t)N * N), 256, 0, st>>>(N, n, s->mo_a, b.H, g_h1);
-  TROT_CHECK_LAUNCH("adj_h1_direct_kernel");
+  // traces c_s[b][g] = tr f_{s,g}, f_{s,g} = R_{s,g} G_s^T; c_tot = sum_s mult_s c_s
+  for (int q = 0; q < a.nspin; ++q) {
+    const int n = a.n[q];
+    TROT_TRY(green_launch(a, q, w[q], b.green[q], b.P[q], b.det, st));
+    TROT_TRY(zero_inactive(W, a.nN[q], b.act, b.green[q], st));
+    TROT_TRY(zero_inactive(W, (size_t)n * n, b.act, b.P[q], st));
+    TROT_TRY(launch_zgemm_cr(W * n, G * n, N, 1.0, b.green[q], N, a.rot_chol[q], N, true, b.F, G * n, false, st));
+    adj_trace_kernel<<<grid_of((size_t)W * G), 256, 0, st>>>(W, G, n, b.F, b.c[q]);
+    TROT_CHECK_LAUNCH("adj_trace_kernel");
+  }
+  {
+    Comb cb{};
+    cb.nx = a.nspin;
+    for (int q = 0; q < a.nspin; ++q) { cb.coef[q] = cmk((double)a.mult[q], 0.0); cb.x[q] = b.c[q]; }
+    TROT_TRY(combine((size_t)W * G, cb, b.ctot, false, st));
+  }
+  // dE/dG_s = mult_s (rot_h1_s + sum_g c_tot,g R_{s,g} - sum_g f_{s,g} R_{s,g})
+  for (int q = 0; q < a.nspin; ++q) {
+    const int n = a.n[q];
+    const double m = (double)a.mult[q];
+    TROT_TRY(launch_zgemm_cr(W * n, G * n, N, 1.0, b.green[q], N, a.rot_chol[q], N, true, b.F, G * n, false, st));
+    adj_block_transpose_kernel<<<grid_of((size_t)W * n * G * n), 256, 0, st>>>(W, G, n, b.F, b.Ft);
+    TROT_CHECK_LAUNCH("adj_block_transpose_kernel");
+    TROT_TRY(launch_zgemm_cr(W * n, N, G * n, -m, b.Ft, G * n, a.rot_chol[q], N, false, b.D, N, false, st));
+    TROT_TRY(launch_zgemm_cr(W, (int)a.nN[q], G, m, b.ctot, G, a.rot_chol[q], (int)a.nN[q], false, b.D, (int)a.nN[q],
+                             true, st));
+    adj_energy_green_kernel<<<grid_of((size_t)W * a.nN[q]), 256, 0, st>>>(W, n, N, m, a.rot_h1[q], b.D, g_energy,
+                                                                           b.gG);
+    TROT_CHECK_LAUNCH("adj_energy_green_kernel");
+    TROT_TRY(green_vjp_launch(a, q, b.green[q], b.gG, b.P[q], gw[q], st));
+    adj_weighted_green_kernel<<<grid_of(a.nN[q]), 256, 0, st>>>(W, n, N, b.green[q], g_energy, b.H);
+    TROT_CHECK_LAUNCH("adj_weighted_green_kernel");
+    adj_h1_direct_kernel<<<grid_of((size_t)N * N), 256, 0, st>>>(N, n, m, a.mo[q], b.H, g_h1);
+    TROT_CHECK_LAUNCH("adj_h1_direct_kernel");
+  }
   return TROT_OK;
 }
 
-int trot_overlap_vjp(const trot_system* s, const double* walkers, const double* g_overlaps, double* g_walkers,
-                     void* ws, size_t ws_bytes, void* stream) {
+int trot_overlap_vjp(const trot_system* s, const double* walkers_a, const double* walkers_b, const double* g_overlaps,
+                     double* g_walkers_a, double* g_walkers_b, void* ws, size_t ws_bytes, void* stream) {
   TROT_TRY(check_adj(s));
-  if (!walkers || !g_overlaps || !g_walkers || !ws) { set_error("null walkers, cotangent or workspace"); return TROT_ERR_NULL_PTR; }
   const AdjCommon a = common_of(s);
+  if (!walkers_a || !g_overlaps || !g_walkers_a || !ws || (a.nspin == 2 && (!walkers_b || !g_walkers_b))) {
+    set_error("null walkers, cotangent or workspace");
+    return TROT_ERR_NULL_PTR;
+  }
   Carver c(ws, ws_bytes);
-  double2* green = c.take<double2>(a.W * a.nN);
-  double2* P = c.take<double2>((size_t)a.W * a.n * a.n);
-  double2* det = c.take<double2>(a.W);
-  double2* kappa = c.take<double2>((size_t)2 * a.W);  // kappa, then W ints of walker flags
+  double2 *green[2] = {nullptr, nullptr}, *P[2] = {nullptr, nullptr}, *det[2] = {nullptr, nullptr};
+  for (int q = 0; q < a.nspin; ++q) {
+    green[q] = c.take<double2>(a.W * a.nN[q]);
+    P[q] = c.take<double2>((size_t)a.W * a.n[q] * a.n[q]);
+    det[q] = c.take<double2>(a.W);
+  }
+  double2* ov = c.take<double2>((size_t)3 * a.W);  // ov, kappa, then W ints of walker flags
+  double2* kappa = ov + a.W;
+  int* act = reinterpret_cast<int*>(ov + 2 * a.W);
   if (!c.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, c.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
   cudaStream_t st = (cudaStream_t)stream;
-  TROT_TRY(green_launch(a, s->mo_a, (const double2*)walkers, green, P, det, st));
-  int* act = reinterpret_cast<int*>(kappa + a.W);
+  const double2* w[2] = {(const double2*)walkers_a, (const double2*)walkers_b};
+  double2* gw[2] = {(double2*)g_walkers_a, (double2*)g_walkers_b};
   adj_act_from_cotangent_kernel<<<(a.W + 127) / 128, 128, 0, st>>>(a.W, g_overlaps, 1, act);
   TROT_CHECK_LAUNCH("adj_act_from_cotangent_kernel");
-  TROT_TRY(zero_inactive(a.W, (size_t)a.n * a.n, act, P, st));
-  adj_kappa_kernel<<<(a.W + 127) / 128, 128, 0, st>>>(a.W, det, (const double2*)g_overlaps, kappa);
+  for (int q = 0; q < a.nspin; ++q) TROT_TRY(green_launch(a, q, w[q], green[q], P[q], det[q], st));
+  TROT_TRY(ov_launch(a, det[0], det[1], ov, st));
+  adj_kappa_kernel<<<(a.W + 127) / 128, 128, 0, st>>>(a.W, ov, (const double2*)g_overlaps, kappa);
   TROT_CHECK_LAUNCH("adj_kappa_kernel");
-  adj_overlap_kernel<<<a.W, 256, 0, st>>>(a.N, a.n, s->mo_a, P, kappa, (double2*)g_walkers);
-  TROT_CHECK_LAUNCH("adj_overlap_kernel");
+  for (int q = 0; q < a.nspin; ++q) {
+    TROT_TRY(zero_inactive(a.W, (size_t)a.n[q] * a.n[q], act, P[q], st));
+    adj_overlap_kernel<<<a.W, 256, 0, st>>>(a.N, a.n[q], (double)a.mult[q], a.mo[q], P[q], kappa, gw[q]);
+    TROT_CHECK_LAUNCH("adj_overlap_kernel");
+  }
   return TROT_OK;
 }
 
-int trot_orthonormalize_vjp(const trot_system* s, const double* walkers, const double* walkers_q, const double* g_q,
-                            double* g_walkers, void* stream) {
+int trot_orthonormalize_vjp(const trot_system* s, const double* walkers_a, const double* walkers_b,
+                            const double* q_a, const double* q_b, const double* g_q_a, const double* g_q_b,
+                            double* g_walkers_a, double* g_walkers_b, void* stream) {
   TROT_TRY(check_adj(s));
-  if (!walkers || !walkers_q || !g_q || !g_walkers) { set_error("null walkers or cotangent"); return TROT_ERR_NULL_PTR; }
   const AdjCommon a = common_of(s);
-  adj_qr_kernel<<<a.W, 256, 0, (cudaStream_t)stream>>>(a.N, a.n, (const double2*)walkers, (const double2*)walkers_q,
-                                                       (const double2*)g_q, (double2*)g_walkers);
-  TROT_CHECK_LAUNCH("adj_qr_kernel");
+  if (!walkers_a || !q_a || !g_q_a || !g_walkers_a || (a.nspin == 2 && (!walkers_b || !q_b || !g_q_b || !g_walkers_b))) {
+    set_error("null walkers or cotangent");
+    return TROT_ERR_NULL_PTR;
+  }
+  const double* w[2] = {walkers_a, walkers_b};
+  const double* qq[2] = {q_a, q_b};
+  const double* gq[2] = {g_q_a, g_q_b};
+  double* gw[2] = {g_walkers_a, g_walkers_b};
+  for (int q = 0; q < a.nspin; ++q) {
+    adj_qr_kernel<<<a.W, 256, 0, (cudaStream_t)stream>>>(a.N, a.n[q], (const double2*)w[q], (const double2*)qq[q],
+                                                         (const double2*)gq[q], (double2*)gw[q]);
+    TROT_CHECK_LAUNCH("adj_qr_kernel");
+  }
   return TROT_OK;
 }
 
