@@ -242,14 +242,17 @@ __global__ void adj_qr_kernel(int N, int n, const double2* __restrict__ w, const
   }
 }
 
-// out[p][q] += Re sum_b sum_j a[b][p][j] conj(c[b][q][j]); grid (q tiles, p tiles), 256 threads
-__global__ void __launch_bounds__(256) adj_outer_sum_kernel(int W, int N, int n, const double2* __restrict__ a,
-                                                            const double2* __restrict__ c, double* __restrict__ out) {
+// part[z][p][q] = Re sum_{b in chunk z} sum_j a[b][p][j] conj(c[b][q][j]); grid (q tiles, p tiles, chunks
+// of wchunk walkers), 256 threads.  The chunk partials are summed in order by adj_outer_reduce_kernel.
+__global__ void __launch_bounds__(256) adj_outer_part_kernel(int W, int N, int n, int wchunk,
+                                                             const double2* __restrict__ a,
+                                                             const double2* __restrict__ c, double* __restrict__ part) {
   __shared__ double2 As[32][33], Cs[32][33];
-  const int q0 = blockIdx.x * 32, p0 = blockIdx.y * 32;
+  const int q0 = blockIdx.x * 32, p0 = blockIdx.y * 32, z = blockIdx.z;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int b = 0; b < W; ++b) {
+  const int b0 = z * wchunk, b1 = min(W, b0 + wchunk);
+  for (int b = b0; b < b1; ++b) {
     for (int j0 = 0; j0 < n; j0 += 32) {
       for (int e = threadIdx.x; e < 32 * 32; e += 256) {
         const int r = e >> 5, j = e & 31;
@@ -258,7 +261,8 @@ __global__ void __launch_bounds__(256) adj_outer_sum_kernel(int W, int N, int n,
         Cs[r][j] = (ok && q0 + r < N) ? c[((size_t)b * N + q0 + r) * n + j0 + j] : cmk(0.0, 0.0);
       }
       __syncthreads();
-      for (int j = 0; j < 32; ++j) {
+      const int jn = min(32, n - j0);
+      for (int j = 0; j < jn; ++j) {
         const double2 cv = Cs[tx][j];
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
@@ -272,8 +276,31 @@ __global__ void __launch_bounds__(256) adj_outer_sum_kernel(int W, int N, int n,
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const int p = p0 + ty + 8 * r, q = q0 + tx;
-    if (p < N && q < N) out[(size_t)p * N + q] += acc[r];
+    if (p < N && q < N) part[((size_t)z * N + p) * N + q] = acc[r];
   }
+}
+
+__global__ void adj_outer_reduce_kernel(int NN, int Z, const double* __restrict__ part, double* __restrict__ out) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < NN; e += gridDim.x * blockDim.x) {
+    double v = 0.0;
+    for (int z = 0; z < Z; ++z) v += part[(size_t)z * NN + e];
+    out[e] += v;
+  }
+}
+
+static constexpr int kOuterChunks = 64;
+
+// out (N x N) += Re sum_b a_b c_b^H over walkers, a_b, c_b (N x n)
+static int outer_sum(int W, int N, int n, const double2* a, const double2* c, double* part, double* out,
+                     cudaStream_t st) {
+  const int wchunk = (W + kOuterChunks - 1) / kOuterChunks;
+  const int Z = (W + wchunk - 1) / wchunk;
+  adj_outer_part_kernel<<<dim3((N + 31) / 32, (N + 31) / 32, Z), 256, 0, st>>>(W, N, n, wchunk, a, c, part);
+  TROT_CHECK_LAUNCH("adj_outer_part_kernel");
+  const int NN = N * N;
+  adj_outer_reduce_kernel<<<(NN + 255) / 256, 256, 0, st>>>(NN, Z, part, out);
+  TROT_CHECK_LAUNCH("adj_outer_reduce_kernel");
+  return TROT_OK;
 }
 
 // out = sum_t coef[t] x[t] over nx vectors of length len (complex coefficients)
@@ -561,9 +588,16 @@ struct SpinWs {  // per-spin buffers of the step adjoint
 struct StepWs {
   SpinWs sp[2];
   double2 *fb, *xs, *st, *ft, *V, *Bc, *gV, *gxsv, *gfb, *kappa, *ov_new;
-  double *wt_new, *wsum, *g_req, *g_c, *g_es;
+  double *wt_new, *wsum, *g_req, *g_c, *g_es, *opart;
+  double2* kpart;  // split-K partials of the long-K products
   int* act;
 };
+
+static int splitk_slices(int M, int Nn) {  // enough CTAs for two per SM
+  const int base = ((Nn + 63) / 64) * ((M + 63) / 64);
+  int S = (2 * 152 + base - 1) / base;
+  return S < 1 ? 1 : (S > 16 ? 16 : S);
+}
 
 static void carve_step(const AdjCommon& a, Carver& c, StepWs& b) {
   const size_t W = a.W, G = a.G, NN = (size_t)a.N * a.N;
@@ -604,6 +638,10 @@ static void carve_step(const AdjCommon& a, Carver& c, StepWs& b) {
   b.g_req = c.take<double>(W);
   b.g_c = c.take<double>(W);
   b.g_es = c.take<double>(W);
+  b.opart = c.take<double>((size_t)kOuterChunks * NN);
+  size_t kp = (size_t)splitk_slices(a.W, a.G) * W * G;
+  for (int q = 0; q < a.nspin; ++q) kp = std::max(kp, (size_t)splitk_slices(a.W, a.G) * W * G);
+  b.kpart = c.take<double2>(kp);
   b.act = c.take<int>(W);
 }
 
@@ -725,8 +763,9 @@ int trot_prop_step_vjp(const trot_system* s, const trot_state* in, const double*
   for (int q = 0; q < a.nspin; ++q) {
     TROT_TRY(green_launch(a, q, w[q], b.sp[q].green, b.sp[q].P, b.sp[q].det, st));
     // fb = sum_s mult_s R_s . G_s
-    TROT_TRY(launch_zgemm_cr(W, G, (int)a.nN[q], (double)a.mult[q], b.sp[q].green, (int)a.nN[q], a.rot_chol[q],
-                             (int)a.nN[q], true, b.fb, G, q > 0, st));
+    TROT_TRY(launch_zgemm_cr_splitk(W, G, (int)a.nN[q], (double)a.mult[q], b.sp[q].green, (int)a.nN[q],
+                                    a.rot_chol[q], (int)a.nN[q], true, b.fb, G, q > 0, b.kpart,
+                                    splitk_slices(W, G), st));
   }
   TROT_TRY(launch_fields(W, G, s->sqrt_dt, b.fb, s->mf_shifts_im, fields, b.xs, b.st, b.ft, st));
   TROT_TRY(launch_zgemm_cr(W, (int)NN, G, 1.0, b.xs, G, s->chol_flat, (int)NN, false, b.V, (int)NN, false, st));
@@ -802,8 +841,7 @@ int trot_prop_step_vjp(const trot_system* s, const trot_state* in, const double*
     adj_overlap_kernel<<<W, 256, 0, st>>>(N, n, (double)a.mult[q], a.mo[q], x.Pn, b.kappa, x.gwn);
     TROT_CHECK_LAUNCH("adj_overlap_kernel");
     // w' = B w2: g_B += Re sum g_w' w2^H; g_w2 = B^T g_w'
-    adj_outer_sum_kernel<<<dim3((N + 31) / 32, (N + 31) / 32), 256, 0, st>>>(W, N, n, x.gwn, x.w2, g_exp_h1_half);
-    TROT_CHECK_LAUNCH("adj_outer_sum_kernel");
+    TROT_TRY(outer_sum(W, N, n, x.gwn, x.w2, b.opart, g_exp_h1_half, st));
     TROT_TRY(zgemm_batched(W, N, n, N, one, b.Bc, 0, N, 1, x.gwn, sw, n, 0, zero, x.gw2, sw, n, st));
     // v_0 = g_w2, v_{j+1} = V^H v_j
     TROT_TRY(dcopy(x.Vv, x.gw2, a.wn[q] * sizeof(double2), st));
@@ -825,12 +863,12 @@ int trot_prop_step_vjp(const trot_system* s, const trot_state* in, const double*
                              2, (q == 0 && l == 0) ? zero : one, b.gV, (long long)NN, N, st));
     }
     // w1 = B w: g_B += Re sum g_w1 w^H; g_w = B^T g_w1 (the Green's-function term is added below)
-    adj_outer_sum_kernel<<<dim3((N + 31) / 32, (N + 31) / 32), 256, 0, st>>>(W, N, n, x.gw1, x.wz, g_exp_h1_half);
-    TROT_CHECK_LAUNCH("adj_outer_sum_kernel");
+    TROT_TRY(outer_sum(W, N, n, x.gw1, x.wz, b.opart, g_exp_h1_half, st));
     TROT_TRY(zgemm_batched(W, N, n, N, one, b.Bc, 0, N, 1, x.gw1, sw, n, 0, zero, gin[q], sw, n, st));
   }
   // V = sum_g xs_g L_g: g_xs^V[b][g] = sum_pq L_g[pq] g_V[b][pq]
-  TROT_TRY(launch_zgemm_cr(W, G, (int)NN, 1.0, b.gV, (int)NN, s->chol_flat, (int)NN, true, b.gxsv, G, false, st));
+  TROT_TRY(launch_zgemm_cr_splitk(W, G, (int)NN, 1.0, b.gV, (int)NN, s->chol_flat, (int)NN, true, b.gxsv, G, false,
+                                  b.kpart, splitk_slices(W, G), st));
   adj_fields_kernel<<<grid_of((size_t)W * G), 256, 0, st>>>(W, G, s->sqrt_dt, s->mf_shifts_im, b.xs, b.gxsv, b.g_req,
                                                              b.g_c, b.gfb);
   TROT_CHECK_LAUNCH("adj_fields_kernel");

@@ -18,7 +18,8 @@ static constexpr int BM = 64, BN = 64, BK = 16, NT = 256;
 template <bool B_NK>
 __global__ void __launch_bounds__(NT)
 zgemm_cr_kernel(int M, int Nn, int K, double alpha, const double2* __restrict__ A, int lda,
-                const double* __restrict__ B, int ldb, double2* __restrict__ C, int ldc, int accumulate) {
+                const double* __restrict__ B, int ldb, double2* __restrict__ C, int ldc, int accumulate, int kchunk,
+                double2* __restrict__ part) {
   __shared__ double2 As[BK][BM + 1];
   __shared__ double Bs[BK][BN + 1];
   const int tid = threadIdx.x;
@@ -30,14 +31,17 @@ zgemm_cr_kernel(int M, int Nn, int K, double alpha, const double2* __restrict__ 
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = cmk(0.0, 0.0);
 
-  for (int k0 = 0; k0 < K; k0 += BK) {
+  // split K (part != null): slice blockIdx.z covers [kb, ke) and writes its unscaled partial
+  const int kb = part ? blockIdx.z * kchunk : 0;
+  const int ke = part ? min(K, kb + kchunk) : K;
+  for (int k0 = kb; k0 < ke; k0 += BK) {
     // A tile: BM x BK complex, 4 per thread
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       int e = tid + r * NT;
       int mm = e / BK, kk = e % BK;
       int gm = m0 + mm, gk = k0 + kk;
-      As[kk][mm] = (gm < M && gk < K) ? A[(size_t)gm * lda + gk] : cmk(0.0, 0.0);
+      As[kk][mm] = (gm < M && gk < ke) ? A[(size_t)gm * lda + gk] : cmk(0.0, 0.0);
     }
     // B tile: BK x BN real, 4 per thread
 #pragma unroll
@@ -47,7 +51,7 @@ zgemm_cr_kernel(int M, int Nn, int K, double alpha, const double2* __restrict__ 
       if (B_NK) { nn = e / BK; kk = e % BK; } else { kk = e / BN; nn = e % BN; }
       int gn = n0 + nn, gk = k0 + kk;
       double v = 0.0;
-      if (gn < Nn && gk < K) v = B_NK ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
+      if (gn < Nn && gk < ke) v = B_NK ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
       Bs[kk][nn] = v;
     }
     __syncthreads();
@@ -74,6 +78,10 @@ zgemm_cr_kernel(int M, int Nn, int K, double alpha, const double2* __restrict__ 
     for (int j = 0; j < 4; ++j) {
       int gn = n0 + tx + 16 * j;
       if (gn >= Nn) continue;
+      if (part) {
+        part[((size_t)blockIdx.z * M + gm) * Nn + gn] = acc[i][j];
+        continue;
+      }
       double2 v = cscale(acc[i][j], alpha);
       double2* c = C + (size_t)gm * ldc + gn;
       *c = accumulate ? cadd(*c, v) : v;
@@ -81,19 +89,48 @@ zgemm_cr_kernel(int M, int Nn, int K, double alpha, const double2* __restrict__ 
   }
 }
 
+// C[m][n] (+)= alpha sum_z part[z][m][n] in slice order (deterministic)
+__global__ void zgemm_splitk_reduce_kernel(int M, int Nn, int S, double alpha, const double2* __restrict__ part,
+                                           double2* __restrict__ C, int ldc, int accumulate) {
+  const size_t total = (size_t)M * Nn;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    double2 v = cmk(0.0, 0.0);
+    for (int z = 0; z < S; ++z) v = cadd(v, part[(size_t)z * total + e]);
+    const size_t m = e / Nn, n = e % Nn;
+    double2* c = C + m * ldc + n;
+    v = cscale(v, alpha);
+    *c = accumulate ? cadd(*c, v) : v;
+  }
+}
+
 int launch_zgemm_cr(int M, int Nn, int K, double alpha, const double2* A, int lda, const double* B,
                     int ldb, bool b_is_nk, double2* C, int ldc, bool accumulate, cudaStream_t st) {
+  return launch_zgemm_cr_splitk(M, Nn, K, alpha, A, lda, B, ldb, b_is_nk, C, ldc, accumulate, nullptr, 1, st);
+}
+
+int launch_zgemm_cr_splitk(int M, int Nn, int K, double alpha, const double2* A, int lda, const double* B, int ldb,
+                           bool b_is_nk, double2* C, int ldc, bool accumulate, double2* part, int S,
+                           cudaStream_t st) {
   if (M <= 0 || Nn <= 0) return TROT_OK;
-  dim3 grid((Nn + BN - 1) / BN, (M + BM - 1) / BM);
-  if (grid.y > 65535) {
+  if (!part) S = 1;
+  const int kchunk = ((K + S - 1) / S + BK - 1) / BK * BK;
+  if (part) S = (K + kchunk - 1) / kchunk;
+  dim3 grid((Nn + BN - 1) / BN, (M + BM - 1) / BM, part ? S : 1);
+  if (grid.y > 65535 || grid.z > 65535) {
     set_error("zgemm_cr: M=%d too large", M);
     return TROT_ERR_UNSUPPORTED;
   }
   if (b_is_nk)
-    zgemm_cr_kernel<true><<<grid, NT, 0, st>>>(M, Nn, K, alpha, A, lda, B, ldb, C, ldc, accumulate);
+    zgemm_cr_kernel<true><<<grid, NT, 0, st>>>(M, Nn, K, alpha, A, lda, B, ldb, C, ldc, accumulate, kchunk, part);
   else
-    zgemm_cr_kernel<false><<<grid, NT, 0, st>>>(M, Nn, K, alpha, A, lda, B, ldb, C, ldc, accumulate);
+    zgemm_cr_kernel<false><<<grid, NT, 0, st>>>(M, Nn, K, alpha, A, lda, B, ldb, C, ldc, accumulate, kchunk, part);
   TROT_CHECK_LAUNCH("zgemm_cr_kernel");
+  if (part) {
+    const size_t total = (size_t)M * Nn;
+    const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+    zgemm_splitk_reduce_kernel<<<blocks, 256, 0, st>>>(M, Nn, S, alpha, part, C, ldc, accumulate ? 1 : 0);
+    TROT_CHECK_LAUNCH("zgemm_splitk_reduce_kernel");
+  }
   return TROT_OK;
 }
 

@@ -41,6 +41,11 @@ int launch_green(const Spins& sp, int W, int N, const double2* wa, const double2
 int launch_zgemm_cr(int M, int Nn, int K, double alpha, const double2* A, int lda,
                     const double* B, int ldb, bool b_is_nk, double2* C, int ldc, bool accumulate,
                     cudaStream_t st);
+// Same with K split into S slices computed by separate CTAs (for small M x Nn and long K):
+// part holds S * M * Nn complex partials, reduced in slice order into C.
+int launch_zgemm_cr_splitk(int M, int Nn, int K, double alpha, const double2* A, int lda, const double* B, int ldb,
+                           bool b_is_nk, double2* C, int ldc, bool accumulate, double2* part, int S,
+                           cudaStream_t st);
 
 // step64.cu
 int launch_fields(int W, int G, double sqrt_dt, const double2* fb, const double* mf_im,
