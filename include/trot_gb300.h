@@ -447,6 +447,9 @@ int trot_get_tuning(int knob);
  * reference (it has no profiling hooks). */
 int trot_profile_enable(int max_launches);
 int trot_profile_collect(int max_names, char* names, double* total_ms, int* launches);
+/* Kernel launches the library issued since the last trot_profile_enable,
+ * timed or not (counted only while enabled). */
+long long trot_profile_launch_count(void);
 
 #ifdef __cplusplus
 }

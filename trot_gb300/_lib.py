@@ -126,6 +126,7 @@ _SIGNATURES = {
     "trot_get_tuning": (_i, [_i]),
     "trot_profile_enable": (_i, [_i]),
     "trot_profile_collect": (_i, [_i, ctypes.c_char_p, _p, _p]),
+    "trot_profile_launch_count": (ctypes.c_longlong, []),
 }
 
 _lock = threading.Lock()
@@ -170,6 +171,11 @@ def call(name: str, *args) -> None:
 
 def profile_enable(max_launches: int = 4096) -> None:
     check(load().trot_profile_enable(int(max_launches)))
+
+
+def profile_launch_count() -> int:
+    """Kernel launches of the library since the last profile_enable (all of them)."""
+    return int(load().trot_profile_launch_count())
 
 
 def profile_collect(max_names: int = 64) -> dict:

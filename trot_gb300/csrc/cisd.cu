@@ -13,10 +13,11 @@
 //   local energy: the terms of energy_kernel_rw_rh, see cisd_energy_combine.
 // The l2ci2 quadratic forms 2 sum_g X_g^T ci2 X_g - X_g^T ci2_perm X_g (ci2_perm[(p,u),(q,t)] = ci2[p,t,q,u])
 // = sum_g X_g^T ci2m X_g (X_g = vec(glgp_g)) are one GEMM over all (walker, g) rows.
+#include <algorithm>
+
 #include "ff.cuh"
 #include "kernels.h"
 #include "mixed.h"
-
 #include "profile.h"
 #include "step_tail.cuh"
 
@@ -29,9 +30,10 @@ struct CisdBuffers {
   double2* x;                   // (W, n v) contiguous x
   double2* cg;                  // ci2g = x ci2m (W, n v)
   double2* ci1g1;               // (W, n, n)
-  double2 *m1, *m2;             // ci1_green, ci2_green (W, N, N)
+  double2 *m1, *m2;             // ci1_green, ci2_green (W, N, N), m2 = m1 + W N N
   double2* wsc;                 // per-walker scalars (W, 8): ci1g, gci2g, e1_1_2, e1_2_2, ...
-  double2 *lg, *lci1g, *lci2g;  // (W, G)
+  double2 *lg, *lci1g, *lci2g;  // (W, G), lci2g = lci1g + W G
+  double2* kpart;               // split-K partials of the FP64 products
   double2* xg;                  // glgp rows (W G, n v)
   double2* y;                   // xg ci2m (W G, n v)    (FP64 l2ci2)
   uint16_t* xq;                 // split3 image of xg    (mixed l2ci2)
@@ -45,6 +47,15 @@ struct CisdBuffers {
 static constexpr int kCisdGChunk = 8;
 static int cisd_chunks(int G) { return (G + kCisdGChunk - 1) / kCisdGChunk; }
 
+// K slices for an FP64 product (M x Nn, long K) so that its 64 x 64 tiles fill
+// every SM twice; at least 64 of K per slice.
+static int cisd_splitk(int M, int Nn, int K) {
+  const int base = ((Nn + 63) / 64) * ((M + 63) / 64);
+  int S = (2 * 152 + base - 1) / base;
+  S = std::min(S, std::max(1, K / 64));
+  return std::max(1, std::min(S, 16));
+}
+
 static size_t carve_cisd(const trot_cisd* c, int W, int op, Carver& cv, CisdBuffers& b) {
   const size_t N = c->norb, n = c->nocc, v = c->nvir, G = c->nchol, nv = n * v;
   b = CisdBuffers{};
@@ -55,13 +66,21 @@ static size_t carve_cisd(const trot_cisd* c, int W, int op, Carver& cv, CisdBuff
   b.x = cv.take<double2>(W * nv);
   b.cg = cv.take<double2>(W * nv);
   b.wsc = cv.take<double2>(W * 8);
+  {
+    size_t kp = (size_t)cisd_splitk(W, (int)nv, (int)nv) * W * nv;  // ci2g
+    if (op != TROT_OP_OVERLAP) {
+      kp = std::max(kp, (size_t)cisd_splitk(W, (int)G, (int)(n * N)) * W * G);  // lg
+      kp = std::max(kp, (size_t)cisd_splitk(2 * W, (int)G, (int)(N * N)) * 2 * W * G);  // lci1g, lci2g
+    }
+    b.kpart = cv.take<double2>(kp);
+  }
   if (op == TROT_OP_OVERLAP) return cv.used;
   b.ci1g1 = cv.take<double2>(W * n * n);
-  b.m1 = cv.take<double2>(W * N * N);
-  b.m2 = cv.take<double2>(W * N * N);
+  b.m1 = cv.take<double2>(2 * W * N * N);
+  b.m2 = b.m1 + W * N * N;
   b.lg = cv.take<double2>(W * G);
-  b.lci1g = cv.take<double2>(W * G);
-  b.lci2g = cv.take<double2>(W * G);
+  b.lci1g = cv.take<double2>(2 * W * G);
+  b.lci2g = b.lci1g + W * G;
   if (op == TROT_OP_FORCE_BIAS) return cv.used;
   b.xg = cv.take<double2>((size_t)W * G * nv);
   if (c->l2ci2_precision == TROT_MIXED) {
@@ -284,18 +303,21 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
   __shared__ double2 red[32];
   const int chunk = blockIdx.x, b = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
   const int nchunk = gridDim.x;
-  ffc* Gs = reinterpret_cast<ffc*>(sm);                   // n x N
-  ffc* C1 = Gs + n * N;                                   // n x n
+  // j-major copies (GsT[j][q] = G[q][j], RdT[j][p] = L_g[p][j], AT[q][p] = lg1[p][q]) keep the
+  // per-thread index q (or p) fastest across a warp: no shared-memory bank conflicts
+  ffc* GsT = reinterpret_cast<ffc*>(sm);                  // N x n
+  ffc* C1 = GsT + n * N;                                  // n x n
   ffc* A = C1 + n * n;                                    // n x n  (lg1)
-  ff* Rd = reinterpret_cast<ff*>(A + n * n);              // n x N  (rows < n of L_g)
-  float2* Gf = reinterpret_cast<float2*>(Rd + n * N);     // n x N
+  ff* RdT = reinterpret_cast<ff*>(A + n * n);             // N x n  (rows < n of L_g, transposed)
+  float2* Gf = reinterpret_cast<float2*>(RdT + n * N);    // n x N
   float2* M2f = Gf + n * N;                               // N x N, transposed
   float2* GLf = M2f + N * N;                              // n x N
   float* Lf = reinterpret_cast<float*>(GLf + n * N);      // N x N
   ff* Lc = reinterpret_cast<ff*>(Lf + N * N + ((N * N) & 1));  // N x n: lci1_g
+  ffc* AT = reinterpret_cast<ffc*>(Lc + N * n);           // n x n: lg1 transposed
   for (int e = tid; e < n * N; e += nt) {
     const double2 g = green[(size_t)b * n * N + e];
-    Gs[e] = ffc{ff_from_d(g.x), ff_from_d(g.y)};
+    GsT[(e % N) * n + e / N] = ffc{ff_from_d(g.x), ff_from_d(g.y)};
     Gf[e] = make_float2(d2f_bits(g.x), d2f_bits(g.y));
   }
   for (int e = tid; e < N * N; e += nt) {  // stored transposed: M2f[i][j] = M2[j][i]
@@ -316,7 +338,7 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
     for (int e = tid; e < N * N; e += nt) {
       const double l = Lg[e];
       Lf[e] = d2f_bits(l);
-      if (e < n * N) Rd[e] = ff_from_d(l);
+      if (e < n * N) RdT[(e % N) * n + e / N] = ff_from_d(l);
     }
     const double* lc = lci1 + (size_t)gg * N * n;
     for (int e = tid; e < N * n; e += nt) Lc[e] = ff_from_d(lc[e]);
@@ -325,12 +347,14 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
       const int p = e / n, q = e % n;
       ffc a = z;
       for (int j = 0; j < N; ++j) {
-        const ff r = Rd[p * N + j];
-        const ffc g = Gs[q * N + j];
+        const ff r = RdT[j * n + p];
+        const ffc g = GsT[j * n + q];
         ff_mad(a.re, r, g.re);
         ff_mad(a.im, r, g.im);
       }
-      A[e] = ffc_norm(a);
+      a = ffc_norm(a);
+      A[e] = a;
+      AT[q * n + p] = a;
     }
     for (int e = tid; e < n * N; e += nt) {
       const int p = e / N, i = e % N;
@@ -347,14 +371,14 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
     for (int e = tid; e < n * n; e += nt) {
       const int p = e / n, q = e % n;
       const ffc apq = A[p * n + q];
-      ffc_mad(s0, apq, A[q * n + p]);
+      ffc_mad(s0, apq, AT[p * n + q]);
       ffc t = z;
-      for (int a2 = 0; a2 < n; ++a2) ffc_mad(t, A[q * n + a2], C1[a2 * n + p]);
+      for (int a2 = 0; a2 < n; ++a2) ffc_mad(t, AT[a2 * n + q], C1[a2 * n + p]);
       ffc_mad(s1, apq, ffc_norm(t));
       ffc bq = z;  // lci1g[q][p] = sum_i lci1[i][q] G[p][i]
       for (int i = 0; i < N; ++i) {
         const ff l = Lc[i * n + q];
-        const ffc g = Gs[p * N + i];
+        const ffc g = GsT[i * n + p];
         ff_mad(bq.re, l, g.re);
         ff_mad(bq.im, l, g.im);
       }
@@ -547,7 +571,7 @@ static size_t cisd_gamma_smem(int N, int n) {
 static size_t cisd_gamma_f32_smem(int N, int n) {
   return (size_t)(n * N + 2 * n * n) * sizeof(double2) + (size_t)n * N * sizeof(double) +
          (size_t)(2 * n * N + N * N) * sizeof(float2) + (size_t)(N * N + ((N * N) & 1)) * sizeof(float) +
-         (size_t)N * n * 8;  // + lci1_g in float-float
+         (size_t)N * n * 8 + (size_t)n * n * 16;  // + lci1_g and lg1^T in float-float
 }
 
 // need_ham: the force bias / energy / step also read h1, chol and lci1
@@ -598,61 +622,63 @@ static Spins cisd_spins(const trot_cisd* c) {
   return sp;
 }
 
+// one timed kernel launch: CISD_LAUNCH("name", kernel, grid, block, smem, stream, args...)
+#define CISD_LAUNCH(name, kernel, grid, block, smem, st, ...)   \
+  TROT_TIMED(name, st, ([&]() -> int {                          \
+    kernel<<<grid, block, smem, st>>>(__VA_ARGS__);             \
+    TROT_CHECK_LAUNCH(name);                                    \
+    return TROT_OK;                                             \
+  })())
+
 // green, x, C_c / C_e, scalars; stage 0 = overlap only, 1 = + N x N matrices and chol contractions, 2 = + energy terms
 static int cisd_run(const trot_cisd* c, int W, const double2* w, CisdBuffers& b, int stage, cudaStream_t st) {
   const int N = c->norb, n = c->nocc, v = c->nvir, G = c->nchol, nv = n * v;
   Spins sp = cisd_spins(c);
   if (stage > 0) cudaMemsetAsync(b.status, 0, 4 * sizeof(int), st);
   TROT_TIMED("cisd_green", st, launch_green(sp, W, N, w, nullptr, b.green, b.det2, b.hg2, st));
-  cisd_x_kernel<<<W, 256, 0, st>>>(N, n, v, b.green, c->ci1, b.x, stage >= 1 ? b.ci1g1 : nullptr, b.wsc);
-  TROT_CHECK_LAUNCH("cisd_x_kernel");
-  TROT_TIMED("cisd_ci2g", st, launch_zgemm_cr(W, nv, nv, 1.0, b.x, nv, c->ci2m, nv, false, b.cg, nv, false, st));
+  CISD_LAUNCH("cisd_x", cisd_x_kernel, W, 256, 0, st, N, n, v, b.green, c->ci1, b.x,
+              stage >= 1 ? b.ci1g1 : nullptr, b.wsc);
+  TROT_TIMED("cisd_ci2g", st,
+             launch_zgemm_cr_splitk(W, nv, nv, 1.0, b.x, nv, c->ci2m, nv, false, b.cg, nv, false, b.kpart,
+                                    cisd_splitk(W, nv, nv), st));
   if (stage == 0) return TROT_OK;
   const size_t smem = cisd_mats_smem(N, n, v);
   if (smem > 40 * 1024) cudaFuncSetAttribute(cisd_mats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  TROT_TIMED("cisd_mats", st, ([&]() -> int {
-    cisd_mats_kernel<<<W, 256, smem, st>>>(N, n, v, b.green, c->ci1, b.cg, b.x, c->h1, b.m1, b.m2, b.wsc);
-    TROT_CHECK_LAUNCH("cisd_mats_kernel");
-    return TROT_OK;
-  })());
+  CISD_LAUNCH("cisd_mats", cisd_mats_kernel, W, 256, smem, st, N, n, v, b.green, c->ci1, b.cg, b.x, c->h1, b.m1,
+              b.m2, b.wsc);
   // lg = rot_chol . G  (rot_chol rows g: chol[g][:n][:] = first n N entries of chol_flat row g)
   TROT_TIMED("cisd_chol_gemm", st,
-             launch_zgemm_cr(W, G, n * N, 1.0, b.green, n * N, c->chol, N * N, true, b.lg, G, false, st));
-  TROT_TRY(launch_zgemm_cr(W, G, N * N, 1.0, b.m1, N * N, c->chol, N * N, true, b.lci1g, G, false, st));
-  TROT_TRY(launch_zgemm_cr(W, G, N * N, 1.0, b.m2, N * N, c->chol, N * N, true, b.lci2g, G, false, st));
+             launch_zgemm_cr_splitk(W, G, n * N, 1.0, b.green, n * N, c->chol, N * N, true, b.lg, G, false, b.kpart,
+                                    cisd_splitk(W, G, n * N), st));
+  // [lci1g; lci2g] = [ci1_green; ci2_green] . chol^T: one (2W, N^2) x (N^2, G) FP64 product.
+  // (FP32-class products here, as the reference's mixed_real_dtype contraction, move
+  // the local energy by ~1e-3 Ha at N=60, G=300: too far from FP64.)
+  TROT_TIMED("cisd_lci_gemm", st,
+             launch_zgemm_cr_splitk(2 * W, G, N * N, 1.0, b.m1, N * N, c->chol, N * N, true, b.lci1g, G, false,
+                                    b.kpart, cisd_splitk(2 * W, G, N * N), st));
   if (stage == 1) return TROT_OK;
   const int nch = cisd_chunks(G);
   if (c->gl_precision == TROT_MIXED) {
     const size_t smem2 = cisd_gamma_f32_smem(N, n);
     cudaFuncSetAttribute(cisd_gamma_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
-    TROT_TIMED("cisd_gamma_f32", st, ([&]() -> int {
-      cisd_gamma_f32_kernel<<<dim3(nch, W), 256, smem2, st>>>(N, n, v, G, b.green, c->chol, c->lci1, b.m2, b.ci1g1,
-                                                             b.xg, b.gpart);
-      TROT_CHECK_LAUNCH("cisd_gamma_f32_kernel");
-      return TROT_OK;
-    })());
+    CISD_LAUNCH("cisd_gamma_f32", cisd_gamma_f32_kernel, dim3(nch, W), 256, smem2, st, N, n, v, G, b.green, c->chol,
+                c->lci1, b.m2, b.ci1g1, b.xg, b.gpart);
   } else {
     const size_t smem2 = cisd_gamma_smem(N, n);
     cudaFuncSetAttribute(cisd_gamma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
-    TROT_TIMED("cisd_gamma", st, ([&]() -> int {
-      cisd_gamma_kernel<<<dim3(nch, W), 256, smem2, st>>>(N, n, v, G, b.green, c->chol, c->lci1, b.m2, b.ci1g1,
-                                                         b.xg, b.gpart);
-      TROT_CHECK_LAUNCH("cisd_gamma_kernel");
-      return TROT_OK;
-    })());
+    CISD_LAUNCH("cisd_gamma", cisd_gamma_kernel, dim3(nch, W), 256, smem2, st, N, n, v, G, b.green, c->chol, c->lci1,
+                b.m2, b.ci1g1, b.xg, b.gpart);
   }
   if (c->l2ci2_precision == TROT_MIXED) {
     TROT_TIMED("cisd_l2ci2_tc", st,
                launch_split3_gemm(W * G, nv, c->nvpad, c->ncpad, b.xg, c->ci2_image, b.xq, b.yd, b.status, st));
-    cisd_l2_reduce_tc_kernel<<<W, 256, 0, st>>>(G, nv, c->ncpad, b.xg, b.yd, b.wsc);
-    TROT_CHECK_LAUNCH("cisd_l2_reduce_tc_kernel");
+    CISD_LAUNCH("cisd_l2_reduce", cisd_l2_reduce_tc_kernel, W, 256, 0, st, G, nv, c->ncpad, b.xg, b.yd, b.wsc);
     return TROT_OK;
   }
   if ((size_t)W * G > 65535u * 64u) { set_error("CISD: W*G too large"); return TROT_ERR_UNSUPPORTED; }
   TROT_TIMED("cisd_l2ci2", st,
              launch_zgemm_cr(W * G, nv, nv, 1.0, b.xg, nv, c->ci2m, nv, false, b.y, nv, false, st));
-  cisd_l2_reduce_kernel<<<W, 256, 0, st>>>(G, nv, b.xg, b.y, b.wsc);
-  TROT_CHECK_LAUNCH("cisd_l2_reduce_kernel");
+  CISD_LAUNCH("cisd_l2_reduce", cisd_l2_reduce_kernel, W, 256, 0, st, G, nv, b.xg, b.y, b.wsc);
   return TROT_OK;
 }
 
@@ -787,13 +813,11 @@ int trot_cisd_prop_step(const trot_cisd* c, const trot_system* prop, const trot_
   // 1. force bias (and local energy) of the incoming walkers
   TROT_TRY(cisd_run(c, W, w, b, energy_out ? 2 : 1, st));
   const size_t wg = (size_t)W * G;
-  cisd_fb_kernel<<<(unsigned)((wg + 255) / 256), 256, 0, st>>>(W, G, b.wsc, b.lg, b.lci1g, b.lci2g, b.fb);
-  TROT_CHECK_LAUNCH("cisd_fb_kernel");
-  if (energy_out) {
-    cisd_energy_kernel<<<W, 256, 0, st>>>(G, cisd_chunks(G), c->h0, b.wsc, b.hg2, b.lg, b.lci1g, b.lci2g, b.gpart,
-                                          (double2*)energy_out);
-    TROT_CHECK_LAUNCH("cisd_energy_kernel");
-  }
+  CISD_LAUNCH("cisd_fb", cisd_fb_kernel, (unsigned)((wg + 255) / 256), 256, 0, st, W, G, b.wsc, b.lg, b.lci1g,
+              b.lci2g, b.fb);
+  if (energy_out)
+    CISD_LAUNCH("cisd_energy", cisd_energy_kernel, W, 256, 0, st, G, cisd_chunks(G), c->h0, b.wsc, b.hg2, b.lg,
+                b.lci1g, b.lci2g, b.gpart, (double2*)energy_out);
   // 2. shifted fields, 3. VHS, 4. propagation in place
   TROT_TIMED("fields", st,
              launch_fields(W, G, prop->sqrt_dt, b.fb, prop->mf_shifts_im, fields, b.xs, b.shift_term, b.fb_term, st));
@@ -812,13 +836,12 @@ int trot_cisd_prop_step(const trot_cisd* c, const trot_system* prop, const trot_
   }
   // 5. CISD overlaps of the new walkers, weights, population shift
   TROT_TRY(cisd_run(c, W, w, b, 0, st));
-  cisd_overlap_kernel<<<W, 256, 0, st>>>(c->nocc * c->nvir, b.x, b.cg, b.wsc, b.det2, b.ov_new);
-  TROT_CHECK_LAUNCH("cisd_overlap_kernel");
+  CISD_LAUNCH("cisd_overlap", cisd_overlap_kernel, W, 256, 0, st, c->nocc * c->nvir, b.x, b.cg, b.wsc, b.det2,
+              b.ov_new);
   a.overlaps = (double2*)state->overlaps; a.weights = state->weights; a.scalars = state->scalars;
   a.shift_term = b.shift_term; a.fb_term = b.fb_term; a.node_flag = b.node_flag;
   a.dt = prop->dt; a.h0_prop = prop->h0_prop; a.w_floor = prop->weight_floor; a.w_cap = prop->weight_cap;
-  cisd_weight_kernel<<<(W + 127) / 128, 128, 0, st>>>(a, b.ov_new);
-  TROT_CHECK_LAUNCH("cisd_weight_kernel");
+  CISD_LAUNCH("cisd_weight", cisd_weight_kernel, (W + 127) / 128, 128, 0, st, a, b.ov_new);
   TROT_TIMED("step_finalize", st,
              launch_step_finalize(W, state->weights, state->scalars, (long long*)state->node_encounters, b.node_flag,
                                   prop->pop_control_damping, prop->dt, st));

@@ -173,10 +173,12 @@ TROT_D double2 block_gauss_jordan(double2* A, int n, int ld, double2* inv, int* 
 namespace trot {
 void set_error(const char* fmt, ...);
 int cuda_status(cudaError_t e, const char* where);
+void prof_count_launch();  // profile.cu: counts launches while the timers are enabled
 }  // namespace trot
 
 #define TROT_CHECK_LAUNCH(where)                                      \
   do {                                                                \
+    trot::prof_count_launch();                                        \
     cudaError_t _e = cudaGetLastError();                              \
     if (_e != cudaSuccess) return trot::cuda_status(_e, where);       \
   } while (0)

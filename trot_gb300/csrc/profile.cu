@@ -3,6 +3,7 @@
 // trot_profile_collect() sums the elapsed times per kernel name.  Disabled by
 // default (zero cost); must stay disabled while a stream is being captured
 // into a CUDA graph.  Events come from a pool created at enable time.
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -18,11 +19,16 @@ struct Rec {
   int a, b;
 };
 std::mutex g_mu;
-bool g_on = false;
+std::atomic<bool> g_on{false};
+std::atomic<long long> g_launches{0};
 std::vector<cudaEvent_t> g_pool;
 size_t g_next = 0;
 std::vector<Rec> g_recs;
 }  // namespace
+
+void prof_count_launch() {
+  if (g_on.load(std::memory_order_relaxed)) g_launches.fetch_add(1, std::memory_order_relaxed);
+}
 
 int prof_begin(cudaStream_t st) {
   if (!g_on) return -1;
@@ -53,6 +59,7 @@ int trot_profile_enable(int max_launches) {
   g_pool.clear();
   g_recs.clear();
   g_next = 0;
+  g_launches = 0;
   g_on = max_launches > 0;
   for (int i = 0; i < 2 * max_launches; ++i) {
     cudaEvent_t e;
@@ -93,5 +100,9 @@ int trot_profile_collect(int max_names, char* names, double* total_ms, int* laun
   g_next = 0;
   return n;
 }
+
+// Kernel launches the library issued since trot_profile_enable (every launch,
+// timed or not).
+long long trot_profile_launch_count(void) { return g_launches.load(); }
 
 }  // extern "C"
