@@ -8,8 +8,9 @@
 //   ci2g = x . ci2m,  gci2g = sum ci2g o x,  ci1g = sum ci1 o x,
 //   ov = 1 + 2 ci1g + gci2g        (overlap = ov det(w_occ)^2)
 //   ci1_green = (gp ci1^T) G,  ci2_green = (gp ci2g^T) G   (N x N; gp rows < n: x, rows >= n: -I)
-//   force bias = (2 lg + 4 ci1g lg + 2 gci2g lg - 2 (lci1g + lci2g)) / ov
-//     with lg = rot_chol . G, lci{1,2}g = chol . ci{1,2}_green
+//   force bias = (2 lg + 4 ci1g lg + 2 gci2g lg - 2 lcs) / ov
+//     with lg = rot_chol . G, lcs = lci1g + lci2g = chol . (ci1_green + ci2_green)
+//     (the energy uses lci1g and lci2g only as -4 (lci1g + lci2g) . lg as well)
 //   local energy: the terms of energy_kernel_rw_rh, see cisd_energy_combine.
 // The l2ci2 quadratic forms 2 sum_g X_g^T ci2 X_g - X_g^T ci2_perm X_g (ci2_perm[(p,u),(q,t)] = ci2[p,t,q,u])
 // = sum_g X_g^T ci2m X_g (X_g = vec(glgp_g)) are one GEMM over all (walker, g) rows.
@@ -30,10 +31,13 @@ struct CisdBuffers {
   double2* x;                   // (W, n v) contiguous x
   double2* cg;                  // ci2g = x ci2m (W, n v)
   double2* ci1g1;               // (W, n, n)
-  double2 *m1, *m2;             // ci1_green, ci2_green (W, N, N), m2 = m1 + W N N
+  double2 *ms, *m2;             // ci1_green + ci2_green, ci2_green (W, N, N)
+  double2* p2;                  // P2 = gp ci2g^T (W, N, n): ci2_green = P2 G
   double2* wsc;                 // per-walker scalars (W, 8): ci1g, gci2g, e1_1_2, e1_2_2, ...
-  double2 *lg, *lci1g, *lci2g;  // (W, G), lci2g = lci1g + W G
+  double2 *lg, *lcs;            // (W, G): rot_chol . G, chol . (ci1_green + ci2_green)
   double2* kpart;               // split-K partials of the FP64 products
+  float* lf;                    // chol in FP32 (G, N, N)                    (FP32 gl)
+  ff *rd, *lc;                  // chol rows < n transposed, lci1: float-float (G, N, n)
   double2* xg;                  // glgp rows (W G, n v)
   double2* y;                   // xg ci2m (W G, n v)    (FP64 l2ci2)
   uint16_t* xq;                 // split3 image of xg    (mixed l2ci2)
@@ -70,17 +74,17 @@ static size_t carve_cisd(const trot_cisd* c, int W, int op, Carver& cv, CisdBuff
     size_t kp = (size_t)cisd_splitk(W, (int)nv, (int)nv) * W * nv;  // ci2g
     if (op != TROT_OP_OVERLAP) {
       kp = std::max(kp, (size_t)cisd_splitk(W, (int)G, (int)(n * N)) * W * G);  // lg
-      kp = std::max(kp, (size_t)cisd_splitk(2 * W, (int)G, (int)(N * N)) * 2 * W * G);  // lci1g, lci2g
+      kp = std::max(kp, (size_t)cisd_splitk(W, (int)G, (int)(N * N)) * W * G);  // lcs
     }
     b.kpart = cv.take<double2>(kp);
   }
   if (op == TROT_OP_OVERLAP) return cv.used;
   b.ci1g1 = cv.take<double2>(W * n * n);
-  b.m1 = cv.take<double2>(2 * W * N * N);
-  b.m2 = b.m1 + W * N * N;
+  b.ms = cv.take<double2>(W * N * N);
+  b.m2 = cv.take<double2>(W * N * N);
+  b.p2 = cv.take<double2>(W * N * n);
   b.lg = cv.take<double2>(W * G);
-  b.lci1g = cv.take<double2>(2 * W * G);
-  b.lci2g = b.lci1g + W * G;
+  b.lcs = cv.take<double2>(W * G);
   if (op == TROT_OP_FORCE_BIAS) return cv.used;
   b.xg = cv.take<double2>((size_t)W * G * nv);
   if (c->l2ci2_precision == TROT_MIXED) {
@@ -91,6 +95,11 @@ static size_t carve_cisd(const trot_cisd* c, int W, int op, Carver& cv, CisdBuff
     b.y = cv.take<double2>((size_t)W * G * nv);
   }
   b.gpart = cv.take<double2>((size_t)W * cisd_chunks((int)G) * 4);
+  if (c->gl_precision == TROT_MIXED) {
+    b.lf = cv.take<float>(G * N * N);
+    b.rd = cv.take<ff>(G * N * n);
+    b.lc = cv.take<ff>(G * N * n);
+  }
   if (op != TROT_OP_PROP_STEP) return cv.used;
   b.fb = cv.take<double2>((size_t)W * G);
   b.xs = cv.take<double2>((size_t)W * G);
@@ -130,12 +139,14 @@ __global__ void cisd_x_kernel(int N, int n, int v, const double2* __restrict__ g
 
 // ------------------------------------------------------------------ per-walker N x N matrices
 // gci2g = sum ci2g o x; P_Y = gp Y^T (N x n); M = P_Y G (N x N) for Y = ci1, ci2g;
-// e1_1_2 = -2 sum h1 o M1, e1_2_2 = -2 sum h1 o M2.
+// e1_1_2 = -2 sum h1 o M1, e1_2_2 = -2 sum h1 o M2.  Stores M1 + M2 (the force bias,
+// the energy and the 1-RDM use chol . ci1_green and chol . ci2_green only in that sum)
+// and M2 (lci2_green).
 __global__ void __launch_bounds__(256)
 cisd_mats_kernel(int N, int n, int v, const double2* __restrict__ green, const double* __restrict__ ci1,
                  const double2* __restrict__ cg, const double2* __restrict__ x,
-                 const double* __restrict__ h1, double2* __restrict__ m1, double2* __restrict__ m2,
-                 double2* __restrict__ wsc) {
+                 const double* __restrict__ h1, double2* __restrict__ ms, double2* __restrict__ m2,
+                 double2* __restrict__ p2o, double2* __restrict__ wsc) {
   extern __shared__ double2 sm[];
   __shared__ double2 red[32];
   const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
@@ -169,6 +180,7 @@ cisd_mats_kernel(int N, int n, int v, const double2* __restrict__ green, const d
     }
     P1[e] = a1;
     P2[e] = a2;
+    p2o[(size_t)b * N * n + e] = a2;
   }
   __syncthreads();
   double2 h1s = cmk(0.0, 0.0), h2s = cmk(0.0, 0.0);
@@ -180,7 +192,7 @@ cisd_mats_kernel(int N, int n, int v, const double2* __restrict__ green, const d
       cfma(s1, P1[i * n + p], gv);
       cfma(s2, P2[i * n + p], gv);
     }
-    m1[(size_t)b * N * N + e] = s1;
+    ms[(size_t)b * N * N + e] = cadd(s1, s2);
     m2[(size_t)b * N * N + e] = s2;
     const double hv = h1[e];
     crfma(h1s, hv, s1);
@@ -280,12 +292,14 @@ cisd_gamma_kernel(int N, int n, int v, int G, const double2* __restrict__ green,
   }
 }
 
-// Same sums as cisd_gamma_kernel with gl = G L and lci2_green = R M2^T in FP32
-// (the reference's float32 mixed dtype; sums accumulated in float-float), and lg1 =
-// R G^T, lci1g = lci1^T G^T and their products in float-float (FP32 pairs, ~2^-44
-// relative: FP64-level results on the FP32 pipe; GB300's FP64 pipe runs a few
-// operations per clock per SM).  Double -> float / float-float conversions by integer
-// operations (ff.cuh) for the same reason.
+// Same sums as cisd_gamma_kernel with gl = G L in FP32 (the reference's float32 mixed
+// dtype; sums accumulated in float-float), and lg1 = R G^T, lci1g = lci1^T G^T and
+// their products in float-float (FP32 pairs, ~2^-44 relative: FP64-level results on
+// the FP32 pipe; GB300's FP64 pipe runs a few operations per clock per SM).  With
+// ci2_green = P2 G (rank n), lci2_green = R ci2_green^T = lg1 P2^T, so the fourth sum
+// sum_pj gl[p][j] lci2_green[p][j] = sum_pk lg1[p][k] (gl P2)[p][k]: an n x N x n
+// product (FP32) instead of the n x N x N one.  Double -> float / float-float
+// conversions by integer operations (ff.cuh) for the same reason.
 TROT_D void ffc_mad(ffc& acc, const ffc& a, const ffc& b) {  // acc += a b (complex)
   ff_mad(acc.re, a.re, b.re);
   ff_mad(acc.re, ff{-a.im.hi, -a.im.lo}, b.im);
@@ -295,9 +309,36 @@ TROT_D void ffc_mad(ffc& acc, const ffc& a, const ffc& b) {  // acc += a b (comp
 TROT_D ffc ffc_norm(ffc a) { return ffc{ff_fast(a.re.hi, a.re.lo), ff_fast(a.im.hi, a.im.lo)}; }
 TROT_D double2 ffc_d(ffc a) { return make_double2(ff_d(a.re), ff_d(a.im)); }
 
+// chol and lci1 in the operand forms of cisd_gamma_f32_kernel, once per call:
+// lf = chol in FP32 (G, N, N); rd[g][j][p] = chol[g][p][j] (p < n) and lc[g][i][q] =
+// lci1[g][i][q] in float-float.
+__global__ void cisd_chol_forms_kernel(int N, int n, int G, const double* __restrict__ chol,
+                                       const double* __restrict__ lci1, float* __restrict__ lf, ff* __restrict__ rd,
+                                       ff* __restrict__ lc) {
+  const size_t NN = (size_t)N * N, total = (size_t)G * NN;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t g = e / NN;
+    const int r = (int)(e % NN), p = r / N, j = r % N;
+    const double l = chol[e];
+    lf[e] = d2f_bits(l);
+    if (p < n) rd[g * N * n + (size_t)j * n + p] = ff_from_d(l);
+    if (r < N * n) lc[g * N * n + r] = ff_from_d(lci1[g * N * n + r]);
+  }
+}
+
+// Four lanes hold partial sums of one item: add them (all lanes of the warp take part)
+TROT_D ffc ffc_quad_sum(ffc a) {
+#pragma unroll
+  for (int o = 1; o < 4; o <<= 1) {
+    a.re = ff_add(a.re, ff_shfl_xor(a.re, o));
+    a.im = ff_add(a.im, ff_shfl_xor(a.im, o));
+  }
+  return a;
+}
+
 __global__ void __launch_bounds__(256)
-cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ green, const double* __restrict__ chol,
-                      const double* __restrict__ lci1, const double2* __restrict__ m2,
+cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ green, const float* __restrict__ lf,
+                      const ff* __restrict__ rd, const ff* __restrict__ lc, const double2* __restrict__ p2,
                       const double2* __restrict__ ci1g1, double2* __restrict__ xg, double2* __restrict__ gpart) {
   extern __shared__ double2 sm[];
   __shared__ double2 red[32];
@@ -310,8 +351,8 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
   ffc* A = C1 + n * n;                                    // n x n  (lg1)
   ff* RdT = reinterpret_cast<ff*>(A + n * n);             // N x n  (rows < n of L_g, transposed)
   float2* Gf = reinterpret_cast<float2*>(RdT + n * N);    // n x N
-  float2* M2f = Gf + n * N;                               // N x N, transposed
-  float2* GLf = M2f + N * N;                              // n x N
+  float2* P2f = Gf + n * N;                               // N x n
+  float2* GLf = P2f + N * n;                              // n x N
   float* Lf = reinterpret_cast<float*>(GLf + n * N);      // N x N
   ff* Lc = reinterpret_cast<ff*>(Lf + N * N + ((N * N) & 1));  // N x n: lci1_g
   ffc* AT = reinterpret_cast<ffc*>(Lc + N * n);           // n x n: lg1 transposed
@@ -320,10 +361,9 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
     GsT[(e % N) * n + e / N] = ffc{ff_from_d(g.x), ff_from_d(g.y)};
     Gf[e] = make_float2(d2f_bits(g.x), d2f_bits(g.y));
   }
-  for (int e = tid; e < N * N; e += nt) {  // stored transposed: M2f[i][j] = M2[j][i]
-    const double2 m = m2[(size_t)b * N * N + e];
-    const int j = e / N, i = e % N;
-    M2f[i * N + j] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
+  for (int e = tid; e < N * n; e += nt) {
+    const double2 m = p2[(size_t)b * N * n + e];
+    P2f[e] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
   }
   for (int e = tid; e < n * n; e += nt) {
     const double2 c = ci1g1[(size_t)b * n * n + e];
@@ -332,29 +372,37 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
   const ffc z{{0.f, 0.f}, {0.f, 0.f}};
   ffc s0 = z, s1 = z, s2 = z, s3 = z;
   const int g0 = chunk * kCisdGChunk, g1 = min(G, g0 + kCisdGChunk);
+  // the float-float n x n phases run four lanes per (p, q), each over every fourth term
+  const int quad = tid >> 2, part = tid & 3, nq = nt >> 2;
   for (int gg = g0; gg < g1; ++gg) {
     __syncthreads();
-    const double* Lg = chol + (size_t)gg * N * N;
-    for (int e = tid; e < N * N; e += nt) {
-      const double l = Lg[e];
-      Lf[e] = d2f_bits(l);
-      if (e < n * N) RdT[(e % N) * n + e / N] = ff_from_d(l);
+    const float* lg = lf + (size_t)gg * N * N;
+    for (int e = tid; e < N * N; e += nt) Lf[e] = lg[e];
+    const ff* rg = rd + (size_t)gg * N * n;
+    const ff* cg = lc + (size_t)gg * N * n;
+    for (int e = tid; e < N * n; e += nt) {
+      RdT[e] = rg[e];
+      Lc[e] = cg[e];
     }
-    const double* lc = lci1 + (size_t)gg * N * n;
-    for (int e = tid; e < N * n; e += nt) Lc[e] = ff_from_d(lc[e]);
     __syncthreads();
-    for (int e = tid; e < n * n; e += nt) {  // lg1[p][q] = sum_j R[p][j] G[q][j]
-      const int p = e / n, q = e % n;
+    for (int e0 = 0; e0 < n * n; e0 += nq) {  // lg1[p][q] = sum_j R[p][j] G[q][j]
+      const int e = e0 + quad;
       ffc a = z;
-      for (int j = 0; j < N; ++j) {
-        const ff r = RdT[j * n + p];
-        const ffc g = GsT[j * n + q];
-        ff_mad(a.re, r, g.re);
-        ff_mad(a.im, r, g.im);
+      if (e < n * n) {
+        const int p = e / n, q = e % n;
+        for (int j = part; j < N; j += 4) {
+          const ff r = RdT[j * n + p];
+          const ffc g = GsT[j * n + q];
+          ff_mad(a.re, r, g.re);
+          ff_mad(a.im, r, g.im);
+        }
+        a = ffc_norm(a);
       }
-      a = ffc_norm(a);
-      A[e] = a;
-      AT[q * n + p] = a;
+      a = ffc_quad_sum(a);
+      if (e < n * n && part == 0) {
+        A[e] = a;
+        AT[(e % n) * n + e / n] = a;
+      }
     }
     for (int e = tid; e < n * N; e += nt) {
       const int p = e / N, i = e % N;
@@ -368,33 +416,41 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
       GLf[e] = make_float2(ar, ai);
     }
     __syncthreads();
-    for (int e = tid; e < n * n; e += nt) {
-      const int p = e / n, q = e % n;
-      const ffc apq = A[p * n + q];
-      ffc_mad(s0, apq, AT[p * n + q]);
-      ffc t = z;
-      for (int a2 = 0; a2 < n; ++a2) ffc_mad(t, AT[a2 * n + q], C1[a2 * n + p]);
-      ffc_mad(s1, apq, ffc_norm(t));
-      ffc bq = z;  // lci1g[q][p] = sum_i lci1[i][q] G[p][i]
-      for (int i = 0; i < N; ++i) {
-        const ff l = Lc[i * n + q];
-        const ffc g = GsT[i * n + p];
-        ff_mad(bq.re, l, g.re);
-        ff_mad(bq.im, l, g.im);
+    for (int e0 = 0; e0 < n * n; e0 += nq) {
+      const int e = e0 + quad;
+      ffc t = z, bq = z;
+      float zr = 0.f, zi = 0.f;
+      if (e < n * n) {
+        const int p = e / n, q = e % n;
+        for (int a2 = part; a2 < n; a2 += 4) ffc_mad(t, AT[a2 * n + q], C1[a2 * n + p]);
+        for (int i = part; i < N; i += 4) {  // lci1g[q][p] = sum_i lci1[i][q] G[p][i]
+          const ff l = Lc[i * n + q];
+          const ffc g = GsT[i * n + p];
+          ff_mad(bq.re, l, g.re);
+          ff_mad(bq.im, l, g.im);
+        }
+        for (int j = part; j < N; j += 4) {  // (gl P2)[p][q]
+          const float2 a = GLf[p * N + j], m = P2f[j * n + q];
+          zr = fmaf(a.x, m.x, fmaf(-a.y, m.y, zr));
+          zi = fmaf(a.x, m.y, fmaf(a.y, m.x, zi));
+        }
+        t = ffc_norm(t);
+        bq = ffc_norm(bq);
       }
-      ffc_mad(s2, ffc_norm(bq), apq);
-    }
-    for (int e = tid; e < n * N; e += nt) {
-      const int p = e / N, j = e % N;
-      float ar = 0.f, ai = 0.f;
-      for (int i = 0; i < N; ++i) {
-        const float l = Lf[p * N + i];
-        const float2 m = M2f[i * N + j];  // consecutive j across the warp
-        ar = fmaf(l, m.x, ar);
-        ai = fmaf(l, m.y, ai);
+      t = ffc_quad_sum(t);
+      bq = ffc_quad_sum(bq);
+#pragma unroll
+      for (int o = 1; o < 4; o <<= 1) {
+        zr += __shfl_xor_sync(0xffffffffu, zr, o);
+        zi += __shfl_xor_sync(0xffffffffu, zi, o);
       }
-      const float2 gl = GLf[e];
-      ffc_mad(s3, ffc{ff{gl.x, 0.f}, ff{gl.y, 0.f}}, ffc{ff{ar, 0.f}, ff{ai, 0.f}});
+      if (e < n * n && part == 0) {
+        const ffc apq = A[e];
+        ffc_mad(s0, apq, AT[e]);
+        ffc_mad(s1, apq, t);
+        ffc_mad(s2, bq, apq);
+        ffc_mad(s3, apq, ffc{ff{zr, 0.f}, ff{zi, 0.f}});
+      }
     }
     s0 = ffc_norm(s0);
     s1 = ffc_norm(s1);
@@ -482,9 +538,9 @@ __global__ void cisd_overlap_kernel(int nv, const double2* __restrict__ x, const
   }
 }
 
-// force bias: (2 lg (1 + 2 ci1g + gci2g) - 2 (lci1g + lci2g)) / ov
+// force bias: (2 lg (1 + 2 ci1g + gci2g) - 2 lcs) / ov,  lcs = lci1g + lci2g
 __global__ void cisd_fb_kernel(int W, int G, const double2* __restrict__ wsc, const double2* __restrict__ lg,
-                               const double2* __restrict__ l1, const double2* __restrict__ l2, double2* __restrict__ fb) {
+                               const double2* __restrict__ lcs, double2* __restrict__ fb) {
   const size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (k >= (size_t)W * G) return;
   const int b = (int)(k / G);
@@ -493,15 +549,14 @@ __global__ void cisd_fb_kernel(int W, int G, const double2* __restrict__ wsc, co
   const double2 f = cmk(2.0 * ci1g.x + gci2g.x, 2.0 * ci1g.y + gci2g.y);  // (ov - 1)
   // 2 lg + 4 ci1g lg + 2 gci2g lg = 2 lg (1 + 2 ci1g + gci2g) = 2 lg ov
   const double2 a = cmul(lg[k], cmk(2.0 * (1.0 + f.x), 2.0 * f.y));
-  const double2 c = cadd(l1[k], l2[k]);
+  const double2 c = lcs[k];
   fb[k] = cdiv(cmk(a.x - 2.0 * c.x, a.y - 2.0 * c.y), ov);
 }
 
 // mixed-estimator 1-RDM (trot/meas/cisd.py:772-820): gamma = G0 - (ci1_green + ci2_green) / ov,
 // G0[i][j] = G[j][i] for j < n, 0 otherwise
-__global__ void cisd_rdm1_kernel(int N, int n, const double2* __restrict__ green, const double2* __restrict__ m1,
-                                 const double2* __restrict__ m2, const double2* __restrict__ wsc,
-                                 double2* __restrict__ out) {
+__global__ void cisd_rdm1_kernel(int N, int n, const double2* __restrict__ green, const double2* __restrict__ ms,
+                                 const double2* __restrict__ wsc, double2* __restrict__ out) {
   const int b = blockIdx.y;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= N * N) return;
@@ -509,7 +564,7 @@ __global__ void cisd_rdm1_kernel(int N, int n, const double2* __restrict__ green
   const double2 ci1g = wsc[(size_t)b * 8 + 0], gci2g = wsc[(size_t)b * 8 + 1];
   const double2 ov = cmk(1.0 + 2.0 * ci1g.x + gci2g.x, 2.0 * ci1g.y + gci2g.y);
   const size_t k = (size_t)b * N * N + e;
-  const double2 corr = cdiv(cadd(m1[k], m2[k]), ov);
+  const double2 corr = cdiv(ms[k], ov);
   const double2 g0 = j < n ? green[(size_t)b * n * N + (size_t)j * N + i] : cmk(0.0, 0.0);
   out[k] = csub(g0, corr);
 }
@@ -523,23 +578,21 @@ __global__ void cisd_weight_kernel(TrotterArgs a, const double2* __restrict__ ov
 // local energy (trot/meas/cisd.py:608-769)
 __global__ void __launch_bounds__(256)
 cisd_energy_kernel(int G, int nchunk, double h0, const double2* __restrict__ wsc, const double2* __restrict__ hg2,
-                   const double2* __restrict__ lg, const double2* __restrict__ l1, const double2* __restrict__ l2,
+                   const double2* __restrict__ lg, const double2* __restrict__ lcs,
                    const double2* __restrict__ gpart, double2* __restrict__ energy) {
   __shared__ double2 red[32];
   const int b = blockIdx.x;
-  double2 lglg = cmk(0.0, 0.0), l1lg = cmk(0.0, 0.0), l2lg = cmk(0.0, 0.0);
+  double2 lglg = cmk(0.0, 0.0), lslg = cmk(0.0, 0.0);
   for (int g = threadIdx.x; g < G; g += blockDim.x) {
     const double2 x = lg[(size_t)b * G + g];
     cfma(lglg, x, x);
-    cfma(l1lg, l1[(size_t)b * G + g], x);
-    cfma(l2lg, l2[(size_t)b * G + g], x);
+    cfma(lslg, lcs[(size_t)b * G + g], x);
   }
   double2 p[4] = {cmk(0.0, 0.0), cmk(0.0, 0.0), cmk(0.0, 0.0), cmk(0.0, 0.0)};
   for (int c = threadIdx.x; c < nchunk; c += blockDim.x)
     for (int k = 0; k < 4; ++k) p[k] = cadd(p[k], gpart[((size_t)b * nchunk + c) * 4 + k]);
   lglg = block_sum2(lglg, red);
-  l1lg = block_sum2(l1lg, red);
-  l2lg = block_sum2(l2lg, red);
+  lslg = block_sum2(lslg, red);
   for (int k = 0; k < 4; ++k) p[k] = block_sum2(p[k], red);
   if (threadIdx.x == 0) {
     const double2 ci1g = wsc[(size_t)b * 8 + 0], gci2g = wsc[(size_t)b * 8 + 1];
@@ -549,13 +602,12 @@ cisd_energy_kernel(int G, int nchunk, double h0, const double2* __restrict__ wsc
     // one body
     const double2 e1 = cadd(cadd(cadd(hg, cmul(cscale(ci1g, 2.0), hg)), e1_1_2),
                             cadd(cmul(hg, gci2g), e1_2_2));
-    // two body
+    // two body; the lci1g . lg terms (2 e2_1_2 = -4 lci1g . lg) and the lci2g . lg term
+    // (4 e2_2_2_1 = -4 lci2g . lg) are summed as -4 lcs . lg
     const double2 e2_0 = csub(cscale(lglg, 2.0), p[0]);
-    const double2 e2_1 = cadd(cmul(cscale(e2_0, 2.0), ci1g),
-                              cscale(cadd(cadd(cscale(l1lg, -2.0), p[1]), cscale(p[2], -1.0)), 2.0));
-    const double2 e2_2 = cadd(cadd(cmul(e2_0, gci2g), cscale(cadd(cscale(l2lg, -1.0), cscale(p[3], 0.5)), 4.0)),
-                              l2ci2);
-    const double2 e2 = cadd(cadd(e2_0, e2_1), e2_2);
+    const double2 e2_1 = cadd(cmul(cscale(e2_0, 2.0), ci1g), cscale(csub(p[1], p[2]), 2.0));
+    const double2 e2_2 = cadd(cadd(cmul(e2_0, gci2g), cscale(p[3], 2.0)), l2ci2);
+    const double2 e2 = cadd(cadd(cadd(e2_0, e2_1), e2_2), cscale(lslg, -4.0));
     const double2 ov = cmk(1.0 + 2.0 * ci1g.x + gci2g.x, 2.0 * ci1g.y + gci2g.y);
     const double2 e = cdiv(cadd(e1, e2), ov);
     energy[b] = cmk(e.x + h0, e.y);
@@ -570,7 +622,7 @@ static size_t cisd_gamma_smem(int N, int n) {
 
 static size_t cisd_gamma_f32_smem(int N, int n) {
   return (size_t)(n * N + 2 * n * n) * sizeof(double2) + (size_t)n * N * sizeof(double) +
-         (size_t)(2 * n * N + N * N) * sizeof(float2) + (size_t)(N * N + ((N * N) & 1)) * sizeof(float) +
+         (size_t)(3 * n * N) * sizeof(float2) + (size_t)(N * N + ((N * N) & 1)) * sizeof(float) +
          (size_t)N * n * 8 + (size_t)n * n * 16;  // + lci1_g and lg1^T in float-float
 }
 
@@ -644,25 +696,28 @@ static int cisd_run(const trot_cisd* c, int W, const double2* w, CisdBuffers& b,
   if (stage == 0) return TROT_OK;
   const size_t smem = cisd_mats_smem(N, n, v);
   if (smem > 40 * 1024) cudaFuncSetAttribute(cisd_mats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  CISD_LAUNCH("cisd_mats", cisd_mats_kernel, W, 256, smem, st, N, n, v, b.green, c->ci1, b.cg, b.x, c->h1, b.m1,
-              b.m2, b.wsc);
+  CISD_LAUNCH("cisd_mats", cisd_mats_kernel, W, 256, smem, st, N, n, v, b.green, c->ci1, b.cg, b.x, c->h1, b.ms,
+              b.m2, b.p2, b.wsc);
   // lg = rot_chol . G  (rot_chol rows g: chol[g][:n][:] = first n N entries of chol_flat row g)
   TROT_TIMED("cisd_chol_gemm", st,
              launch_zgemm_cr_splitk(W, G, n * N, 1.0, b.green, n * N, c->chol, N * N, true, b.lg, G, false, b.kpart,
                                     cisd_splitk(W, G, n * N), st));
-  // [lci1g; lci2g] = [ci1_green; ci2_green] . chol^T: one (2W, N^2) x (N^2, G) FP64 product.
+  // lcs = (ci1_green + ci2_green) . chol^T: one (W, N^2) x (N^2, G) FP64 product.
   // (FP32-class products here, as the reference's mixed_real_dtype contraction, move
   // the local energy by ~1e-3 Ha at N=60, G=300: too far from FP64.)
   TROT_TIMED("cisd_lci_gemm", st,
-             launch_zgemm_cr_splitk(2 * W, G, N * N, 1.0, b.m1, N * N, c->chol, N * N, true, b.lci1g, G, false,
-                                    b.kpart, cisd_splitk(2 * W, G, N * N), st));
+             launch_zgemm_cr_splitk(W, G, N * N, 1.0, b.ms, N * N, c->chol, N * N, true, b.lcs, G, false,
+                                    b.kpart, cisd_splitk(W, G, N * N), st));
   if (stage == 1) return TROT_OK;
   const int nch = cisd_chunks(G);
   if (c->gl_precision == TROT_MIXED) {
     const size_t smem2 = cisd_gamma_f32_smem(N, n);
     cudaFuncSetAttribute(cisd_gamma_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
-    CISD_LAUNCH("cisd_gamma_f32", cisd_gamma_f32_kernel, dim3(nch, W), 256, smem2, st, N, n, v, G, b.green, c->chol,
-                c->lci1, b.m2, b.ci1g1, b.xg, b.gpart);
+    const size_t gnn = (size_t)G * N * N;
+    CISD_LAUNCH("cisd_chol_forms", cisd_chol_forms_kernel, (unsigned)std::min<size_t>((gnn + 255) / 256, 152 * 16),
+                256, 0, st, N, n, G, c->chol, c->lci1, b.lf, b.rd, b.lc);
+    CISD_LAUNCH("cisd_gamma_f32", cisd_gamma_f32_kernel, dim3(nch, W), 256, smem2, st, N, n, v, G, b.green, b.lf,
+                b.rd, b.lc, b.p2, b.ci1g1, b.xg, b.gpart);
   } else {
     const size_t smem2 = cisd_gamma_smem(N, n);
     cudaFuncSetAttribute(cisd_gamma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
@@ -725,8 +780,7 @@ int trot_cisd_force_bias(const trot_cisd* c, int W, const double* walkers, doubl
   cudaStream_t st = (cudaStream_t)stream;
   TROT_TRY(cisd_run(c, W, (const double2*)walkers, b, 1, st));
   const size_t n = (size_t)W * c->nchol;
-  cisd_fb_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(W, c->nchol, b.wsc, b.lg, b.lci1g, b.lci2g,
-                                                             (double2*)out);
+  cisd_fb_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(W, c->nchol, b.wsc, b.lg, b.lcs, (double2*)out);
   TROT_CHECK_LAUNCH("cisd_fb_kernel");
   return TROT_OK;
 }
@@ -741,8 +795,8 @@ int trot_cisd_local_energy(const trot_cisd* c, int W, const double* walkers, dou
   if (!cv.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, cv.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
   cudaStream_t st = (cudaStream_t)stream;
   TROT_TRY(cisd_run(c, W, (const double2*)walkers, b, 2, st));
-  cisd_energy_kernel<<<W, 256, 0, st>>>(c->nchol, cisd_chunks(c->nchol), c->h0, b.wsc, b.hg2, b.lg, b.lci1g,
-                                        b.lci2g, b.gpart, (double2*)out);
+  cisd_energy_kernel<<<W, 256, 0, st>>>(c->nchol, cisd_chunks(c->nchol), c->h0, b.wsc, b.hg2, b.lg, b.lcs,
+                                        b.gpart, (double2*)out);
   TROT_CHECK_LAUNCH("cisd_energy_kernel");
   return TROT_OK;
 }
@@ -758,7 +812,7 @@ int trot_cisd_rdm1(const trot_cisd* c, int W, const double* walkers, double* out
   cudaStream_t st = (cudaStream_t)stream;
   TROT_TRY(cisd_run(c, W, (const double2*)walkers, b, 1, st));
   const int N = c->norb;
-  cisd_rdm1_kernel<<<dim3((N * N + 255) / 256, W), 256, 0, st>>>(N, c->nocc, b.green, b.m1, b.m2, b.wsc,
+  cisd_rdm1_kernel<<<dim3((N * N + 255) / 256, W), 256, 0, st>>>(N, c->nocc, b.green, b.ms, b.wsc,
                                                                 (double2*)out);
   TROT_CHECK_LAUNCH("cisd_rdm1_kernel");
   return TROT_OK;
@@ -813,11 +867,11 @@ int trot_cisd_prop_step(const trot_cisd* c, const trot_system* prop, const trot_
   // 1. force bias (and local energy) of the incoming walkers
   TROT_TRY(cisd_run(c, W, w, b, energy_out ? 2 : 1, st));
   const size_t wg = (size_t)W * G;
-  CISD_LAUNCH("cisd_fb", cisd_fb_kernel, (unsigned)((wg + 255) / 256), 256, 0, st, W, G, b.wsc, b.lg, b.lci1g,
-              b.lci2g, b.fb);
+  CISD_LAUNCH("cisd_fb", cisd_fb_kernel, (unsigned)((wg + 255) / 256), 256, 0, st, W, G, b.wsc, b.lg, b.lcs,
+              b.fb);
   if (energy_out)
     CISD_LAUNCH("cisd_energy", cisd_energy_kernel, W, 256, 0, st, G, cisd_chunks(G), c->h0, b.wsc, b.hg2, b.lg,
-                b.lci1g, b.lci2g, b.gpart, (double2*)energy_out);
+                b.lcs, b.gpart, (double2*)energy_out);
   // 2. shifted fields, 3. VHS, 4. propagation in place
   TROT_TIMED("fields", st,
              launch_fields(W, G, prop->sqrt_dt, b.fb, prop->mf_shifts_im, fields, b.xs, b.shift_term, b.fb_term, st));
