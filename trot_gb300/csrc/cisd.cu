@@ -43,12 +43,14 @@ struct CisdBuffers {
   uint16_t* xq;                 // split3 image of xg    (mixed l2ci2)
   float* yd;                    // xg ci2m, FP32         (mixed l2ci2)
   double2* gpart;               // per (walker, gamma chunk) partial sums (W, nchunk, 4)
+  double2* l2part;              // l2ci2 partial sums (W, kL2Parts)
   // propagation step
   double2 *fb, *xs, *shift_term, *fb_term, *vhs, *ov_new;
   int* node_flag;
 };
 
 static constexpr int kCisdGChunk = 8;
+static constexpr int kL2Parts = 8;  // CTAs per walker of the l2ci2 reductions
 static int cisd_chunks(int G) { return (G + kCisdGChunk - 1) / kCisdGChunk; }
 
 // K slices for an FP64 product (M x Nn, long K) so that its 64 x 64 tiles fill
@@ -95,6 +97,7 @@ static size_t carve_cisd(const trot_cisd* c, int W, int op, Carver& cv, CisdBuff
     b.y = cv.take<double2>((size_t)W * G * nv);
   }
   b.gpart = cv.take<double2>((size_t)W * cisd_chunks((int)G) * 4);
+  b.l2part = cv.take<double2>((size_t)W * kL2Parts);
   if (c->gl_precision == TROT_MIXED) {
     b.lf = cv.take<float>(G * N * N);
     b.rd = cv.take<ff>(G * N * n);
@@ -336,7 +339,7 @@ TROT_D ffc ffc_quad_sum(ffc a) {
   return a;
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ green, const float* __restrict__ lf,
                       const ff* __restrict__ rd, const ff* __restrict__ lc, const double2* __restrict__ p2,
                       const double2* __restrict__ ci1g1, double2* __restrict__ xg, double2* __restrict__ gpart) {
@@ -350,17 +353,23 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
   ffc* C1 = GsT + n * N;                                  // n x n
   ffc* A = C1 + n * n;                                    // n x n  (lg1)
   ff* RdT = reinterpret_cast<ff*>(A + n * n);             // N x n  (rows < n of L_g, transposed)
+  const int ne = (n + 1) & ~1;                            // even row stride of GfT
   float2* Gf = reinterpret_cast<float2*>(RdT + n * N);    // n x N
   float2* P2f = Gf + n * N;                               // N x n
   float2* GLf = P2f + N * n;                              // n x N
-  float* Lf = reinterpret_cast<float*>(GLf + n * N);      // N x N
+  float2* GfT = GLf + n * N;                              // N x ne: GfT[j][p] = G[p][j] (16-byte pairs)
+  float* Lf = reinterpret_cast<float*>(GfT + N * ne);     // N x N
   ff* Lc = reinterpret_cast<ff*>(Lf + N * N + ((N * N) & 1));  // N x n: lci1_g
   ffc* AT = reinterpret_cast<ffc*>(Lc + N * n);           // n x n: lg1 transposed
   for (int e = tid; e < n * N; e += nt) {
     const double2 g = green[(size_t)b * n * N + e];
     GsT[(e % N) * n + e / N] = ffc{ff_from_d(g.x), ff_from_d(g.y)};
-    Gf[e] = make_float2(d2f_bits(g.x), d2f_bits(g.y));
+    const float2 gf = make_float2(d2f_bits(g.x), d2f_bits(g.y));
+    Gf[e] = gf;
+    GfT[(e % N) * ne + e / N] = gf;
   }
+  if (n & 1)
+    for (int j = tid; j < N; j += nt) GfT[j * ne + n] = make_float2(0.f, 0.f);
   for (int e = tid; e < N * n; e += nt) {
     const double2 m = p2[(size_t)b * N * n + e];
     P2f[e] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
@@ -404,16 +413,19 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
         AT[(e % n) * n + e / n] = a;
       }
     }
-    for (int e = tid; e < n * N; e += nt) {
-      const int p = e / N, i = e % N;
-      float ar = 0.f, ai = 0.f;
+    for (int e = tid; e < (ne / 2) * N; e += nt) {  // gl = G L: rows p, p + 1 per thread
+      const int p = 2 * (e / N), i = e % N;
+      float a0r = 0.f, a0i = 0.f, a1r = 0.f, a1i = 0.f;
       for (int j = 0; j < N; ++j) {
         const float l = Lf[j * N + i];
-        const float2 g = Gf[p * N + j];
-        ar = fmaf(l, g.x, ar);
-        ai = fmaf(l, g.y, ai);
+        const float4 g = *reinterpret_cast<const float4*>(GfT + j * ne + p);
+        a0r = fmaf(l, g.x, a0r);
+        a0i = fmaf(l, g.y, a0i);
+        a1r = fmaf(l, g.z, a1r);
+        a1i = fmaf(l, g.w, a1i);
       }
-      GLf[e] = make_float2(ar, ai);
+      GLf[p * N + i] = make_float2(a0r, a0i);
+      if (p + 1 < n) GLf[(p + 1) * N + i] = make_float2(a1r, a1i);
     }
     __syncthreads();
     for (int e0 = 0; e0 < n * n; e0 += nq) {
@@ -481,36 +493,55 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
 
 // l2ci2 from the tensor-core product: Y = xg ci2m in FP32, rows 2r (Re) / 2r+1 (Im) of yd
 // (row stride ldy); per walker sum over g of X_g . Y_g, FP64 accumulation.
-__global__ void cisd_l2_reduce_tc_kernel(int G, int nv, int ldy, const double2* __restrict__ xg,
-                                         const float* __restrict__ yd, double2* __restrict__ wsc) {
+// l2ci2 partial sums: CTA (c, b) takes Cholesky rows [c G/P, (c+1) G/P) of walker b
+// (a warp per row, lanes along nv) and writes part[b][c] (P = kL2Parts); the energy
+// kernel adds the P partials in order.
+
+// Y is FP32 and X is rounded to FP32 (by integer operations): FP32 complex products,
+// summed per thread in float-float and across the block in FP64 (no FP64-pipe work
+// per element)
+__global__ void __launch_bounds__(256)
+cisd_l2_reduce_tc_kernel(int G, int nv, int ldy, const double2* __restrict__ xg, const float* __restrict__ yd,
+                         double2* __restrict__ part) {
   __shared__ double2 red[32];
-  const int b = blockIdx.x;
-  double2 acc = cmk(0.0, 0.0);
-  const size_t cnt = (size_t)G * nv;
-  for (size_t e = threadIdx.x; e < cnt; e += blockDim.x) {
-    const size_t r = (size_t)b * G + e / nv;
-    const int k = (int)(e % nv);
-    const double2 xv = xg[r * nv + k];
-    const float* yr = yd + 2 * r * (size_t)ldy;
-    const float* yi = yr + ldy;
-    cfma(acc, xv, cmk((double)yr[k], (double)yi[k]));
+  const int c = blockIdx.x, b = blockIdx.y, nparts = gridDim.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int gpp = (G + nparts - 1) / nparts, g0 = c * gpp, g1 = min(G, g0 + gpp);
+  ff ar{0.f, 0.f}, ai{0.f, 0.f};
+  for (int g = g0 + warp; g < g1; g += nw) {
+    const size_t r = (size_t)b * G + g;
+    const double2* xr = xg + r * nv;
+    const float* y0 = yd + 2 * r * (size_t)ldy;
+    const float* y1 = y0 + ldy;
+    for (int k = lane; k < nv; k += 32) {
+      const double2 xv = xr[k];
+      const float xre = d2f_bits(xv.x), xim = d2f_bits(xv.y);
+      const float yr = y0[k], yi = y1[k];
+      const float pr = fmaf(xre, yr, __fmul_rn(-xim, yi)), pi = fmaf(xre, yi, __fmul_rn(xim, yr));
+      const ff tr = ff_two_sum(ar.hi, pr), ti = ff_two_sum(ai.hi, pi);
+      ar = ff{tr.hi, __fadd_rn(ar.lo, tr.lo)};
+      ai = ff{ti.hi, __fadd_rn(ai.lo, ti.lo)};
+    }
   }
-  acc = block_sum2(acc, red);
-  if (threadIdx.x == 0) wsc[(size_t)b * 8 + 6] = acc;
+  const double2 acc = block_sum2(make_double2(ff_d(ar), ff_d(ai)), red);
+  if (threadIdx.x == 0) part[(size_t)b * nparts + c] = acc;
 }
 
-// l2ci2: per walker sum over g of X_g . Y_g, Y = xg ci2m  -> wsc[b][6]
-__global__ void cisd_l2_reduce_kernel(int G, int nv, const double2* __restrict__ xg, const double2* __restrict__ y,
-                                      double2* __restrict__ wsc) {
+// l2ci2 (FP64): per walker sum over g of X_g . Y_g, Y = xg ci2m, partials as above
+__global__ void __launch_bounds__(256)
+cisd_l2_reduce_kernel(int G, int nv, const double2* __restrict__ xg, const double2* __restrict__ y,
+                      double2* __restrict__ part) {
   __shared__ double2 red[32];
-  const int b = blockIdx.x;
+  const int c = blockIdx.x, b = blockIdx.y, nparts = gridDim.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int gpp = (G + nparts - 1) / nparts, g0 = c * gpp, g1 = min(G, g0 + gpp);
   double2 acc = cmk(0.0, 0.0);
-  const size_t base = (size_t)b * G * nv, cnt = (size_t)G * nv;
-  for (size_t e = threadIdx.x; e < cnt; e += blockDim.x) {
-    cfma(acc, xg[base + e], y[base + e]);
+  for (int g = g0 + warp; g < g1; g += nw) {
+    const size_t base = ((size_t)b * G + g) * nv;
+    for (int k = lane; k < nv; k += 32) cfma(acc, xg[base + k], y[base + k]);
   }
   acc = block_sum2(acc, red);
-  if (threadIdx.x == 0) wsc[(size_t)b * 8 + 6] = acc;
+  if (threadIdx.x == 0) part[(size_t)b * nparts + c] = acc;
 }
 
 // ------------------------------------------------------------------ combines
@@ -579,7 +610,8 @@ __global__ void cisd_weight_kernel(TrotterArgs a, const double2* __restrict__ ov
 __global__ void __launch_bounds__(256)
 cisd_energy_kernel(int G, int nchunk, double h0, const double2* __restrict__ wsc, const double2* __restrict__ hg2,
                    const double2* __restrict__ lg, const double2* __restrict__ lcs,
-                   const double2* __restrict__ gpart, double2* __restrict__ energy) {
+                   const double2* __restrict__ gpart, const double2* __restrict__ l2part,
+                   double2* __restrict__ energy) {
   __shared__ double2 red[32];
   const int b = blockIdx.x;
   double2 lglg = cmk(0.0, 0.0), lslg = cmk(0.0, 0.0);
@@ -597,7 +629,8 @@ cisd_energy_kernel(int G, int nchunk, double h0, const double2* __restrict__ wsc
   if (threadIdx.x == 0) {
     const double2 ci1g = wsc[(size_t)b * 8 + 0], gci2g = wsc[(size_t)b * 8 + 1];
     const double2 e1_1_2 = wsc[(size_t)b * 8 + 2], e1_2_2 = wsc[(size_t)b * 8 + 3];
-    const double2 l2ci2 = wsc[(size_t)b * 8 + 6];
+    double2 l2ci2 = cmk(0.0, 0.0);
+    for (int c = 0; c < kL2Parts; ++c) l2ci2 = cadd(l2ci2, l2part[(size_t)b * kL2Parts + c]);
     const double2 hg = hg2[b];  // 2 hg
     // one body
     const double2 e1 = cadd(cadd(cadd(hg, cmul(cscale(ci1g, 2.0), hg)), e1_1_2),
@@ -622,7 +655,7 @@ static size_t cisd_gamma_smem(int N, int n) {
 
 static size_t cisd_gamma_f32_smem(int N, int n) {
   return (size_t)(n * N + 2 * n * n) * sizeof(double2) + (size_t)n * N * sizeof(double) +
-         (size_t)(3 * n * N) * sizeof(float2) + (size_t)(N * N + ((N * N) & 1)) * sizeof(float) +
+         (size_t)(3 * n * N + N * ((n + 1) & ~1)) * sizeof(float2) + (size_t)(N * N + ((N * N) & 1)) * sizeof(float) +
          (size_t)N * n * 8 + (size_t)n * n * 16;  // + lci1_g and lg1^T in float-float
 }
 
@@ -727,13 +760,14 @@ static int cisd_run(const trot_cisd* c, int W, const double2* w, CisdBuffers& b,
   if (c->l2ci2_precision == TROT_MIXED) {
     TROT_TIMED("cisd_l2ci2_tc", st,
                launch_split3_gemm(W * G, nv, c->nvpad, c->ncpad, b.xg, c->ci2_image, b.xq, b.yd, b.status, st));
-    CISD_LAUNCH("cisd_l2_reduce", cisd_l2_reduce_tc_kernel, W, 256, 0, st, G, nv, c->ncpad, b.xg, b.yd, b.wsc);
+    CISD_LAUNCH("cisd_l2_reduce", cisd_l2_reduce_tc_kernel, dim3(kL2Parts, W), 256, 0, st, G, nv, c->ncpad, b.xg,
+                b.yd, b.l2part);
     return TROT_OK;
   }
   if ((size_t)W * G > 65535u * 64u) { set_error("CISD: W*G too large"); return TROT_ERR_UNSUPPORTED; }
   TROT_TIMED("cisd_l2ci2", st,
              launch_zgemm_cr(W * G, nv, nv, 1.0, b.xg, nv, c->ci2m, nv, false, b.y, nv, false, st));
-  CISD_LAUNCH("cisd_l2_reduce", cisd_l2_reduce_kernel, W, 256, 0, st, G, nv, b.xg, b.y, b.wsc);
+  CISD_LAUNCH("cisd_l2_reduce", cisd_l2_reduce_kernel, dim3(kL2Parts, W), 256, 0, st, G, nv, b.xg, b.y, b.l2part);
   return TROT_OK;
 }
 
@@ -796,7 +830,7 @@ int trot_cisd_local_energy(const trot_cisd* c, int W, const double* walkers, dou
   cudaStream_t st = (cudaStream_t)stream;
   TROT_TRY(cisd_run(c, W, (const double2*)walkers, b, 2, st));
   cisd_energy_kernel<<<W, 256, 0, st>>>(c->nchol, cisd_chunks(c->nchol), c->h0, b.wsc, b.hg2, b.lg, b.lcs,
-                                        b.gpart, (double2*)out);
+                                        b.gpart, b.l2part, (double2*)out);
   TROT_CHECK_LAUNCH("cisd_energy_kernel");
   return TROT_OK;
 }
@@ -871,7 +905,7 @@ int trot_cisd_prop_step(const trot_cisd* c, const trot_system* prop, const trot_
               b.fb);
   if (energy_out)
     CISD_LAUNCH("cisd_energy", cisd_energy_kernel, W, 256, 0, st, G, cisd_chunks(G), c->h0, b.wsc, b.hg2, b.lg,
-                b.lcs, b.gpart, (double2*)energy_out);
+                b.lcs, b.gpart, b.l2part, (double2*)energy_out);
   // 2. shifted fields, 3. VHS, 4. propagation in place
   TROT_TIMED("fields", st,
              launch_fields(W, G, prop->sqrt_dt, b.fb, prop->mf_shifts_im, fields, b.xs, b.shift_term, b.fb_term, st));
