@@ -336,7 +336,7 @@ def cpu_port_rate(cfg, W_sample, steps, threads=None, min_seconds=0.0, max_steps
     return W_sample * k / dt, dt, k
 
 
-def adjoint_leg(chol_scale=0.1, seed=11):
+def adjoint_leg(chol_scale=0.1, seed=11, n_steps=None):
     """Energy gradient through a whole run on the config-3 shapes (RHF trial, N=80, n=10,
     G=400, W=512, dt=0.01, 200 steps, checkpoints / blocks of 20 steps): one forward run,
     one forward + adjoint run, and central finite differences of the forward along a
@@ -352,6 +352,8 @@ def adjoint_leg(chol_scale=0.1, seed=11):
     cfg = synthetic.CONFIGS["cfg3_rhf_n80"]
     N, (n, _), G, W, T, spb, dt = (cfg["norb"], cfg["nelec"], cfg["nchol"], cfg["n_walkers"], cfg["n_steps"],
                                    cfg["qr_every"], cfg["dt"])
+    if n_steps:
+        T = int(n_steps)
     h0, h1, chol = synthetic.hamiltonian(N, G, cfg["decay"], seed, 0.0)
     chol = chol * chol_scale
     mo = synthetic.scf(h1, chol, n, n, 30)[0]
@@ -403,6 +405,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=0, help="walkers in the CPU baseline sample (0 = auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the config-3 energy-gradient leg")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="run only the config-3 energy-gradient leg and print its JSON (for profiling)")
+    ap.add_argument("--adjoint-steps", type=int, default=0,
+                    help="steps of the energy-gradient leg (default: the config's 200)")
     ap.add_argument("--profile-run", action="store_true",
                     help="timed steps only (no e2e, FP64 comparison, precision check or CPU baseline): "
                          "for profiler launch lists")
@@ -453,6 +459,10 @@ def main():
         dist.init_process_group("nccl")
     from trot_gb300 import _lib
 
+    if args.adjoint_only:
+        if rank == 0:
+            print(json.dumps({"adjoint": adjoint_leg(n_steps=args.adjoint_steps)}), flush=True)
+        return
     wl = build_workload(cfg, args.precision)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     # warm-up: W steps, then one untimed block tail (QR, energy, SR) so the
@@ -604,7 +614,7 @@ def main():
     if precision_info is not None:
         line["precision_check"] = precision_info
     if not args.no_adjoint and rank == 0 and world == 1:
-        line["adjoint"] = adjoint_leg()
+        line["adjoint"] = adjoint_leg(n_steps=args.adjoint_steps)
     if not args.no_cpu_baseline:
         sample = args.cpu_sample or 64
         r, secs, ks = cpu_port_rate(cfg, sample, 2, min_seconds=10.0)
