@@ -190,7 +190,7 @@ int trot_local_energy(const trot_system* s, const double* wa, const double* wb, 
   TROT_TRY(launch_green(sp, W, N, (const double2*)wa, (const double2*)wb, b.green, nullptr, b.e1, st));
   TROT_TRY(force_bias_from_green(s, sp, b.green, b.fb, st));
   TROT_TRY(launch_exchange(sp, W, N, G, b.green, b.exc, st));
-  return launch_energy_combine(W, G, exchange_chunks(G), s->h0, b.fb, b.e1, b.exc, (double2*)out, st);
+  return launch_energy_combine(W, G, exchange_chunks(G), s->h0, b.fb, b.e1, 1, b.exc, (double2*)out, st);
 }
 
 int trot_apply_trotter(const trot_system* s, const double* wa, const double* wb, const double* xs,
@@ -247,7 +247,7 @@ int trot_prop_step(const trot_system* s, const trot_state* state, const double* 
   if (energy_out) {
     TROT_TIMED("exchange_fp64", st, launch_exchange(sp, W, N, G, b.green, b.exc, st));
     TROT_TIMED("energy_combine", st,
-               launch_energy_combine(W, G, exchange_chunks(G), s->h0, b.fb, b.e1, b.exc, (double2*)energy_out, st));
+               launch_energy_combine(W, G, exchange_chunks(G), s->h0, b.fb, b.e1, 1, b.exc, (double2*)energy_out, st));
   }
   // 4. shifted fields
   TROT_TIMED("fields", st, launch_fields(W, G, s->sqrt_dt, b.fb, s->mf_shifts_im, fields, b.xs, b.shift_term, b.fb_term, st));

@@ -73,7 +73,8 @@ int launch_step_finalize(int W, double* weights, double* scalars, long long* nod
 int exchange_chunks(int G);
 int launch_exchange(const Spins& sp, int W, int N, int G, const double2* green, double2* partial,
                     cudaStream_t st);
-int launch_energy_combine(int W, int G, int nchunks, double h0, const double2* fb, const double2* e1,
+// e1: e1_parts consecutive arrays of W values (one per spin for the mixed path), added in order
+int launch_energy_combine(int W, int G, int nchunks, double h0, const double2* fb, const double2* e1, int e1_parts,
                           const double2* partial, double2* energy, cudaStream_t st);
 
 // walkers.cu

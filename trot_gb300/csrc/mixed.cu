@@ -29,7 +29,7 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ double2 red[32];
   __shared__ int piv;
-  const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const int b = blockIdx.x, s = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
   const int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
   ffc* Wf = reinterpret_cast<ffc*>(smem_raw);                    // N x n
   ff* Cf = reinterpret_cast<ff*>(Wf + (size_t)N * nmax);          // N x n
@@ -37,7 +37,7 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
   double2* Mi = Md + nmax * nmax;                                 // n x n
   ffc* Mif = reinterpret_cast<ffc*>(Mi + nmax * nmax);            // n x n
   ff e1r{0.f, 0.f}, e1i{0.f, 0.f};
-  for (int s = 0; s < sp.nspin; ++s) {
+  {
     const int n = s ? sp.n[1] : sp.n[0];
     const double2* w = (s == 0 ? wa : wb) + (size_t)b * N * n;
     const double* C = s ? sp.mo[1] : sp.mo[0];
@@ -109,7 +109,7 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
   if (e1_out) {
     double2 v = make_double2(ff_d(e1r), ff_d(e1i));
     v = block_sum2(v, red);
-    if (tid == 0) e1_out[b] = v;
+    if (tid == 0) e1_out[(size_t)s * gridDim.x + b] = v;
   }
 }
 
@@ -122,7 +122,7 @@ static int launch_green_ff(const Spins& sp, int W, int N, const double2* wa, con
     return TROT_ERR_UNSUPPORTED;
   }
   if (smem > 40 * 1024) cudaFuncSetAttribute(green_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  green_ff_kernel<<<W, 256, smem, st>>>(sp, N, wa, wb, green, e1_out);
+  green_ff_kernel<<<dim3(W, sp.nspin), 256, smem, st>>>(sp, N, wa, wb, green, e1_out);
   TROT_CHECK_LAUNCH("green_ff_kernel");
   return TROT_OK;
 }
@@ -182,6 +182,7 @@ struct MixedBuffers {
   float* vhs;
   uint16_t* vimg;  // [Vr | Vi] operand images of the tensor-core Trotter kernel
   double2* ov_new; // overlaps of the propagated walkers (tensor-core Trotter, step mode)
+  double2* ovp;    // det(M_s)^mult_s per (spin, walker) of the propagated walkers
   int* node_flag;
   int* status;
   int nblk_total, mpad;
@@ -195,7 +196,7 @@ static size_t carve_mixed(const trot_system* s, const Spins& sp, Carver& c, Mixe
   const bool meas = op == TROT_OP_FORCE_BIAS || op == TROT_OP_LOCAL_ENERGY || op == TROT_OP_PROP_STEP;
   if (meas) {
     m.green = c.take<double2>(W * sp.ntot * N);
-    m.e1 = c.take<double2>(W);
+    m.e1 = c.take<double2>(2 * W);  // one-body energy per (spin, walker)
     m.nblk_total = 0;
     for (int q = 0; q < sp.nspin; ++q) {
       SpinLayout L = spin_layout(s, sp, q);
@@ -215,6 +216,7 @@ static size_t carve_mixed(const trot_system* s, const Spins& sp, Carver& c, Mixe
     if (s->mixed->exp_h1_half_img) {
       m.vimg = c.take<uint16_t>(W * (kTcImgBytes / 2));
       m.ov_new = c.take<double2>(W);
+      m.ovp = c.take<double2>(2 * W);
     }
     m.shift_term = c.take<double2>(W);
     m.fb_term = c.take<double2>(W);
@@ -1201,66 +1203,70 @@ __global__ void tc_weight_kernel(TrotterArgs a, const double2* __restrict__ ov_n
   if (b < a.W) phaseless_update(a, b, ov_new[b]);
 }
 
-// New overlaps of the propagated walkers and their phaseless weights in one pass:
+// New overlaps of the propagated walkers and their phaseless weights:
 // M_s = C_s^T w'_s in float-float (four independent accumulators per element),
-// det by FP64 Gauss-Jordan, overlap = prod_s det(M_s)^mult_s, then phaseless_update.
-// One CTA per walker.
-__global__ void __launch_bounds__(256) overlap_weight_ff_kernel(Spins sp, TrotterArgs a) {
+// det by FP64 Gauss-Jordan; one CTA per (walker, spin) writes det(M_s)^mult_s, then
+// overlap_weight_finish_kernel multiplies the spins and applies phaseless_update.
+__global__ void __launch_bounds__(256) overlap_weight_ff_kernel(Spins sp, TrotterArgs a, double2* __restrict__ ovp) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ double2 red[32];
   __shared__ int piv;
-  const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const int b = blockIdx.x, s = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
   const int N = a.N;
   const int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
   ffc* Wf = reinterpret_cast<ffc*>(smem_raw);                      // N x n
   ff* Cf = reinterpret_cast<ff*>(Wf + (size_t)N * nmax);            // N x n
   double2* Md = reinterpret_cast<double2*>(Cf + (size_t)N * nmax + ((N * nmax) & 1));  // n x n
-  double2 det_all = cmk(1.0, 0.0);
-  for (int s = 0; s < sp.nspin; ++s) {
-    const int n = s ? sp.n[1] : sp.n[0];
-    const double2* w = (s == 0 ? a.out_a : a.out_b) + (size_t)b * N * n;
-    const double* C = s ? sp.mo[1] : sp.mo[0];
-    __syncthreads();
-    for (int e = tid; e < N * n; e += nt) {
-      const double2 x = w[e];
-      Wf[e] = ffc{ff_from_d(x.x), ff_from_d(x.y)};
-      Cf[e] = ff_from_d(C[e]);
-    }
-    __syncthreads();
-    for (int e = tid; e < n * n; e += nt) {
-      const int i = e / n, j = e % n;
-      ff ar[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-      ff ai[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-      int p = 0;
-      for (; p + 4 <= N; p += 4) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const ff c = Cf[(p + u) * n + i];
-          const ffc x = Wf[(p + u) * n + j];
-          ff_mad(ar[u], c, x.re);
-          ff_mad(ai[u], c, x.im);
-        }
-      }
-      for (; p < N; ++p) {
-        const ff c = Cf[p * n + i];
-        const ffc x = Wf[p * n + j];
-        ff_mad(ar[0], c, x.re);
-        ff_mad(ai[0], c, x.im);
-      }
+  const int n = s ? sp.n[1] : sp.n[0];
+  const double2* w = (s == 0 ? a.out_a : a.out_b) + (size_t)b * N * n;
+  const double* C = s ? sp.mo[1] : sp.mo[0];
+  for (int e = tid; e < N * n; e += nt) {
+    const double2 x = w[e];
+    Wf[e] = ffc{ff_from_d(x.x), ff_from_d(x.y)};
+    Cf[e] = ff_from_d(C[e]);
+  }
+  __syncthreads();
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e / n, j = e % n;
+    ff ar[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    ff ai[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    int p = 0;
+    for (; p + 4 <= N; p += 4) {
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        ar[u] = ff_fast(ar[u].hi, ar[u].lo);
-        ai[u] = ff_fast(ai[u].hi, ai[u].lo);
+        const ff c = Cf[(p + u) * n + i];
+        const ffc x = Wf[(p + u) * n + j];
+        ff_mad(ar[u], c, x.re);
+        ff_mad(ai[u], c, x.im);
       }
-      const ff sr = ff_add(ff_add(ar[0], ar[1]), ff_add(ar[2], ar[3]));
-      const ff si = ff_add(ff_add(ai[0], ai[1]), ff_add(ai[2], ai[3]));
-      Md[e] = make_double2(ff_d(sr), ff_d(si));
     }
-    __syncthreads();
-    const double2 det = block_gauss_jordan(Md, n, n, nullptr, &piv, red);
-    det_all = cmul(det_all, (s ? sp.mult[1] : sp.mult[0]) == 2 ? cmul(det, det) : det);
+    for (; p < N; ++p) {
+      const ff c = Cf[p * n + i];
+      const ffc x = Wf[p * n + j];
+      ff_mad(ar[0], c, x.re);
+      ff_mad(ai[0], c, x.im);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      ar[u] = ff_fast(ar[u].hi, ar[u].lo);
+      ai[u] = ff_fast(ai[u].hi, ai[u].lo);
+    }
+    const ff sr = ff_add(ff_add(ar[0], ar[1]), ff_add(ar[2], ar[3]));
+    const ff si = ff_add(ff_add(ai[0], ai[1]), ff_add(ai[2], ai[3]));
+    Md[e] = make_double2(ff_d(sr), ff_d(si));
   }
-  if (tid == 0) phaseless_update(a, b, det_all);
+  __syncthreads();
+  const double2 det = block_gauss_jordan(Md, n, n, nullptr, &piv, red);
+  if (tid == 0) ovp[(size_t)s * a.W + b] = (s ? sp.mult[1] : sp.mult[0]) == 2 ? cmul(det, det) : det;
+}
+
+// overlap = prod_s det(M_s)^mult_s, then the phaseless weight update
+__global__ void overlap_weight_finish_kernel(int nspin, TrotterArgs a, const double2* __restrict__ ovp) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.W) return;
+  double2 ov = cmul(cmk(1.0, 0.0), ovp[b]);
+  if (nspin == 2) ov = cmul(ov, ovp[(size_t)a.W + b]);
+  phaseless_update(a, b, ov);
 }
 
 // ------------------------------------------------------------------ host orchestration
@@ -1457,8 +1463,10 @@ static int run_trotter_tc(const trot_system* s, const Spins& sp, const TrotterAr
     if (smem > 40 * 1024)
       cudaFuncSetAttribute(overlap_weight_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     TROT_TIMED("overlap_weight_ff", st, ([&]() -> int {
-      overlap_weight_ff_kernel<<<W, 256, smem, st>>>(sp, t);
+      overlap_weight_ff_kernel<<<dim3(W, sp.nspin), 256, smem, st>>>(sp, t, m.ovp);
       TROT_CHECK_LAUNCH("overlap_weight_ff_kernel");
+      overlap_weight_finish_kernel<<<(W + 127) / 128, 128, 0, st>>>(sp.nspin, t, m.ovp);
+      TROT_CHECK_LAUNCH("overlap_weight_finish_kernel");
       return TROT_OK;
     })());
   }
@@ -1503,7 +1511,8 @@ int mixed_local_energy(const trot_system* s, const Spins& sp, const double2* wa,
   TROT_TRY(begin(s, sp, c, m, TROT_OP_LOCAL_ENERGY, st));
   TROT_TRY(launch_green_ff(sp, s->n_walkers, s->norb, wa, wb, m.green, m.e1, st));
   TROT_TRY(run_slices_and_exchange(s, sp, m, st));
-  return launch_energy_combine(s->n_walkers, s->nchol, m.nblk_total, s->h0, m.fb, m.e1, m.xpart, energy, st);
+  return launch_energy_combine(s->n_walkers, s->nchol, m.nblk_total, s->h0, m.fb, m.e1, sp.nspin, m.xpart, energy,
+                               st);
 }
 
 int mixed_apply_trotter(const trot_system* s, const Spins& sp, const double2* xs, const TrotterArgs& a, void* ws,
@@ -1531,7 +1540,7 @@ int mixed_prop_step(const trot_system* s, const Spins& sp, const trot_state* sta
   TROT_TRY(run_slices_and_exchange(s, sp, m, st));
   if (energy_out)
     TROT_TIMED("energy_combine", st,
-               launch_energy_combine(W, G, m.nblk_total, s->h0, m.fb, m.e1, m.xpart, energy_out, st));
+               launch_energy_combine(W, G, m.nblk_total, s->h0, m.fb, m.e1, sp.nspin, m.xpart, energy_out, st));
   TROT_TIMED("fields", st, launch_fields(W, G, s->sqrt_dt, m.fb, s->mf_shifts_im, fields, m.xs, m.shift_term,
                                          m.fb_term, st));
   TROT_TRY(run_vhs(s, m, m.xs, st));

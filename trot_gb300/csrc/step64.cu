@@ -213,10 +213,11 @@ int launch_exchange(const Spins& sp, int W, int N, int G, const double2* green, 
   return TROT_OK;
 }
 
-// E = h0 + e1 + 1/2 sum_g fb_g^2 - 1/2 sum_chunks partial   (fb already carries the spin multiplicity)
+// E = h0 + e1 + 1/2 sum_g fb_g^2 - 1/2 sum_chunks partial   (fb already carries the spin multiplicity;
+// e1 comes in e1_parts parts of W values each, added in order)
 __global__ void __launch_bounds__(256)
 energy_combine_kernel(int G, int nchunks, double h0, const double2* __restrict__ fb,
-                      const double2* __restrict__ e1, const double2* __restrict__ partial,
+                      const double2* __restrict__ e1, int e1_parts, const double2* __restrict__ partial,
                       double2* __restrict__ energy) {
   __shared__ double2 red[32];
   const int b = blockIdx.x;
@@ -229,14 +230,15 @@ energy_combine_kernel(int G, int nchunks, double h0, const double2* __restrict__
   c = block_sum2(c, red);
   x = block_sum2(x, red);
   if (threadIdx.x == 0) {
-    const double2 e = e1[b];
+    double2 e = e1[b];
+    for (int k = 1; k < e1_parts; ++k) e = cadd(e, e1[(size_t)k * gridDim.x + b]);
     energy[b] = cmk(h0 + e.x + 0.5 * c.x - 0.5 * x.x, e.y + 0.5 * c.y - 0.5 * x.y);
   }
 }
 
-int launch_energy_combine(int W, int G, int nchunks, double h0, const double2* fb, const double2* e1,
+int launch_energy_combine(int W, int G, int nchunks, double h0, const double2* fb, const double2* e1, int e1_parts,
                           const double2* partial, double2* energy, cudaStream_t st) {
-  energy_combine_kernel<<<W, 256, 0, st>>>(G, nchunks, h0, fb, e1, partial, energy);
+  energy_combine_kernel<<<W, 256, 0, st>>>(G, nchunks, h0, fb, e1, e1_parts, partial, energy);
   TROT_CHECK_LAUNCH("energy_combine_kernel");
   return TROT_OK;
 }
