@@ -14,6 +14,8 @@
 //   local energy: the terms of energy_kernel_rw_rh, see cisd_energy_combine.
 // The l2ci2 quadratic forms 2 sum_g X_g^T ci2 X_g - X_g^T ci2_perm X_g (ci2_perm[(p,u),(q,t)] = ci2[p,t,q,u])
 // = sum_g X_g^T ci2m X_g (X_g = vec(glgp_g)) are one GEMM over all (walker, g) rows.
+#include <cuda_bf16.h>
+
 #include <algorithm>
 
 #include "ff.cuh"
@@ -21,6 +23,7 @@
 #include "mixed.h"
 #include "profile.h"
 #include "step_tail.cuh"
+#include "tc.cuh"
 
 namespace trot {
 
@@ -36,8 +39,9 @@ struct CisdBuffers {
   double2* wsc;                 // per-walker scalars (W, 8): ci1g, gci2g, e1_1_2, e1_2_2, ...
   double2 *lg, *lcs;            // (W, G): rot_chol . G, chol . (ci1_green + ci2_green)
   double2* kpart;               // split-K partials of the FP64 products
-  float* lf;                    // chol in FP32 (G, N, N)                    (FP32 gl)
-  ff *rd, *lc;                  // chol rows < n transposed, lci1: float-float (G, N, n)
+  ff *rd, *lc;                  // chol rows < n transposed, lci1: float-float (G, N, n)   (FP32 gl)
+  uint16_t *glimg, *glq;        // split3 images of chol (rows (g, j), K = i) and of G     (FP32 gl)
+  float* gld;                   // gl = G L_g for all (walker, p) x (g, j), FP32           (FP32 gl)
   double2* xg;                  // glgp rows (W G, n v)
   double2* y;                   // xg ci2m (W G, n v)    (FP64 l2ci2)
   uint16_t* xq;                 // split3 image of xg    (mixed l2ci2)
@@ -52,6 +56,9 @@ struct CisdBuffers {
 static constexpr int kCisdGChunk = 8;
 static constexpr int kL2Parts = 8;  // CTAs per walker of the l2ci2 reductions
 static int cisd_chunks(int G) { return (G + kCisdGChunk - 1) / kCisdGChunk; }
+// gl = G L_g as one split-BF16 tensor-core product: K = N padded to 64, columns (g, j) to 128
+static size_t cisd_gl_kpad(int N) { return (size_t)(N + 63) / 64 * 64; }
+static size_t cisd_gl_npad(int N, int G) { return ((size_t)G * N + 127) / 128 * 128; }
 
 // K slices for an FP64 product (M x Nn, long K) so that its 64 x 64 tiles fill
 // every SM twice; at least 64 of K per slice.
@@ -99,7 +106,10 @@ static size_t carve_cisd(const trot_cisd* c, int W, int op, Carver& cv, CisdBuff
   b.gpart = cv.take<double2>((size_t)W * cisd_chunks((int)G) * 4);
   b.l2part = cv.take<double2>((size_t)W * kL2Parts);
   if (c->gl_precision == TROT_MIXED) {
-    b.lf = cv.take<float>(G * N * N);
+    const size_t kp = cisd_gl_kpad((int)N), np = cisd_gl_npad((int)N, (int)G), mp = split3_mpad((int)(W * n));
+    b.glimg = cv.take<uint16_t>(3 * np * kp);
+    b.glq = cv.take<uint16_t>(3 * mp * kp);
+    b.gld = cv.take<float>(mp * np);
     b.rd = cv.take<ff>(G * N * n);
     b.lc = cv.take<ff>(G * N * n);
   }
@@ -313,19 +323,40 @@ TROT_D ffc ffc_norm(ffc a) { return ffc{ff_fast(a.re.hi, a.re.lo), ff_fast(a.im.
 TROT_D double2 ffc_d(ffc a) { return make_double2(ff_d(a.re), ff_d(a.im)); }
 
 // chol and lci1 in the operand forms of cisd_gamma_f32_kernel, once per call:
-// lf = chol in FP32 (G, N, N); rd[g][j][p] = chol[g][p][j] (p < n) and lc[g][i][q] =
-// lci1[g][i][q] in float-float.
+// rd[g][j][p] = chol[g][p][j] (p < n) and lc[g][i][q] = lci1[g][i][q] in float-float.
 __global__ void cisd_chol_forms_kernel(int N, int n, int G, const double* __restrict__ chol,
-                                       const double* __restrict__ lci1, float* __restrict__ lf, ff* __restrict__ rd,
-                                       ff* __restrict__ lc) {
-  const size_t NN = (size_t)N * N, total = (size_t)G * NN;
+                                       const double* __restrict__ lci1, ff* __restrict__ rd, ff* __restrict__ lc) {
+  const size_t Nn = (size_t)N * n, total = (size_t)G * Nn;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-    const size_t g = e / NN;
-    const int r = (int)(e % NN), p = r / N, j = r % N;
-    const double l = chol[e];
-    lf[e] = d2f_bits(l);
-    if (p < n) rd[g * N * n + (size_t)j * n + p] = ff_from_d(l);
-    if (r < N * n) lc[g * N * n + r] = ff_from_d(lci1[g * N * n + r]);
+    const size_t g = e / Nn;
+    const int r = (int)(e % Nn), p = r / N, j = r % N;  // r < n N: rows p < n of chol_g
+    rd[g * Nn + (size_t)j * n + p] = ff_from_d(chol[g * N * N + r]);
+    lc[g * Nn + r] = ff_from_d(lci1[g * Nn + r]);
+  }
+}
+
+// The B operand of gl = G L_g for every Cholesky vector: B(i, (g, j)) = chol[g][i][j],
+// stored as B^T (rows (g, j), K = i) in the split-BF16 tensor-core image
+// [npad/128][kpad/64][3 slices][128][64] (core-matrix order), once per call.
+__global__ void cisd_gl_image_kernel(int N, int G, int kpad, int npad, const double* __restrict__ chol,
+                                     uint16_t* __restrict__ img) {
+  const int nkc = kpad / 64;
+  const size_t total = (size_t)npad * kpad;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int row = (int)(e / kpad), k = (int)(e % kpad);
+    float x = 0.f;
+    if (row < G * N && k < N) {
+      const int g = row / N, j = row % N;
+      x = d2f_bits(chol[((size_t)g * N + k) * N + j]);
+    }
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(h);
+    const __nv_bfloat16 m = __float2bfloat16_rn(r1);
+    const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
+    const size_t base = ((size_t)(row >> 7) * nkc + (k >> 6)) * 3 * 8192 + tc::tile_off(row & 127, k & 63) / 2;
+    img[base] = *reinterpret_cast<const uint16_t*>(&h);
+    img[base + 8192] = *reinterpret_cast<const uint16_t*>(&m);
+    img[base + 16384] = *reinterpret_cast<const uint16_t*>(&l);
   }
 }
 
@@ -340,8 +371,8 @@ TROT_D ffc ffc_quad_sum(ffc a) {
 }
 
 __global__ void __launch_bounds__(256, 4)
-cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ green, const float* __restrict__ lf,
-                      const ff* __restrict__ rd, const ff* __restrict__ lc, const double2* __restrict__ p2,
+cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ green, const float* __restrict__ gld,
+                      int ldd, const ff* __restrict__ rd, const ff* __restrict__ lc, const double2* __restrict__ p2,
                       const double2* __restrict__ ci1g1, double2* __restrict__ xg, double2* __restrict__ gpart) {
   extern __shared__ double2 sm[];
   __shared__ double2 red[32];
@@ -353,23 +384,16 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
   ffc* C1 = GsT + n * N;                                  // n x n
   ffc* A = C1 + n * n;                                    // n x n  (lg1)
   ff* RdT = reinterpret_cast<ff*>(A + n * n);             // N x n  (rows < n of L_g, transposed)
-  const int ne = (n + 1) & ~1;                            // even row stride of GfT
   float2* Gf = reinterpret_cast<float2*>(RdT + n * N);    // n x N
   float2* P2f = Gf + n * N;                               // N x n
-  float2* GLf = P2f + N * n;                              // n x N
-  float2* GfT = GLf + n * N;                              // N x ne: GfT[j][p] = G[p][j] (16-byte pairs)
-  float* Lf = reinterpret_cast<float*>(GfT + N * ne);     // N x N
-  ff* Lc = reinterpret_cast<ff*>(Lf + N * N + ((N * N) & 1));  // N x n: lci1_g
+  float2* GLf = P2f + N * n;                              // n x N: gl_g of this walker
+  ff* Lc = reinterpret_cast<ff*>(GLf + n * N);            // N x n: lci1_g
   ffc* AT = reinterpret_cast<ffc*>(Lc + N * n);           // n x n: lg1 transposed
   for (int e = tid; e < n * N; e += nt) {
     const double2 g = green[(size_t)b * n * N + e];
     GsT[(e % N) * n + e / N] = ffc{ff_from_d(g.x), ff_from_d(g.y)};
-    const float2 gf = make_float2(d2f_bits(g.x), d2f_bits(g.y));
-    Gf[e] = gf;
-    GfT[(e % N) * ne + e / N] = gf;
+    Gf[e] = make_float2(d2f_bits(g.x), d2f_bits(g.y));
   }
-  if (n & 1)
-    for (int j = tid; j < N; j += nt) GfT[j * ne + n] = make_float2(0.f, 0.f);
   for (int e = tid; e < N * n; e += nt) {
     const double2 m = p2[(size_t)b * N * n + e];
     P2f[e] = make_float2(d2f_bits(m.x), d2f_bits(m.y));
@@ -385,8 +409,12 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
   const int quad = tid >> 2, part = tid & 3, nq = nt >> 2;
   for (int gg = g0; gg < g1; ++gg) {
     __syncthreads();
-    const float* lg = lf + (size_t)gg * N * N;
-    for (int e = tid; e < N * N; e += nt) Lf[e] = lg[e];
+    // gl_g rows p of this walker: rows 2 (b n + p) (Re) and 2 (b n + p) + 1 (Im), columns g N + j
+    for (int e = tid; e < n * N; e += nt) {
+      const int p = e / N, j = e % N;
+      const float* r0 = gld + 2 * ((size_t)b * n + p) * ldd + (size_t)gg * N + j;
+      GLf[e] = make_float2(r0[0], r0[ldd]);
+    }
     const ff* rg = rd + (size_t)gg * N * n;
     const ff* cg = lc + (size_t)gg * N * n;
     for (int e = tid; e < N * n; e += nt) {
@@ -412,20 +440,6 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
         A[e] = a;
         AT[(e % n) * n + e / n] = a;
       }
-    }
-    for (int e = tid; e < (ne / 2) * N; e += nt) {  // gl = G L: rows p, p + 1 per thread
-      const int p = 2 * (e / N), i = e % N;
-      float a0r = 0.f, a0i = 0.f, a1r = 0.f, a1i = 0.f;
-      for (int j = 0; j < N; ++j) {
-        const float l = Lf[j * N + i];
-        const float4 g = *reinterpret_cast<const float4*>(GfT + j * ne + p);
-        a0r = fmaf(l, g.x, a0r);
-        a0i = fmaf(l, g.y, a0i);
-        a1r = fmaf(l, g.z, a1r);
-        a1i = fmaf(l, g.w, a1i);
-      }
-      GLf[p * N + i] = make_float2(a0r, a0i);
-      if (p + 1 < n) GLf[(p + 1) * N + i] = make_float2(a1r, a1i);
     }
     __syncthreads();
     for (int e0 = 0; e0 < n * n; e0 += nq) {
@@ -654,9 +668,8 @@ static size_t cisd_gamma_smem(int N, int n) {
 }
 
 static size_t cisd_gamma_f32_smem(int N, int n) {
-  return (size_t)(n * N + 2 * n * n) * sizeof(double2) + (size_t)n * N * sizeof(double) +
-         (size_t)(3 * n * N + N * ((n + 1) & ~1)) * sizeof(float2) + (size_t)(N * N + ((N * N) & 1)) * sizeof(float) +
-         (size_t)N * n * 8 + (size_t)n * n * 16;  // + lci1_g and lg1^T in float-float
+  // GsT, C1, A, AT (complex float-float) + RdT, Lc (float-float) + Gf, P2f, GLf (float2)
+  return (size_t)(n * N + 3 * n * n) * 16 + (size_t)(2 * n * N) * 8 + (size_t)(3 * n * N) * sizeof(float2);
 }
 
 // need_ham: the force bias / energy / step also read h1, chol and lci1
@@ -746,10 +759,17 @@ static int cisd_run(const trot_cisd* c, int W, const double2* w, CisdBuffers& b,
   if (c->gl_precision == TROT_MIXED) {
     const size_t smem2 = cisd_gamma_f32_smem(N, n);
     cudaFuncSetAttribute(cisd_gamma_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
-    const size_t gnn = (size_t)G * N * N;
+    const size_t gnn = (size_t)G * N * n;
     CISD_LAUNCH("cisd_chol_forms", cisd_chol_forms_kernel, (unsigned)std::min<size_t>((gnn + 255) / 256, 152 * 16),
-                256, 0, st, N, n, G, c->chol, c->lci1, b.lf, b.rd, b.lc);
-    CISD_LAUNCH("cisd_gamma_f32", cisd_gamma_f32_kernel, dim3(nch, W), 256, smem2, st, N, n, v, G, b.green, b.lf,
+                256, 0, st, N, n, G, c->chol, c->lci1, b.rd, b.lc);
+    // gl = G L_g for all walkers and Cholesky vectors: one split-BF16 tensor-core product
+    // (FP32-class, the reference's float32 gl), rows (walker, p), columns (g, j)
+    const int kp = (int)cisd_gl_kpad(N), np = (int)cisd_gl_npad(N, G);
+    const size_t nimg = (size_t)np * kp;
+    CISD_LAUNCH("cisd_gl_tc", cisd_gl_image_kernel, (unsigned)std::min<size_t>((nimg + 255) / 256, 152 * 16), 256, 0,
+                st, N, G, kp, np, c->chol, b.glimg);
+    TROT_TIMED("cisd_gl_tc", st, launch_split3_gemm(W * n, N, kp, np, b.green, b.glimg, b.glq, b.gld, b.status, st));
+    CISD_LAUNCH("cisd_gamma_f32", cisd_gamma_f32_kernel, dim3(nch, W), 256, smem2, st, N, n, v, G, b.green, b.gld, np,
                 b.rd, b.lc, b.p2, b.ci1g1, b.xg, b.gpart);
   } else {
     const size_t smem2 = cisd_gamma_smem(N, n);
