@@ -379,19 +379,21 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
   const int chunk = blockIdx.x, b = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
   const int nchunk = gridDim.x;
   // j-major copies (GsT[j][q] = G[q][j], RdT[j][p] = L_g[p][j], AT[q][p] = lg1[p][q]) keep the
-  // per-thread index q (or p) fastest across a warp: no shared-memory bank conflicts
-  ffc* GsT = reinterpret_cast<ffc*>(sm);                  // N x n
-  ffc* C1 = GsT + n * N;                                  // n x n
-  ffc* A = C1 + n * n;                                    // n x n  (lg1)
-  ff* RdT = reinterpret_cast<ff*>(A + n * n);             // N x n  (rows < n of L_g, transposed)
-  float2* Gf = reinterpret_cast<float2*>(RdT + n * N);    // n x N
+  // per-thread index q (or p) fastest across a warp; their rows are padded to ns = n + 1
+  // entries so that the four lanes of a quad (rows part + 4k) fall on different banks
+  const int ns = n + 1;
+  ffc* GsT = reinterpret_cast<ffc*>(sm);                  // N x ns
+  ffc* C1 = GsT + ns * N;                                 // n x ns
+  ffc* A = C1 + ns * n;                                   // n x n  (lg1)
+  ff* RdT = reinterpret_cast<ff*>(A + n * n);             // N x ns (rows < n of L_g, transposed)
+  float2* Gf = reinterpret_cast<float2*>(RdT + ns * N);   // n x N
   float2* P2f = Gf + n * N;                               // N x n
   float2* GLf = P2f + N * n;                              // n x N: gl_g of this walker
   ff* Lc = reinterpret_cast<ff*>(GLf + n * N);            // N x n: lci1_g
-  ffc* AT = reinterpret_cast<ffc*>(Lc + N * n);           // n x n: lg1 transposed
+  ffc* AT = reinterpret_cast<ffc*>(Lc + N * n);           // n x ns: lg1 transposed
   for (int e = tid; e < n * N; e += nt) {
     const double2 g = green[(size_t)b * n * N + e];
-    GsT[(e % N) * n + e / N] = ffc{ff_from_d(g.x), ff_from_d(g.y)};
+    GsT[(e % N) * ns + e / N] = ffc{ff_from_d(g.x), ff_from_d(g.y)};
     Gf[e] = make_float2(d2f_bits(g.x), d2f_bits(g.y));
   }
   for (int e = tid; e < N * n; e += nt) {
@@ -400,7 +402,7 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
   }
   for (int e = tid; e < n * n; e += nt) {
     const double2 c = ci1g1[(size_t)b * n * n + e];
-    C1[e] = ffc{ff_from_d(c.x), ff_from_d(c.y)};
+    C1[(e / n) * ns + e % n] = ffc{ff_from_d(c.x), ff_from_d(c.y)};
   }
   const ffc z{{0.f, 0.f}, {0.f, 0.f}};
   ffc s0 = z, s1 = z, s2 = z, s3 = z;
@@ -418,7 +420,7 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
     const ff* rg = rd + (size_t)gg * N * n;
     const ff* cg = lc + (size_t)gg * N * n;
     for (int e = tid; e < N * n; e += nt) {
-      RdT[e] = rg[e];
+      RdT[(e / n) * ns + e % n] = rg[e];
       Lc[e] = cg[e];
     }
     __syncthreads();
@@ -428,8 +430,8 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
       if (e < n * n) {
         const int p = e / n, q = e % n;
         for (int j = part; j < N; j += 4) {
-          const ff r = RdT[j * n + p];
-          const ffc g = GsT[j * n + q];
+          const ff r = RdT[j * ns + p];
+          const ffc g = GsT[j * ns + q];
           ff_mad(a.re, r, g.re);
           ff_mad(a.im, r, g.im);
         }
@@ -438,7 +440,7 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
       a = ffc_quad_sum(a);
       if (e < n * n && part == 0) {
         A[e] = a;
-        AT[(e % n) * n + e / n] = a;
+        AT[(e % n) * ns + e / n] = a;
       }
     }
     __syncthreads();
@@ -448,10 +450,10 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
       float zr = 0.f, zi = 0.f;
       if (e < n * n) {
         const int p = e / n, q = e % n;
-        for (int a2 = part; a2 < n; a2 += 4) ffc_mad(t, AT[a2 * n + q], C1[a2 * n + p]);
+        for (int a2 = part; a2 < n; a2 += 4) ffc_mad(t, AT[a2 * ns + q], C1[a2 * ns + p]);
         for (int i = part; i < N; i += 4) {  // lci1g[q][p] = sum_i lci1[i][q] G[p][i]
           const ff l = Lc[i * n + q];
-          const ffc g = GsT[i * n + p];
+          const ffc g = GsT[i * ns + p];
           ff_mad(bq.re, l, g.re);
           ff_mad(bq.im, l, g.im);
         }
@@ -472,7 +474,7 @@ cisd_gamma_f32_kernel(int N, int n, int v, int G, const double2* __restrict__ gr
       }
       if (e < n * n && part == 0) {
         const ffc apq = A[e];
-        ffc_mad(s0, apq, AT[e]);
+        ffc_mad(s0, apq, AT[(e / n) * ns + e % n]);
         ffc_mad(s1, apq, t);
         ffc_mad(s2, bq, apq);
         ffc_mad(s3, apq, ffc{ff{zr, 0.f}, ff{zi, 0.f}});
@@ -668,8 +670,11 @@ static size_t cisd_gamma_smem(int N, int n) {
 }
 
 static size_t cisd_gamma_f32_smem(int N, int n) {
-  // GsT, C1, A, AT (complex float-float) + RdT, Lc (float-float) + Gf, P2f, GLf (float2)
-  return (size_t)(n * N + 3 * n * n) * 16 + (size_t)(2 * n * N) * 8 + (size_t)(3 * n * N) * sizeof(float2);
+  // GsT, C1, AT (complex float-float, rows padded to n + 1), A + RdT (padded), Lc (float-float)
+  // + Gf, P2f, GLf (float2)
+  const size_t ns = (size_t)n + 1;
+  return (N * ns + 2 * n * ns + (size_t)n * n) * 16 + (N * ns + (size_t)N * n) * 8 +
+         (size_t)(3 * n * N) * sizeof(float2);
 }
 
 // need_ham: the force bias / energy / step also read h1, chol and lci1
