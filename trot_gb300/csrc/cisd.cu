@@ -704,7 +704,8 @@ static int check_cisd(const trot_cisd* c, int W, bool need_ham = true) {
     }
   }
   if (c->nocc > 64 || cisd_mats_smem(c->norb, c->nocc, c->nvir) > 200 * 1024 ||
-      cisd_gamma_smem(c->norb, c->nocc) > 200 * 1024) {
+      cisd_gamma_smem(c->norb, c->nocc) > 200 * 1024 ||
+      (c->gl_precision == TROT_MIXED && cisd_gamma_f32_smem(c->norb, c->nocc) > 200 * 1024)) {
     set_error("CISD tile of N=%d, n=%d exceeds shared memory", c->norb, c->nocc);
     return TROT_ERR_UNSUPPORTED;
   }
