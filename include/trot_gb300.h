@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define TROT_ABI_VERSION 1
+#define TROT_ABI_VERSION 2
 
 typedef enum {
   TROT_OK = 0,
@@ -278,6 +278,11 @@ typedef struct {
    * (trot_gb300.mixed.split3_image). */
   int nvpad, ncpad;
   const uint16_t* ci2_image;
+  /* nonzero when every chol[g] is symmetric to working precision (checked by
+   * the caller): the contraction chol . (ci1_green + ci2_green) then runs over
+   * the packed upper triangle of (chol[g] + chol[g]^T) / 2 (norb (norb + 1) / 2
+   * terms instead of norb^2). */
+  int chol_symmetric;
 } trot_cisd;
 
 /* Device workspace for trot_cisd_overlap (TROT_OP_OVERLAP), trot_cisd_force_bias

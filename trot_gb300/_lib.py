@@ -72,6 +72,7 @@ class TrotCisd(ctypes.Structure):
         ("norb", _i), ("nocc", _i), ("nvir", _i), ("nchol", _i), ("h0", _d),
         ("ci1", _p), ("ci2m", _p), ("h1", _p), ("chol", _p), ("lci1", _p), ("mo", _p),
         ("l2ci2_precision", _i), ("gl_precision", _i), ("nvpad", _i), ("ncpad", _i), ("ci2_image", _p),
+        ("chol_symmetric", _i),
     ]
 
 
@@ -153,7 +154,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
-        if lib.trot_abi_version() != 1:
+        if lib.trot_abi_version() != 2:
             raise RuntimeError("trot_gb300 ABI version mismatch")
         _lib = lib
         return lib

@@ -131,6 +131,7 @@ class CisdMeasCtx:
     ci2_image: torch.Tensor | None = None  # ci2m split-BF16 image (testing=False)
     nvpad: int = 0
     ncpad: int = 0
+    chol_symmetric: bool = False  # every chol[g] symmetric: packed-triangle contraction
 
 
 def build_meas_ctx(ham_data: HamChol, trial_data: CisdTrial, cfg: CisdMeasCfg = CisdMeasCfg()) -> CisdMeasCtx:
@@ -151,8 +152,13 @@ def build_meas_ctx(ham_data: HamChol, trial_data: CisdTrial, cfg: CisdMeasCfg = 
         bt = _trial_dev(trial_data)["ci2m"].T.cpu().numpy()  # (nv columns, nv K)
         img, ncpad, nvpad = mixed.split3_image(bt)
         img = img.to(chol.device)
+    # Cholesky vectors of real two-electron integrals are symmetric matrices (to rounding after a
+    # basis rotation); checked once here: the packed contraction uses (L + L^T) / 2
+    amax = float(chol.abs().max()) if chol.numel() else 0.0
+    sym = bool(float((chol - chol.transpose(1, 2)).abs().max()) <= 1e-12 * amax) if chol.numel() else False
     return CisdMeasCtx(rot_chol=chol[:, :n, :], lci1=lci1, cfg=cfg, h1=h1, chol=chol,
-                       h0=float(np.real(np.asarray(h0))), ci2_image=img, nvpad=nvpad, ncpad=ncpad)
+                       h0=float(np.real(np.asarray(h0))), ci2_image=img, nvpad=nvpad, ncpad=ncpad,
+                       chol_symmetric=sym)
 
 
 def _struct(trial: CisdTrial, meas_ctx: CisdMeasCtx | None) -> _lib.TrotCisd:
@@ -166,6 +172,7 @@ def _struct(trial: CisdTrial, meas_ctx: CisdMeasCtx | None) -> _lib.TrotCisd:
         c.h0 = meas_ctx.h0
         c.h1, c.chol, c.lci1 = native.ptr(meas_ctx.h1), native.ptr(meas_ctx.chol), native.ptr(meas_ctx.lci1)
         c.gl_precision = _lib.MIXED if meas_ctx.cfg.mixed_precision else _lib.FP64
+        c.chol_symmetric = 1 if meas_ctx.chol_symmetric else 0
         if meas_ctx.ci2_image is not None:
             c.l2ci2_precision = _lib.MIXED
             c.ci2_image, c.nvpad, c.ncpad = meas_ctx.ci2_image.data_ptr(), meas_ctx.nvpad, meas_ctx.ncpad

@@ -35,6 +35,8 @@ struct CisdBuffers {
   double2* cg;                  // ci2g = x ci2m (W, n v)
   double2* ci1g1;               // (W, n, n)
   double2 *ms, *m2;             // ci1_green + ci2_green, ci2_green (W, N, N)
+  double2* msp;                 // ms packed: upper triangle, ms[i][j] + ms[j][i] off the diagonal (W, P)
+  double* lp;                   // chol packed: upper triangle of chol[g] (G, P), P = N (N + 1) / 2
   double2* p2;                  // P2 = gp ci2g^T (W, N, n): ci2_green = P2 G
   double2* wsc;                 // per-walker scalars (W, 8): ci1g, gci2g, e1_1_2, e1_2_2, ...
   double2 *lg, *lcs;            // (W, G): rot_chol . G, chol . (ci1_green + ci2_green)
@@ -83,7 +85,7 @@ static size_t carve_cisd(const trot_cisd* c, int W, int op, Carver& cv, CisdBuff
     size_t kp = (size_t)cisd_splitk(W, (int)nv, (int)nv) * W * nv;  // ci2g
     if (op != TROT_OP_OVERLAP) {
       kp = std::max(kp, (size_t)cisd_splitk(W, (int)G, (int)(n * N)) * W * G);  // lg
-      kp = std::max(kp, (size_t)cisd_splitk(W, (int)G, (int)(N * N)) * W * G);  // lcs
+      kp = std::max(kp, (size_t)cisd_splitk(W, (int)G, (int)(N * N)) * W * G);  // lcs (the packed K is shorter)
     }
     b.kpart = cv.take<double2>(kp);
   }
@@ -91,6 +93,10 @@ static size_t carve_cisd(const trot_cisd* c, int W, int op, Carver& cv, CisdBuff
   b.ci1g1 = cv.take<double2>(W * n * n);
   b.ms = cv.take<double2>(W * N * N);
   b.m2 = cv.take<double2>(W * N * N);
+  if (c->chol_symmetric) {
+    b.msp = cv.take<double2>(W * N * (N + 1) / 2);
+    b.lp = cv.take<double>(G * N * (N + 1) / 2);
+  }
   b.p2 = cv.take<double2>(W * N * n);
   b.lg = cv.take<double2>(W * G);
   b.lcs = cv.take<double2>(W * G);
@@ -122,6 +128,33 @@ static size_t carve_cisd(const trot_cisd* c, int W, int op, Carver& cv, CisdBuff
   b.ov_new = cv.take<double2>(W);
   b.node_flag = cv.take<int>(W);
   return cv.used;
+}
+
+// ------------------------------------------------------------------ packed symmetric contraction
+// With every L_g symmetric, sum_ij L_g[i][j] M[i][j] = sum_{i <= j} L_g[i][j] Mp[i][j] over the
+// upper triangle (of (L_g + L_g^T) / 2: symmetric to rounding after a basis rotation) (row-major, k(i, j) = i N - i (i - 1) / 2 + j - i), Mp[i][j] = M[i][j] + M[j][i]
+// off the diagonal and M[i][i] on it: half the FP64 products of chol . (ci1_green + ci2_green).
+__global__ void cisd_pack_chol_kernel(int N, int G, const double* __restrict__ chol, double* __restrict__ lp) {
+  const size_t P = (size_t)N * (N + 1) / 2, total = (size_t)G * N * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t g = e / ((size_t)N * N);
+    const int r = (int)(e % ((size_t)N * N)), i = r / N, j = r % N;
+    if (j >= i)
+      lp[g * P + (size_t)i * N - (size_t)i * (i - 1) / 2 + (j - i)] =
+          0.5 * (chol[e] + chol[g * N * N + (size_t)j * N + i]);
+  }
+}
+
+__global__ void cisd_pack_ms_kernel(int N, int W, const double2* __restrict__ ms, double2* __restrict__ msp) {
+  const size_t P = (size_t)N * (N + 1) / 2, total = (size_t)W * N * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t b = e / ((size_t)N * N);
+    const int r = (int)(e % ((size_t)N * N)), i = r / N, j = r % N;
+    if (j < i) continue;
+    double2 v = ms[e];
+    if (j > i) v = cadd(v, ms[b * N * N + (size_t)j * N + i]);
+    msp[b * P + (size_t)i * N - (size_t)i * (i - 1) / 2 + (j - i)] = v;
+  }
 }
 
 // ------------------------------------------------------------------ x, ci1g, ci1g1
@@ -754,12 +787,25 @@ static int cisd_run(const trot_cisd* c, int W, const double2* w, CisdBuffers& b,
   TROT_TIMED("cisd_chol_gemm", st,
              launch_zgemm_cr_splitk(W, G, n * N, 1.0, b.green, n * N, c->chol, N * N, true, b.lg, G, false, b.kpart,
                                     cisd_splitk(W, G, n * N), st));
-  // lcs = (ci1_green + ci2_green) . chol^T: one (W, N^2) x (N^2, G) FP64 product.
+  // lcs = (ci1_green + ci2_green) . chol^T: one (W, N^2) x (N^2, G) FP64 product, over the packed
+  // upper triangle when every chol[g] is symmetric.
   // (FP32-class products here, as the reference's mixed_real_dtype contraction, move
   // the local energy by ~1e-3 Ha at N=60, G=300: too far from FP64.)
-  TROT_TIMED("cisd_lci_gemm", st,
-             launch_zgemm_cr_splitk(W, G, N * N, 1.0, b.ms, N * N, c->chol, N * N, true, b.lcs, G, false,
-                                    b.kpart, cisd_splitk(W, G, N * N), st));
+  if (c->chol_symmetric) {
+    const int P = N * (N + 1) / 2;
+    const size_t gnn = (size_t)G * N * N, wnn = (size_t)W * N * N;
+    CISD_LAUNCH("cisd_lci_gemm", cisd_pack_chol_kernel, (unsigned)std::min<size_t>((gnn + 255) / 256, 152 * 16), 256,
+                0, st, N, G, c->chol, b.lp);
+    CISD_LAUNCH("cisd_lci_gemm", cisd_pack_ms_kernel, (unsigned)std::min<size_t>((wnn + 255) / 256, 152 * 16), 256, 0,
+                st, N, W, b.ms, b.msp);
+    TROT_TIMED("cisd_lci_gemm", st,
+               launch_zgemm_cr_splitk(W, G, P, 1.0, b.msp, P, b.lp, P, true, b.lcs, G, false, b.kpart,
+                                      cisd_splitk(W, G, P), st));
+  } else {
+    TROT_TIMED("cisd_lci_gemm", st,
+               launch_zgemm_cr_splitk(W, G, N * N, 1.0, b.ms, N * N, c->chol, N * N, true, b.lcs, G, false,
+                                      b.kpart, cisd_splitk(W, G, N * N), st));
+  }
   if (stage == 1) return TROT_OK;
   const int nch = cisd_chunks(G);
   if (c->gl_precision == TROT_MIXED) {
