@@ -85,6 +85,32 @@ def test_cisd_vs_oracle(N, n, G, W, noise):
     assert rel(cpu(S.rdm1(wd))[:, 0], co.rdm1(w, tr)) <= TOL
 
 
+@pytest.mark.parametrize("mixed", [False, True])
+def test_cisd_symmetric_and_general_cholesky(mixed):
+    """The Cholesky contraction runs over the packed upper triangle only when every
+    Cholesky matrix is symmetric to working precision; a general (non-symmetric) set
+    takes the full N^2 contraction and still matches the oracle."""
+    N, n, G, W = 24, 5, 40, 6
+    cs, w = _synthetic(N, n, G, W, 0.1, seed=3)
+    tr = co.CisdTrial(cs.ci1, cs.ci2)
+    wd = dev(w)
+    S = CisdSetup(cs.h0, cs.h1, cs.chol, cs.ci1, cs.ci2, W, mixed=mixed)
+    assert S.meas_ctx.chol_symmetric
+    skew = np.random.default_rng(8).normal(scale=1e-3, size=cs.chol.shape)
+    chol_g = cs.chol + (skew - skew.transpose(0, 2, 1))
+    Sg = CisdSetup(cs.h0, cs.h1, chol_g, cs.ci1, cs.ci2, W, mixed=mixed)
+    assert not Sg.meas_ctx.chol_symmetric
+    e_tol = 1e-5 if mixed else TOL  # mixed: FP32-class gl and l2ci2, absolute Ha
+    for setup, chol in ((S, cs.chol), (Sg, chol_g)):
+        assert rel(cpu(setup.force_bias(wd)), co.force_bias(w, tr, chol)) <= TOL
+        e_ref = co.energy(w, tr, cs.h0, cs.h1, chol)
+        e = cpu(setup.energy(wd))
+        if mixed:
+            assert np.max(np.abs(e - e_ref)) <= e_tol
+        else:
+            assert rel(e, e_ref) <= TOL
+
+
 @pytest.mark.parametrize("N,n,G,W,noise", [(60, 8, 300, 6, 0.1), (31, 6, 70, 37, 0.3), (44, 11, 130, 5, 0.2),
                                            (9, 2, 11, 3, 0.05), (31, 6, 70, 37, 0.1)])
 def test_cisd_mixed_energy(N, n, G, W, noise):
