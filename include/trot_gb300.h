@@ -95,6 +95,11 @@ typedef struct {
    * the Trotter action runs on the tensor cores (N <= 128, nocc_a + nocc_b <=
    * 32), else in FP32. */
   const uint16_t* exp_h1_half_img;
+  /* 1 when every Cholesky matrix is symmetric to working precision: the rows of
+   * chol_t_slices are then the packed upper triangle k(p, q) = p N - p (p - 1) / 2
+   * + q - p (p <= q) of (L + L^T) / 2, n2pad = N (N + 1) / 2 rounded up to 128,
+   * and the VHS (symmetric) is produced in that packed column order. */
+  int vhs_packed;
 } trot_mixed;
 
 /* Static description of one Hamiltonian + trial + propagation context.

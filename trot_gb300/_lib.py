@@ -38,7 +38,7 @@ class TrotMixed(ctypes.Structure):
         ("slices", _i), ("max_order", _i), ("kpad", _i), ("gammas_per_block", _i * 2), ("n_blocks", _i * 2),
         ("rot_slices", _p * 2), ("rot_exp", _p * 2), ("vhs_slices", _i), ("vhs_order", _i), ("n2pad", _i),
         ("gpad", _i), ("chol_t_slices", _p), ("exp_h1_half_f32", _p),
-        ("exp_h1_half_img", _p),
+        ("exp_h1_half_img", _p), ("vhs_packed", _i),
     ]
 
 

@@ -849,10 +849,22 @@ __device__ void taylor_term32(int N, int nc, const float2* V, const float2* T, f
   }
 }
 
+// column of V[p][q] in the VHS GEMM output: p N + q, or its packed upper-triangle
+// column k(min, max) when the Cholesky image is packed (symmetric L: V is symmetric)
+__device__ __forceinline__ size_t vhs_col(int p, int q, int N, int packed) {
+  if (!packed) return (size_t)p * N + q;
+  if (p > q) {
+    const int t = p;
+    p = q;
+    q = t;
+  }
+  return (size_t)p * N - (size_t)p * (p - 1) / 2 + (q - p);
+}
+
 struct Trot32Args {
   TrotterArgs t;
   const float* vhs;
-  int n2pad;
+  int n2pad, packed;
   const float* expH32;
 };
 
@@ -873,7 +885,10 @@ __global__ void __launch_bounds__(256) trotter32_kernel(Spins sp, Trot32Args a32
   unsigned char* extra = smem_raw + vbytes + 3 * tbytes;
   const float* vre = a32.vhs + (size_t)(2 * b) * a32.n2pad;
   const float* vim = vre + a32.n2pad;
-  for (int e = tid; e < N * N; e += nt) V[e] = make_float2(vre[e], vim[e]);
+  for (int e = tid; e < N * N; e += nt) {
+    const size_t c = vhs_col(e / N, e % N, N, a32.packed);
+    V[e] = make_float2(vre[c], vim[c]);
+  }
   for (int s = 0; s < sp.nspin; ++s) {
     const int n = sp.n[s];
     const double2* w = (s == 0 ? a.in_a : a.in_b) + (size_t)b * N * n;
@@ -1167,21 +1182,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, Tro
 }
 
 // [Vr | Vi] of every walker as the A image of trotter_tc_kernel: (W, 8 chunks, 3 slices, 128 rows, 32)
-// from the VHS GEMM output (rows 2b / 2b+1 = Re / Im of walker b, n2pad columns pq).
-// One thread per (walker, chunk, row, 8 consecutive k): three 16-byte stores.
-__global__ void vhs_image_kernel(int W, int N, int n2pad, const float* __restrict__ D, uint16_t* __restrict__ img) {
+// from the VHS GEMM output (rows 2b / 2b+1 = Re / Im of walker b, n2pad columns pq, packed
+// upper triangle when `packed`). One thread per (walker, chunk, row, 8 consecutive k): three
+// 16-byte stores.
+__global__ void vhs_image_kernel(int W, int N, int n2pad, int packed, const float* __restrict__ D,
+                                 uint16_t* __restrict__ img) {
   const size_t total = (size_t)W * 8 * 128 * 4;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
     const int kg = (int)(e & 3), p = (int)((e >> 2) & 127), kc = (int)((e >> 9) & 7);
     const size_t b = e >> 12;
     const int k0 = kc * kTcKC + kg * 8;              // 0..255
     const int im = k0 >= 128 ? 1 : 0, q0 = k0 & 127;
-    const float* src = D + (2 * b + im) * (size_t)n2pad + (size_t)p * N;
+    const float* src = D + (2 * b + im) * (size_t)n2pad;
     uint32_t hw[4], mw[4], lw[4];
 #pragma unroll
     for (int i = 0; i < 8; i += 2) {
-      const float x0 = (p < N && q0 + i < N) ? src[q0 + i] : 0.f;
-      const float x1 = (p < N && q0 + i + 1 < N) ? src[q0 + i + 1] : 0.f;
+      const float x0 = (p < N && q0 + i < N) ? src[vhs_col(p, q0 + i, N, packed)] : 0.f;
+      const float x1 = (p < N && q0 + i + 1 < N) ? src[vhs_col(p, q0 + i + 1, N, packed)] : 0.f;
       uint16_t h0, m0, l0, h1, m1, l1;
       split3_bf16(x0, h0, m0, l0);
       split3_bf16(x1, h1, m1, l1);
@@ -1412,6 +1429,7 @@ static int run_trotter32(const trot_system* s, const Spins& sp, const TrotterArg
   a.t = t;
   a.vhs = m.vhs;
   a.n2pad = s->mixed->n2pad;
+  a.packed = s->mixed->vhs_packed;
   a.expH32 = s->mixed->exp_h1_half_f32;
   trotter32_kernel<<<s->n_walkers, 256, smem, st>>>(sp, a);
   TROT_CHECK_LAUNCH("trotter32_kernel");
@@ -1438,7 +1456,7 @@ static int run_trotter_tc(const trot_system* s, const Spins& sp, const TrotterAr
   TROT_TIMED("vhs_image", st, ([&]() -> int {
     const size_t threads = (size_t)W * 8 * 128 * 4;
     const int blocks = (int)std::min<size_t>((threads + 255) / 256, 152 * 32);
-    vhs_image_kernel<<<blocks, 256, 0, st>>>(W, N, s->mixed->n2pad, m.vhs, m.vimg);
+    vhs_image_kernel<<<blocks, 256, 0, st>>>(W, N, s->mixed->n2pad, s->mixed->vhs_packed, m.vhs, m.vimg);
     TROT_CHECK_LAUNCH("vhs_image_kernel");
     return TROT_OK;
   })());

@@ -121,10 +121,23 @@ class MixedCtx:
         self.struct = s
         if chol_flat is None:
             return
-        sl, n2pad, gpad = split3_image(np.asarray(chol_flat).T)
+        cf = np.asarray(chol_flat)
+        G, N = cf.shape[0], int(round(np.sqrt(cf.shape[1])))
+        L = cf.reshape(G, N, N)
+        amax = float(np.abs(L).max()) if L.size else 0.0
+        packed = L.size > 0 and float(np.abs(L - L.transpose(0, 2, 1)).max()) <= 1e-12 * amax
+        if packed:
+            # symmetric L (Cholesky vectors of real integrals): the VHS is symmetric, so only its
+            # packed upper triangle (row-major, p <= q) is computed, from (L + L^T) / 2
+            iu, ju = np.triu_indices(N)
+            bt = (0.5 * (L[:, iu, ju] + L[:, ju, iu])).T  # (N (N + 1) / 2, G)
+        else:
+            bt = cf.T
+        sl, n2pad, gpad = split3_image(bt)
         sl = sl.to(dev)
         self._keep.append(sl)
         s.vhs_slices, s.vhs_order, s.n2pad, s.gpad = VHS_SLICES, VHS_ORDER, n2pad, gpad
+        s.vhs_packed = 1 if packed else 0
         s.chol_t_slices = sl.data_ptr()
         eh = torch.as_tensor(np.asarray(exp_h1_half, dtype=np.float32)).to(dev).contiguous()
         self._keep.append(eh)
