@@ -67,3 +67,24 @@ def test_split3_image_layout(kchunk):
     # the image's first row of the first chunk is contiguous in 8-element core-matrix rows
     flat = img.to(torch.float64).numpy().reshape(2, kpad // kchunk, 3, -1)
     assert flat[0, 0, 0, 1] == m[0, 0, 1]
+
+
+def test_packed_vhs_operand_matches_full_product():
+    """With symmetric Cholesky matrices the VHS operand is the packed upper triangle, and
+    column packed_index(p, q) of x @ B reproduces VHS[p][q] for every (p, q); a general set
+    keeps the full (N^2, G) operand."""
+    from trot_gb300 import mixed, synthetic
+
+    N, G = 9, 13
+    _, _, chol = synthetic.hamiltonian(N, G, 30.0, 3, 0.0)
+    x = np.random.default_rng(4).standard_normal((5, G))
+    vhs = np.einsum("bg,gpq->bpq", x, chol)
+    bt, packed = mixed.vhs_operand(chol.reshape(G, N * N))
+    assert packed and bt.shape == (N * (N + 1) // 2, G)
+    vp = x @ bt.T
+    for p in range(N):
+        for q in range(N):
+            np.testing.assert_allclose(vp[:, mixed.packed_index(p, q, N)], vhs[:, p, q], rtol=1e-13, atol=1e-13)
+    skew = np.random.default_rng(5).standard_normal(chol.shape) * 1e-3
+    bt_g, packed_g = mixed.vhs_operand((chol + skew - skew.transpose(0, 2, 1)).reshape(G, N * N))
+    assert not packed_g and bt_g.shape == (N * N, G)

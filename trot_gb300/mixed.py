@@ -77,6 +77,29 @@ def split3_image(bt: np.ndarray, kchunk: int = 64):
     return sl.reshape(nt, nk, 3, 128, kchunk).contiguous(), npad, kpad
 
 
+def vhs_operand(chol_flat):
+    """B^T of the VHS product VHS = x chol_flat: (N^2, G) rows pq, or, when every Cholesky
+    matrix is symmetric to working precision (Cholesky vectors of real integrals are), the
+    packed upper triangle (N (N + 1) / 2, G) of (L + L^T) / 2 in row-major p <= q order, so
+    that only the upper triangle of the symmetric VHS is computed.  Returns (bt, packed)."""
+    cf = np.asarray(chol_flat, dtype=np.float64)
+    G, N = cf.shape[0], int(round(np.sqrt(cf.shape[1])))
+    L = cf.reshape(G, N, N)
+    amax = float(np.abs(L).max()) if L.size else 0.0
+    packed = L.size > 0 and float(np.abs(L - L.transpose(0, 2, 1)).max()) <= 1e-12 * amax
+    if not packed:
+        return cf.T, False
+    iu, ju = np.triu_indices(N)
+    return (0.5 * (L[:, iu, ju] + L[:, ju, iu])).T, True
+
+
+def packed_index(p: int, q: int, N: int) -> int:
+    """Column of V[p][q] in the packed upper triangle (the kernels' vhs_col)."""
+    if p > q:
+        p, q = q, p
+    return p * N - p * (p - 1) // 2 + (q - p)
+
+
 def gammas_per_block(n: int) -> int:
     return max(1, 128 // n)
 
@@ -121,18 +144,7 @@ class MixedCtx:
         self.struct = s
         if chol_flat is None:
             return
-        cf = np.asarray(chol_flat)
-        G, N = cf.shape[0], int(round(np.sqrt(cf.shape[1])))
-        L = cf.reshape(G, N, N)
-        amax = float(np.abs(L).max()) if L.size else 0.0
-        packed = L.size > 0 and float(np.abs(L - L.transpose(0, 2, 1)).max()) <= 1e-12 * amax
-        if packed:
-            # symmetric L (Cholesky vectors of real integrals): the VHS is symmetric, so only its
-            # packed upper triangle (row-major, p <= q) is computed, from (L + L^T) / 2
-            iu, ju = np.triu_indices(N)
-            bt = (0.5 * (L[:, iu, ju] + L[:, ju, iu])).T  # (N (N + 1) / 2, G)
-        else:
-            bt = cf.T
+        bt, packed = vhs_operand(chol_flat)
         sl, n2pad, gpad = split3_image(bt)
         sl = sl.to(dev)
         self._keep.append(sl)
