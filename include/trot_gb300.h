@@ -158,6 +158,14 @@ size_t trot_workspace_size(const trot_system* sys, int op);
 int trot_overlap(const trot_system* sys, const double* walkers_a, const double* walkers_b,
                  double* overlaps_out, void* stream);
 
+/* Half-rotated Green's functions of all walkers, G_s = (w_s (C_s^H w_s)^{-1})^T
+ * (_half_green_from_overlap_matrix, trot/meas/rhf.py:21-25, per spin for
+ * unrestricted walkers): green_out complex128 (W, nocc_a + nocc_b, norb), rows
+ * [0, nocc_a) alpha and [nocc_a, nocc_a + nocc_b) beta (restricted walkers:
+ * (W, nocc_a, norb)); overlaps_out (optional) as trot_overlap. FP64. */
+int trot_half_green(const trot_system* sys, const double* walkers_a, const double* walkers_b, double* green_out,
+                    double* overlaps_out, void* stream);
+
 /* Force bias of all walkers (complex128 out (W, G)).
  * Replaces force_bias_kernel_rw_rh / _uw_rh: trot/meas/rhf.py:119-125,141-153;
  * trot/meas/uhf.py:43-57. */

@@ -87,6 +87,7 @@ _SIGNATURES = {
     "trot_abi_version": (_i, []),
     "trot_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(TrotSystem), _i]),
     "trot_overlap": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p]),
+    "trot_half_green": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p, _p]),
     "trot_force_bias": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p, ctypes.c_size_t, _p]),
     "trot_local_energy": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p, ctypes.c_size_t, _p]),
     "trot_apply_trotter": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),

@@ -153,6 +153,16 @@ int trot_overlap(const trot_system* s, const double* wa, const double* wb, doubl
                       (double2*)out, nullptr, (cudaStream_t)stream);
 }
 
+int trot_half_green(const trot_system* s, const double* wa, const double* wb, double* green_out,
+                    double* overlaps_out, void* stream) {
+  TROT_TRY(check_system(s));
+  TROT_TRY(check_walkers(s, wa, wb));
+  if (!green_out) { set_error("null output"); return TROT_ERR_NULL_PTR; }
+  Spins sp = make_spins(s);
+  return launch_green(sp, s->n_walkers, s->norb, (const double2*)wa, (const double2*)wb, (double2*)green_out,
+                      (double2*)overlaps_out, nullptr, (cudaStream_t)stream);
+}
+
 int trot_force_bias(const trot_system* s, const double* wa, const double* wb, double* out, void* ws,
                     size_t ws_bytes, void* stream) {
   TROT_TRY(check_system(s));

@@ -78,6 +78,27 @@ def overlap_batched(walkers, trial_data, walker_kind: str) -> torch.Tensor:
     return out
 
 
+def half_green_batched(walkers, trial_data, walker_kind: str, with_overlaps: bool = False):
+    """Half-rotated Green's functions (W, nocc_a [+ nocc_b], N) of a walker batch,
+    ``_half_green_from_overlap_matrix`` (trot/meas/rhf.py:21-25) per spin; with
+    ``with_overlaps`` also the trial overlaps (W)."""
+    kind = native.kind_of(trial_data, walker_kind)
+    wa, wb = native.split_walkers(walkers, kind)
+    ca, cb = trial_data.coeffs()
+    W, N = wa.shape[0], ca.shape[0]
+    native.check_walker_tensor(wa, ca.shape[0], ca.shape[1])
+    rows = ca.shape[1]
+    if wb is not None:
+        native.check_walker_tensor(wb, cb.shape[0], cb.shape[1], W)
+        rows += cb.shape[1]
+    green = torch.empty((W, rows, N), dtype=torch.complex128, device=wa.device)
+    ov = torch.empty(W, dtype=torch.complex128, device=wa.device) if with_overlaps else None
+    s = native.system(kind, W, trial_data)
+    _lib.call("trot_half_green", ctypes.byref(s), native.ptr(wa), native.ptr(wb), green.data_ptr(),
+              native.ptr(ov), native.stream_ptr())
+    return (green, ov) if with_overlaps else green
+
+
 def _make_overlap(walker_kind: str):
     @batched
     def overlap(walkers, trial_data):
