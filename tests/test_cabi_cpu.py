@@ -170,3 +170,31 @@ def test_ctx_builders_errors():
     assert lib.trot_half_rotate(24, 10, 5, p, p, p, None, p, None) == 3
     assert lib.trot_cisd_lci1(24, 10, 24, p, p, p, None) == 1
     assert lib.trot_cisd_lci1(24, 10, 5, p, None, p, None) == 3
+
+
+def test_half_green_arguments():
+    """trot_half_green: null output or walkers and bad shapes are rejected before any launch."""
+    s = _sys()
+    assert _status("trot_half_green", ctypes.byref(s), 0x1000, None, None, None, None) == 3
+    assert _status("trot_half_green", ctypes.byref(s), None, None, 0x1000, None, None) == 3
+    assert _status("trot_half_green", ctypes.byref(_sys(nocc_a=9)), 0x1000, None, 0x1000, None, None) == 1
+
+
+def test_cisd_packed_contraction_workspace():
+    """With chol_symmetric the Cholesky contraction runs on packed copies (extra workspace for
+    the packed triangles); the float-float gamma tile is bounded by shared memory too."""
+    lib = _lib.load()
+    for op in (_lib.OP_FORCE_BIAS, _lib.OP_LOCAL_ENERGY, _lib.OP_PROP_STEP):
+        full = lib.trot_cisd_workspace_size(ctypes.byref(_cisd()), 8, op)
+        packed = lib.trot_cisd_workspace_size(ctypes.byref(_cisd(chol_symmetric=1)), 8, op)
+        # + W N (N + 1) / 2 complex and G N (N + 1) / 2 real values, 256-byte aligned pieces
+        assert packed - full >= 8 * 55 * 16 + 12 * 55 * 8, op
+    assert lib.trot_cisd_workspace_size(ctypes.byref(_cisd()), 8, _lib.OP_OVERLAP) == \
+        lib.trot_cisd_workspace_size(ctypes.byref(_cisd(chol_symmetric=1)), 8, _lib.OP_OVERLAP)
+    # float-float gamma tile: N = 48 with 44 occupied orbitals fits the FP64 tiles but not the
+    # float-float one (mixed gl)
+    big = dict(norb=48, nocc=44, nvir=4)
+    assert lib.trot_cisd_workspace_size(ctypes.byref(_cisd(**big)), 8, _lib.OP_LOCAL_ENERGY) > 0
+    assert lib.trot_cisd_workspace_size(ctypes.byref(_cisd(gl_precision=_lib.MIXED, **big)), 8,
+                                        _lib.OP_LOCAL_ENERGY) == 0
+    assert b"exceeds shared memory" in lib.trot_last_error()
