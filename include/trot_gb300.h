@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define TROT_ABI_VERSION 2
+#define TROT_ABI_VERSION 3
 
 typedef enum {
   TROT_OK = 0,
@@ -69,20 +69,24 @@ typedef enum {
  * trot_system.mixed (this struct lives in host memory; its pointers are
  * device pointers).
  *
- * Local energy / force bias use an exact-slice BF16 product on tensor cores:
+ * Local energy / force bias use an exact-digit FP16 product on tensor cores:
  * every row x of rot_chol (rows (g, i) over orbitals p) and of the half
- * Green's function is written as x = sum_t 2^(e - 8(t+1)) q_t with integer
- * slices |q_t| <= 255 (exact in bf16) and one exponent e per row; slice
- * products accumulate exactly in FP32 (K <= 256) and products with equal
- * t + u share one accumulator.  The VHS uses a plain 3-term bf16 split
- * (x = hi + mid + lo) with FP32 accumulation. */
+ * Green's function is written as x = 2^e sum_t q_t 2^-(T + 9 t) with integer
+ * digits (exact in FP16), one exponent e per row, a leading digit of T bits
+ * (T = 9, |q_0| <= 512, for rot_chol; T = 8, |q_0| <= 256, for the Green's
+ * function) and balanced 9-bit lower digits |q_t| <= 256; a rot_chol row whose
+ * sum of |q_0| exceeds 2^15 has its exponent raised by one.  Digit products
+ * with equal t + u share one FP32 accumulator, and the two leading groups
+ * (t + u <= 1) stay below 2^24 in magnitude, so they accumulate exactly.  The
+ * VHS uses a plain 3-term bf16 split (x = hi + mid + lo) with FP32
+ * accumulation. */
 typedef struct {
-  int slices;            /* slices per operand of the exact product (5) */
+  int slices;            /* digits per operand of the exact product (5) */
   int max_order;         /* products with t + u <= max_order (4) */
   int kpad;              /* padded orbital dimension of the exact product (128) */
   int gammas_per_block[2];   /* Cholesky vectors per 128-row tile, per spin */
   int n_blocks[2];           /* tiles per spin: ceil(G / gammas_per_block) */
-  const uint16_t* rot_slices[2]; /* bf16 (slices, n_blocks, 128, kpad) per spin */
+  const uint16_t* rot_slices[2]; /* fp16 digits (slices, n_blocks, 128, kpad) per spin */
   const int32_t* rot_exp[2];     /* int32 (n_blocks, 128) row exponents per spin */
   int vhs_slices;        /* 3 */
   int vhs_order;         /* products with t + u <= vhs_order (2) */
@@ -100,6 +104,9 @@ typedef struct {
    * + q - p (p <= q) of (L + L^T) / 2, n2pad = N (N + 1) / 2 rounded up to 128,
    * and the VHS (symmetric) is produced in that packed column order. */
   int vhs_packed;
+  /* digit format of rot_slices: 1 = the FP16 digits described above (the only
+   * format this library accepts) */
+  int digit_format;
 } trot_mixed;
 
 /* Static description of one Hamiltonian + trial + propagation context.
@@ -199,8 +206,19 @@ int trot_prop_step(const trot_system* sys, const trot_state* state, const double
 /* Device status of the last mixed-precision op that used this workspace
  * (its first bytes): TROT_OK, or TROT_ERR_DEVICE_TIMEOUT when a tensor-core
  * kernel's completion wait ran out (the kernel then skipped its output, freed
- * its tensor memory and returned).  Synchronous (cudaMemcpy). */
+ * its tensor memory and returned, and the op wrote NaN results: the local
+ * energies, or the step's weights and population shift).  Synchronous
+ * (cudaMemcpy). */
 int trot_workspace_status(const void* workspace, int* status_out);
+
+/* Sticky device status of every mixed-precision op that used this workspace
+ * since the sticky word (the fourth int of the workspace) was last cleared:
+ * TROT_ERR_DEVICE_TIMEOUT if any of them timed out as above, else TROT_OK.
+ * A workspace whose first 16 bytes were zero-filled starts clear; clear != 0
+ * resets the word after reading it.  Lets a caller that issues many
+ * asynchronous calls (steps, graph replays) check once per block.
+ * Synchronous.  No counterpart in the reference (it has no device waits). */
+int trot_workspace_timeouts(void* workspace, int clear, int* status_out);
 
 /* Reduced QR of every walker with diag(R) real non-negative; Q replaces the
  * walkers in place; norm_out (complex128 (W), may be NULL) receives
@@ -248,12 +266,23 @@ int trot_split_key(int64_t* key, void* stream);
  * device memory, e.g. a JAX custom call inside a process whose GPU memory
  * XLA has pre-allocated.  Systems needing more scratch than 32 MiB
  * (trot_workspace_size(sys, TROT_OP_LOCAL_ENERGY)) are rejected with
- * TROT_ERR_WORKSPACE_TOO_SMALL.  The first call on a device resolves the
- * array's address (cudaGetSymbolAddress) and should come before any stream
- * capture; all calls share the array, so calls that overlap on the GPU race.
- * No counterpart in the reference. */
+ * TROT_ERR_WORKSPACE_TOO_SMALL.  A call outside stream capture resolves the
+ * array's address on the current device (cudaGetSymbolAddress) and caches it;
+ * calls under capture use the cache, so the first call on a device must come
+ * before any stream capture.  With CUDA's lazy module loading that first call
+ * also reserves the 32 MiB: make it before a framework pre-allocates the GPU,
+ * or set CUDA_MODULE_LOADING=EAGER.  All calls share the array, so calls that
+ * overlap on the GPU race.  A mixed-precision call whose tensor-core kernel
+ * timed out writes NaN energies; mixed-precision callers check
+ * trot_local_energy_noalloc_status.  No counterpart in the reference. */
 int trot_local_energy_noalloc(const trot_system* sys, const double* walkers_a, const double* walkers_b,
                               double* energy_out, void* stream);
+
+/* Sticky timeout status of trot_local_energy_noalloc on the current device
+ * (trot_workspace_timeouts on the built-in array): TROT_ERR_DEVICE_TIMEOUT if
+ * a call since the last clear had a tensor-core wait run out, else TROT_OK;
+ * clear != 0 resets it.  Synchronous.  No counterpart in the reference. */
+int trot_local_energy_noalloc_status(int clear, int* status_out);
 
 /* ---------------------------------------------------------------- CISD trial
  * Configuration-interaction singles+doubles trial with restricted walkers in
@@ -449,10 +478,20 @@ int trot_tc_gemm_bf16(const uint16_t* A, const uint16_t* B, float* D, int M, int
 /* Tuning knobs (process-wide; 0 restores the built-in default).  Chosen by
  * timing candidates on the caller's workload (trot_gb300.autotune); every
  * setting computes bit-identical results.  No counterpart in the reference.
- *   TROT_TUNE_EXCHANGE_TILES: walker tiles per work item of the exact-slice
+ *   TROT_TUNE_EXCHANGE_TILES: walker tiles per work item of the exact-digit
  *     exchange kernel (default 8);
- *   TROT_TUNE_EXCHANGE_GRID: persistent CTAs of that kernel (default 152). */
-typedef enum { TROT_TUNE_EXCHANGE_TILES = 0, TROT_TUNE_EXCHANGE_GRID = 1, TROT_TUNE_COUNT = 2 } trot_tune_knob;
+ *   TROT_TUNE_EXCHANGE_GRID: persistent CTAs of that kernel (default 152);
+ *   TROT_TUNE_TEST_TIMEOUT: test switch of the device-timeout path, not a
+ *     tuning knob: when v > 0 the exchange kernel's first wait is on a barrier
+ *     nothing arrives on, limited to v polls, so it takes its timeout path
+ *     (status TROT_ERR_DEVICE_TIMEOUT, no copies or MMAs issued, NaN energies)
+ *     on every call until the knob is set back to 0. */
+typedef enum {
+  TROT_TUNE_EXCHANGE_TILES = 0,
+  TROT_TUNE_EXCHANGE_GRID = 1,
+  TROT_TUNE_TEST_TIMEOUT = 2,
+  TROT_TUNE_COUNT = 3
+} trot_tune_knob;
 int trot_set_tuning(int knob, int value);
 int trot_get_tuning(int knob);
 

@@ -6,22 +6,46 @@ import torch
 from trot_gb300 import mixed
 
 
-def test_exact_slices_reconstruct_rows():
+def test_digit_slices_reconstruct_rows():
+    """Cholesky-row digits: |q_0| <= 512, balanced |q_t| <= 256, all exact in FP16,
+    representation error <= 2^-45 of the row's power-of-two scale 2^e, and the sum
+    of |q_0| over a row capped at 2^15 (the exponent is raised by one otherwise)."""
     rng = np.random.default_rng(0)
-    x = rng.normal(size=(7, 120)) * np.exp(rng.normal(size=(7, 1)) * 5)
+    x = rng.normal(size=(9, 120)) * np.exp(rng.normal(size=(9, 1)) * 5)
     x[3] = 0.0
-    x[4, :] = 2.0 ** 5  # exact power of two: the row max hits the slice range boundary
-    q, e = mixed.exact_slices(x)
-    assert q.shape == (mixed.SLICES, 7, 120)
-    assert np.all(np.abs(q) <= 255) and np.all(q == np.rint(q))
-    # every slice is exactly representable in bf16
-    qb = torch.from_numpy(q).to(torch.bfloat16).to(torch.float32).numpy()
-    np.testing.assert_array_equal(qb, q)
-    rec = sum(q[t].astype(np.float64) * np.ldexp(1.0, e - 8 * (t + 1))[:, None] for t in range(mixed.SLICES))
-    mx = np.max(np.abs(x), axis=1, keepdims=True)
-    err = np.abs(rec - x) / np.where(mx > 0, mx, 1.0)
-    assert np.max(err) <= 2.0 ** (-8 * mixed.SLICES)
+    x[4, :] = 2.0 ** 5  # exact power of two: every element sits on the digit range boundary
+    x[5, :] = 0.3       # constant row: the top digits all share one sign (largest L1 norm)
+    q, e = mixed.digit_slices(x)
+    assert q.shape == (mixed.SLICES, 9, 120)
+    assert np.all(q == np.rint(q))
+    assert np.all(np.abs(q[0]) <= 2 ** mixed.ROT_TOP_BITS)
+    assert np.all(np.abs(q[1:]) <= 2 ** (mixed.LOW_BITS - 1))
+    assert np.all(np.sum(np.abs(q[0]), axis=-1) <= mixed.ROT_L1_CAP)
+    # every digit is exactly representable in fp16
+    qh = torch.from_numpy(q).to(torch.float16).to(torch.float32).numpy()
+    np.testing.assert_array_equal(qh, q)
+    sh = [mixed.ROT_TOP_BITS + mixed.LOW_BITS * t for t in range(mixed.SLICES)]
+    rec = sum(q[t].astype(np.float64) * np.ldexp(1.0, e - sh[t])[:, None] for t in range(mixed.SLICES))
+    err = np.abs(rec - x) / np.ldexp(1.0, e)[:, None]
+    assert np.max(err) <= 2.0 ** -(sh[-1] + 1)
     assert np.all(rec[3] == 0.0)
+    # the constant row needed the raised exponent: 120 top digits of 0.3 / 0.5 * 512 = 307
+    assert int(e[5]) == 0
+
+
+def test_digit_groups_fit_fp32_exactly():
+    """Worst-case partial sums of the two leading digit-product groups against
+    Green's-function digits (|q_0| <= 256, |q_t| <= 256) stay within 2^24, so the
+    tensor core's FP32 accumulator adds them exactly."""
+    rng = np.random.default_rng(7)
+    rows = np.concatenate([rng.normal(size=(20, 128)), np.full((2, 128), 0.7), np.abs(rng.normal(size=(2, 128)))])
+    q, _ = mixed.digit_slices(rows)
+    l1_0 = np.sum(np.abs(q[0]), axis=-1)
+    l1_1 = np.sum(np.abs(q[1]), axis=-1)
+    g0max = 2.0 ** mixed.GREEN_TOP_BITS
+    glow = 2.0 ** (mixed.LOW_BITS - 1)
+    assert np.all(l1_0 * g0max <= 2 ** 24)               # group 0: sum |qA_0 qB_0|
+    assert np.all(l1_0 * glow + l1_1 * g0max <= 2 ** 24)  # group 1: sum |qA_0 qB_1| + |qA_1 qB_0|
 
 
 def test_plain_split_is_fp32_accurate():
@@ -43,8 +67,10 @@ def test_rot_tiles_layout():
     im = img.to(torch.float64).numpy().reshape(nblk, mixed.SLICES, 16, 16, 8, 8)
     qd = im.transpose(1, 0, 2, 4, 3, 5).reshape(mixed.SLICES, nblk, 128, mixed.KPAD)
     # row (g=13, i=4) lives in block 1, row 3*12+4, orbitals 0..N-1; padding is zero
-    rec = sum(qd[t, 1, 3 * n + 4, :N] * np.ldexp(1.0, int(e[1, 3 * n + 4]) - 8 * (t + 1)) for t in range(mixed.SLICES))
-    np.testing.assert_allclose(rec, rc[13, 4], rtol=0, atol=2.0 ** -40 * np.max(np.abs(rc[13, 4])))
+    sh = [mixed.ROT_TOP_BITS + mixed.LOW_BITS * t for t in range(mixed.SLICES)]
+    rec = sum(qd[t, 1, 3 * n + 4, :N] * np.ldexp(1.0, int(e[1, 3 * n + 4]) - sh[t]) for t in range(mixed.SLICES))
+    np.testing.assert_allclose(rec, rc[13, 4], rtol=0, atol=2.0 ** -44 * np.max(np.abs(rc[13, 4])))
+    assert img.dtype == torch.float16
     assert np.all(qd[:, :, :, N:] == 0)
     assert np.all(qd[:, 2, 5 * n:, :] == 0)  # last block holds 5 vectors
 

@@ -29,17 +29,19 @@ def setup():
     trial = tg.UhfTrial(ss.mo_a, ss.mo_b)
     meas_ctx = tg.make_uhf_meas_ops(sysm).build_meas_ctx(ham, trial)
     s = native.system(_lib.UHF_U, W, trial, meas_ctx, h0=ss.h0)
+    # the same system on the tensor-core path: exact-digit exchange, status words in the scratch
+    s_mixed = native.system(_lib.UHF_U, W, trial, meas_ctx, h0=ss.h0, precision=_lib.MIXED)
     walkers = []
     for seed in (31, 32):
         wa = torch.as_tensor(synthetic.perturbed_walkers(ss.mo_a, W, 0.2, seed)).cuda()
         wb = torch.as_tensor(synthetic.perturbed_walkers(ss.mo_b, W, 0.2, seed + 100)).cuda()
         walkers.append((wa, wb))
     # the struct holds raw device pointers: keep their owners (trial, meas_ctx) alive
-    return dict(lib=_lib, native=native, s=s, walkers=walkers, W=W, owners=(trial, meas_ctx))
+    return dict(lib=_lib, native=native, s=s, s_mixed=s_mixed, walkers=walkers, W=W, owners=(trial, meas_ctx))
 
 
-def _with_workspace(d, wa, wb):
-    lib, native, s = d["lib"], d["native"], d["s"]
+def _with_workspace(d, wa, wb, key="s"):
+    lib, native, s = d["lib"], d["native"], d[key]
     out = torch.empty(d["W"], dtype=torch.complex128, device="cuda")
     n = lib.load().trot_workspace_size(ctypes.byref(s), lib.OP_LOCAL_ENERGY)
     ws = torch.empty(n, dtype=torch.uint8, device="cuda")
@@ -48,8 +50,8 @@ def _with_workspace(d, wa, wb):
     return out
 
 
-def _no_alloc(d, wa, wb):
-    lib, native, s = d["lib"], d["native"], d["s"]
+def _no_alloc(d, wa, wb, key="s"):
+    lib, native, s = d["lib"], d["native"], d[key]
     out = torch.empty(d["W"], dtype=torch.complex128, device="cuda")
     lib.check(lib.load().trot_local_energy_noalloc(ctypes.byref(s), wa.data_ptr(), wb.data_ptr(), out.data_ptr(),
                                                    native.stream_ptr()))
@@ -61,6 +63,22 @@ def test_no_alloc_matches_workspace_entry_point_twice(setup):
         ref = _with_workspace(setup, wa, wb).cpu().numpy()
         got = _no_alloc(setup, wa, wb).cpu().numpy()
         assert np.max(np.abs(got - ref)) <= TOL * np.max(np.abs(ref))
+
+
+def test_no_alloc_mixed_precision_twice(setup):
+    """The tensor-core path through the built-in scratch (its status words, digit
+    planes and exchange partial sums live there): same energies as the workspace
+    entry point on two calls in a row, and the sticky timeout status reads OK."""
+    lib = setup["lib"]
+    st = ctypes.c_int(-1)
+    lib.call("trot_local_energy_noalloc_status", 1, ctypes.addressof(st))
+    for wa, wb in setup["walkers"]:
+        ref = _with_workspace(setup, wa, wb, "s_mixed").cpu().numpy()
+        got = _no_alloc(setup, wa, wb, "s_mixed").cpu().numpy()
+        assert np.all(np.isfinite(got))
+        assert np.max(np.abs(got - ref)) <= TOL * np.max(np.abs(ref))
+    lib.call("trot_local_energy_noalloc_status", 0, ctypes.addressof(st))
+    assert st.value == 0
 
 
 def test_no_alloc_rejects_oversized_system(setup):

@@ -20,7 +20,7 @@ STATUS_NAMES = {
 # trot_kind
 RHF_R, RHF_U, UHF_U = 0, 1, 2
 # trot_tune_knob
-TUNE_EXCHANGE_TILES, TUNE_EXCHANGE_GRID = 0, 1
+TUNE_EXCHANGE_TILES, TUNE_EXCHANGE_GRID, TUNE_TEST_TIMEOUT = 0, 1, 2
 # trot_precision
 FP64, MIXED = 0, 1
 # trot_op
@@ -38,7 +38,7 @@ class TrotMixed(ctypes.Structure):
         ("slices", _i), ("max_order", _i), ("kpad", _i), ("gammas_per_block", _i * 2), ("n_blocks", _i * 2),
         ("rot_slices", _p * 2), ("rot_exp", _p * 2), ("vhs_slices", _i), ("vhs_order", _i), ("n2pad", _i),
         ("gpad", _i), ("chol_t_slices", _p), ("exp_h1_half_f32", _p),
-        ("exp_h1_half_img", _p), ("vhs_packed", _i),
+        ("exp_h1_half_img", _p), ("vhs_packed", _i), ("digit_format", _i),
     ]
 
 
@@ -102,6 +102,8 @@ _SIGNATURES = {
     "trot_split_key": (_i, [_p, _p]),
     "trot_local_energy_noalloc": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p]),
     "trot_workspace_status": (_i, [_p, _p]),
+    "trot_workspace_timeouts": (_i, [_p, _i, _p]),
+    "trot_local_energy_noalloc_status": (_i, [_i, _p]),
     "trot_tc_gemm_bf16": (_i, [_p, _p, _p, _i, _i, _i, _p, _p]),
     "trot_cisd_workspace_size": (ctypes.c_size_t, [ctypes.POINTER(TrotCisd), _i, _i]),
     "trot_cisd_overlap": (_i, [ctypes.POINTER(TrotCisd), _i, _p, _p, _p, ctypes.c_size_t, _p]),
@@ -155,7 +157,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
-        if lib.trot_abi_version() != 2:
+        if lib.trot_abi_version() != 3:
             raise RuntimeError("trot_gb300 ABI version mismatch")
         _lib = lib
         return lib

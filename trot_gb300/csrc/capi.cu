@@ -284,6 +284,19 @@ int trot_workspace_status(const void* workspace, int* status_out) {
   return TROT_OK;
 }
 
+int trot_workspace_timeouts(void* workspace, int clear, int* status_out) {
+  if (!workspace || !status_out) { set_error("null pointer"); return TROT_ERR_NULL_PTR; }
+  int* sticky = static_cast<int*>(workspace) + 3;
+  cudaError_t e = cudaMemcpy(status_out, sticky, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e, "trot_workspace_timeouts");
+  if (clear) {
+    const int zero = 0;
+    e = cudaMemcpy(sticky, &zero, sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_status(e, "trot_workspace_timeouts clear");
+  }
+  return TROT_OK;
+}
+
 int trot_orthonormalize(const trot_system* s, double* wa, double* wb, double* norm_out, void* stream) {
   TROT_TRY(check_system(s));
   TROT_TRY(check_walkers(s, wa, wb));

@@ -74,7 +74,7 @@ static int cisd_splitk(int M, int Nn, int K) {
 static size_t carve_cisd(const trot_cisd* c, int W, int op, Carver& cv, CisdBuffers& b) {
   const size_t N = c->norb, n = c->nocc, v = c->nvir, G = c->nchol, nv = n * v;
   b = CisdBuffers{};
-  b.status = cv.take<int>(4);
+  b.status = cv.status();
   b.green = cv.take<double2>(W * n * N);
   b.det2 = cv.take<double2>(W);
   b.hg2 = cv.take<double2>(W);
@@ -660,9 +660,14 @@ __global__ void __launch_bounds__(256)
 cisd_energy_kernel(int G, int nchunk, double h0, const double2* __restrict__ wsc, const double2* __restrict__ hg2,
                    const double2* __restrict__ lg, const double2* __restrict__ lcs,
                    const double2* __restrict__ gpart, const double2* __restrict__ l2part,
-                   double2* __restrict__ energy) {
+                   double2* __restrict__ energy, const int* __restrict__ status) {
   __shared__ double2 red[32];
   const int b = blockIdx.x;
+  if (status[0] != 0) {  // a tensor-core product of this call timed out: no numbers
+    const double nan = __longlong_as_double(0x7FF8000000000000ll);
+    if (threadIdx.x == 0) energy[b] = cmk(nan, nan);
+    return;
+  }
   double2 lglg = cmk(0.0, 0.0), lslg = cmk(0.0, 0.0);
   for (int g = threadIdx.x; g < G; g += blockDim.x) {
     const double2 x = lg[(size_t)b * G + g];
@@ -771,7 +776,7 @@ static Spins cisd_spins(const trot_cisd* c) {
 static int cisd_run(const trot_cisd* c, int W, const double2* w, CisdBuffers& b, int stage, cudaStream_t st) {
   const int N = c->norb, n = c->nocc, v = c->nvir, G = c->nchol, nv = n * v;
   Spins sp = cisd_spins(c);
-  if (stage > 0) cudaMemsetAsync(b.status, 0, 4 * sizeof(int), st);
+  if (stage > 0) cudaMemsetAsync(b.status, 0, sizeof(int), st);  // this call's word; the sticky one persists
   TROT_TIMED("cisd_green", st, launch_green(sp, W, N, w, nullptr, b.green, b.det2, b.hg2, st));
   CISD_LAUNCH("cisd_x", cisd_x_kernel, W, 256, 0, st, N, n, v, b.green, c->ci1, b.x,
               stage >= 1 ? b.ci1g1 : nullptr, b.wsc);
@@ -902,7 +907,7 @@ int trot_cisd_local_energy(const trot_cisd* c, int W, const double* walkers, dou
   cudaStream_t st = (cudaStream_t)stream;
   TROT_TRY(cisd_run(c, W, (const double2*)walkers, b, 2, st));
   cisd_energy_kernel<<<W, 256, 0, st>>>(c->nchol, cisd_chunks(c->nchol), c->h0, b.wsc, b.hg2, b.lg, b.lcs,
-                                        b.gpart, b.l2part, (double2*)out);
+                                        b.gpart, b.l2part, (double2*)out, b.status);
   TROT_CHECK_LAUNCH("cisd_energy_kernel");
   return TROT_OK;
 }
@@ -977,7 +982,7 @@ int trot_cisd_prop_step(const trot_cisd* c, const trot_system* prop, const trot_
               b.fb);
   if (energy_out)
     CISD_LAUNCH("cisd_energy", cisd_energy_kernel, W, 256, 0, st, G, cisd_chunks(G), c->h0, b.wsc, b.hg2, b.lg,
-                b.lcs, b.gpart, b.l2part, (double2*)energy_out);
+                b.lcs, b.gpart, b.l2part, (double2*)energy_out, b.status);
   // 2. shifted fields, 3. VHS, 4. propagation in place
   TROT_TIMED("fields", st,
              launch_fields(W, G, prop->sqrt_dt, b.fb, prop->mf_shifts_im, fields, b.xs, b.shift_term, b.fb_term, st));
@@ -988,6 +993,8 @@ int trot_cisd_prop_step(const trot_cisd* c, const trot_system* prop, const trot_
   if (prop->precision == TROT_MIXED) {
     TROT_TRY(trot_apply_trotter(prop, (const double*)w, nullptr, (const double*)b.xs, (double*)w, nullptr,
                                 static_cast<char*>(ws) + cisd_bytes, ws_bytes - cisd_bytes, stream));
+    // the propagation's status block sits at the start of its workspace region
+    TROT_TRY(launch_status_merge(reinterpret_cast<const int*>(static_cast<char*>(ws) + cisd_bytes), b.status, st));
   } else {
     TROT_TIMED("vhs_fp64", st,
                launch_zgemm_cr(W, N * N, G, 1.0, b.xs, G, prop->chol_flat, N * N, false, b.vhs, N * N, false, st));
@@ -1004,7 +1011,7 @@ int trot_cisd_prop_step(const trot_cisd* c, const trot_system* prop, const trot_
   CISD_LAUNCH("cisd_weight", cisd_weight_kernel, (W + 127) / 128, 128, 0, st, a, b.ov_new);
   TROT_TIMED("step_finalize", st,
              launch_step_finalize(W, state->weights, state->scalars, (long long*)state->node_encounters, b.node_flag,
-                                  prop->pop_control_damping, prop->dt, st));
+                                  prop->pop_control_damping, prop->dt, st, b.status));
   return TROT_OK;
 }
 

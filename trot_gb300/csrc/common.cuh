@@ -8,6 +8,17 @@
 #define TROT_HD __host__ __device__ __forceinline__
 #define TROT_D __device__ __forceinline__
 
+// ---------------------------------------------------------------- device status words
+// A mixed-precision workspace starts with int[4] status words: [0] the status of
+// the current call (reset when the call begins), [3] a sticky copy that only
+// trot_workspace_timeouts clears.  A tensor-core kernel whose bounded wait ran out
+// records TROT_ERR_DEVICE_TIMEOUT in both, skips its outputs and returns; the
+// kernels that combine its results then write NaN instead of numbers.
+TROT_D void report_timeout(int* status) {
+  atomicExch(status, (int)TROT_ERR_DEVICE_TIMEOUT);
+  atomicExch(status + 3, (int)TROT_ERR_DEVICE_TIMEOUT);
+}
+
 // ---------------------------------------------------------------- complex (double2)
 TROT_HD double2 cmk(double r, double i) { return make_double2(r, i); }
 TROT_HD double2 cadd(double2 a, double2 b) { return cmk(a.x + b.x, a.y + b.y); }

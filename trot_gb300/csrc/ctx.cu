@@ -42,7 +42,7 @@ static size_t carve_ctx(int N, int G, Carver& c, CtxBuffers& b) {
   int S, gper;
   ctx_slices(N, G, S, gper);
   const size_t nn = (size_t)N * N;
-  b.status = c.take<int>(64);
+  b.status = c.status();  // 64 ints
   b.a = c.take<double>(nn);
   b.p0 = c.take<double>(nn);
   b.p1 = c.take<double>(nn);

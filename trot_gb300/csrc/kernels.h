@@ -6,12 +6,20 @@
 
 namespace trot {
 
-// Bump allocator over the caller's workspace (256-byte aligned slices).
+// Bump allocator over the caller's workspace (256-byte aligned slices).  Every
+// layout begins with a 256-byte status block at offset 0 (int[0]: the current
+// call's status, int[3]: the sticky timeout word of report_timeout), so any
+// workspace can be shared between ops without one op's buffers overwriting
+// another's status words.
 struct Carver {
+  static constexpr size_t kStatusBytes = 256;
   char* base;
-  size_t size, used = 0;
+  size_t size, used = kStatusBytes;
   bool ok = true;
-  Carver(void* b, size_t s) : base(static_cast<char*>(b)), size(s) {}
+  Carver(void* b, size_t s) : base(static_cast<char*>(b)), size(s) {
+    if (base && size < kStatusBytes) ok = false;
+  }
+  int* status() { return (base && size >= kStatusBytes) ? reinterpret_cast<int*>(base) : nullptr; }
   template <class T>
   T* take(size_t count) {
     size_t off = (used + 255) & ~size_t(255);
@@ -67,15 +75,22 @@ struct TrotterArgs {
   double dt, h0_prop, w_floor, w_cap;
 };
 int launch_trotter(const Spins& sp, const TrotterArgs& a, cudaStream_t st);
+// status (optional): the mixed-precision status words of the step (int[4], see
+// report_timeout); when status[0] is set the step's weights and population shift
+// become NaN instead of numbers computed from skipped tensor-core results
 int launch_step_finalize(int W, double* weights, double* scalars, long long* nodes,
-                         const int* node_flag, double damping, double dt, cudaStream_t st);
+                         const int* node_flag, double damping, double dt, cudaStream_t st,
+                         const int* status = nullptr);
 
 int exchange_chunks(int G);
 int launch_exchange(const Spins& sp, int W, int N, int G, const double2* green, double2* partial,
                     cudaStream_t st);
 // e1: e1_parts consecutive arrays of W values (one per spin for the mixed path), added in order
+// status (optional): as for launch_step_finalize; the energies become NaN when status[0] is set
 int launch_energy_combine(int W, int G, int nchunks, double h0, const double2* fb, const double2* e1, int e1_parts,
-                          const double2* partial, double2* energy, cudaStream_t st);
+                          const double2* partial, double2* energy, cudaStream_t st, const int* status = nullptr);
+// dst[0] = dst[3] = src[0] when src[0] is set (status words of two workspace regions, see report_timeout)
+int launch_status_merge(const int* src, int* dst, cudaStream_t st);
 
 // walkers.cu
 // write_q = false: only the norms prod_j |R_jj| (free-projection qr_norm); the walkers are left unchanged

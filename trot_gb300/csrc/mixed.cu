@@ -7,6 +7,7 @@
 //  * VHS = x_shifted . chol: 3-term BF16 split on tcgen05, FP32 accumulation;
 //  * one-body half steps and the Taylor series: FP32 on the CUDA cores.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 
@@ -19,10 +20,13 @@
 namespace trot {
 
 // ------------------------------------------------------------------ Green's functions in float-float
-// Same quantities as green_kernel (green.cu): M_s = C_s^T w_s, M_s^{-1} by
+// Same quantities as green_kernel (green.cu): M_s = C_s^T w_s in FP64, M_s^{-1} by
 // FP64 Gauss-Jordan, G_s = (w_s M_s^{-1})^T and e1 = sum_s mult_s sum G_s o rot_h1_s,
-// with the two N x n^2 products in float-float (FP32 pairs, ~2^-44 relative)
-// on the FP32 pipe instead of FP64.  One CTA per walker.
+// with the N x n^2 product G_s in float-float (FP32 pairs, ~2^-44 relative) on the
+// FP32 pipe.  M_s stays FP64: its rounding error is amplified by the condition
+// number of M_s (10^4 - 10^5 for walkers far from the trial), and a float-float M_s
+// moved such walkers' local energies by up to 5e-5 Ha at |E_L| ~ 5e5 Ha.  One CTA per
+// (walker, spin).
 __global__ void __launch_bounds__(256)
 green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* __restrict__ wb,
                 double2* __restrict__ green, double2* __restrict__ e1_out) {
@@ -32,8 +36,7 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
   const int b = blockIdx.x, s = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
   const int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
   ffc* Wf = reinterpret_cast<ffc*>(smem_raw);                    // N x n
-  ff* Cf = reinterpret_cast<ff*>(Wf + (size_t)N * nmax);          // N x n
-  double2* Md = reinterpret_cast<double2*>(Cf + (size_t)N * nmax + ((N * nmax) & 1));  // n x n
+  double2* Md = reinterpret_cast<double2*>(Wf + (size_t)N * nmax);  // n x n
   double2* Mi = Md + nmax * nmax;                                 // n x n
   ffc* Mif = reinterpret_cast<ffc*>(Mi + nmax * nmax);            // n x n
   ff e1r{0.f, 0.f}, e1i{0.f, 0.f};
@@ -45,39 +48,30 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
     for (int e = tid; e < N * n; e += nt) {
       const double2 x = w[e];
       Wf[e] = ffc{ff_from_d(x.x), ff_from_d(x.y)};
-      Cf[e] = ff_from_d(C[e]);
     }
     __syncthreads();
     for (int e = tid; e < n * n; e += nt) {
-      // four independent accumulator pairs over p (mod 4): the N-long dot products are
-      // latency-bound chains otherwise
+      // M[i][j] = sum_p C[p][i] w[p][j] in FP64 from the walker in global memory (L1-resident
+      // after the staging loop); two independent accumulator pairs over p (mod 2) in a fixed
+      // order, so the result is the same on every run
       const int i = e / n, j = e % n;
-      ff ar[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-      ff ai[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      double ar0 = 0.0, ai0 = 0.0, ar1 = 0.0, ai1 = 0.0;
       int p = 0;
-      for (; p + 4 <= N; p += 4) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const ff c = Cf[(p + u) * n + i];
-          const ffc x = Wf[(p + u) * n + j];
-          ff_mad(ar[u], c, x.re);
-          ff_mad(ai[u], c, x.im);
-        }
+      for (; p + 2 <= N; p += 2) {
+        const double c0 = C[p * n + i], c1 = C[(p + 1) * n + i];
+        const double2 x0 = w[p * n + j], x1 = w[(p + 1) * n + j];
+        ar0 = fma(c0, x0.x, ar0);
+        ai0 = fma(c0, x0.y, ai0);
+        ar1 = fma(c1, x1.x, ar1);
+        ai1 = fma(c1, x1.y, ai1);
       }
-      for (; p < N; ++p) {
-        const ff c = Cf[p * n + i];
-        const ffc x = Wf[p * n + j];
-        ff_mad(ar[0], c, x.re);
-        ff_mad(ai[0], c, x.im);
+      if (p < N) {
+        const double c0 = C[p * n + i];
+        const double2 x0 = w[p * n + j];
+        ar0 = fma(c0, x0.x, ar0);
+        ai0 = fma(c0, x0.y, ai0);
       }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        ar[u] = ff_fast(ar[u].hi, ar[u].lo);
-        ai[u] = ff_fast(ai[u].hi, ai[u].lo);
-      }
-      const ff sr = ff_add(ff_add(ar[0], ar[1]), ff_add(ar[2], ar[3]));
-      const ff si = ff_add(ff_add(ai[0], ai[1]), ff_add(ai[2], ai[3]));
-      Md[e] = make_double2(ff_d(sr), ff_d(si));
+      Md[e] = make_double2(ar0 + ar1, ai0 + ai1);
     }
     __syncthreads();
     block_gauss_jordan(Md, n, n, Mi, &piv, red);
@@ -116,7 +110,7 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
 static int launch_green_ff(const Spins& sp, int W, int N, const double2* wa, const double2* wb, double2* green,
                            double2* e1_out, cudaStream_t st) {
   const int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
-  const size_t smem = (size_t)N * nmax * (sizeof(ffc) + sizeof(ff)) + 16 + (size_t)nmax * nmax * 3 * 16;
+  const size_t smem = (size_t)N * nmax * sizeof(ffc) + (size_t)nmax * nmax * 3 * 16;
   if (smem > 200 * 1024) {
     set_error("green_ff: %zu bytes of shared memory needed", smem);
     return TROT_ERR_UNSUPPORTED;
@@ -136,6 +130,12 @@ static constexpr int kGroups = 5;     // accumulators for t + u = 0..4
 static constexpr int kSlices = 5;
 static constexpr int kSlots = 2;      // ring of Green's-function slice buffers
 static constexpr int kMaxOcc = 16;    // largest n the epilogue handles (2 * n_pad <= 32 columns per walker)
+// FP16 digit format of the exact product (trot_mixed.digit_format 1): Cholesky rows
+// 2^eA sum_t qA_t 2^-(9 + 9t), Green's-function rows 2^eB sum_u qB_u 2^-(8 + 9u);
+// digit products of order d = t + u carry 2^(eA + eB - 17 - 9d)
+static constexpr int kDigitFormat = 1;
+static constexpr int kRotTopBits = 9, kGreenTopBits = 8, kLowBits = 9;
+static constexpr int kGreenBits = kGreenTopBits + kLowBits * (kSlices - 1);  // 44 fixed-point bits per row
 static constexpr uint32_t kAImg = (uint32_t)kSlices * 128 * kKP * 2;  // 163840 B: 5 rot slices of a tile
 static constexpr uint32_t kBImg = (uint32_t)kBN * kKH * 2;            // 12288 B: one K-half of a green slice
 
@@ -192,7 +192,7 @@ static size_t carve_mixed(const trot_system* s, const Spins& sp, Carver& c, Mixe
   const size_t W = s->n_walkers, N = s->norb, G = s->nchol;
   m = MixedBuffers{};
   if (op == TROT_OP_SR || op == TROT_OP_QR) return c.used;
-  m.status = c.take<int>(4);
+  m.status = c.status();
   const bool meas = op == TROT_OP_FORCE_BIAS || op == TROT_OP_LOCAL_ENERGY || op == TROT_OP_PROP_STEP;
   if (meas) {
     m.green = c.take<double2>(W * sp.ntot * N);
@@ -254,14 +254,15 @@ TROT_D long long rint_scaled(double x, int s) {
   return (u >> 63) ? -(long long)q : (long long)q;
 }
 
-// ------------------------------------------------------------------ Green's function slices
+// ------------------------------------------------------------------ Green's function digits
 // Rows (b, spin, c in {re, im}, j) of the half Green's function over orbitals
-// p, as exact fixed-point bf16 slices: v = round(x 2^(40 - e)) (|v| <= 2^40),
-// balanced base-256 digits q_0..q_4 (|q| <= 255), x ~= sum_t q_t 2^(e - 8(t+1)).
-// Written straight into the shared-memory image of the exchange kernel's B
-// operand: per walker tile, per slice, per K-half, kBN rows (walker bl, row
-// c*n_pad + j) x 64 orbitals in core-matrix order; padding rows are zero.
-// One CTA per tile.
+// p, as exact integer FP16 digits: v = round(x 2^(44 - e)) (|v| <= 2^44, e the
+// smallest integer with max |x| <= 2^e), an 8-bit leading digit q_0 = round(v /
+// 2^36) (|q_0| <= 256) and balanced 9-bit digits q_1..q_4 (|q| <= 256), so
+// x ~= 2^e sum_t q_t 2^-(8 + 9 t).  Written straight into the shared-memory image
+// of the exchange kernel's B operand: per walker tile, per digit, per K-half, kBN
+// rows (walker bl, row c*n_pad + j) x 64 orbitals in core-matrix order; padding
+// rows are zero.  One CTA per tile.
 __global__ void __launch_bounds__(256)
 green_slices_kernel(int N, int n, int n_pad, int WB, int W, int ntot, int off, const double2* __restrict__ green,
                     uint16_t* __restrict__ gq, int32_t* __restrict__ ge) {
@@ -289,23 +290,22 @@ green_slices_kernel(int N, int n, int n_pad, int WB, int W, int ntot, int off, c
     }
     // e = the smallest integer with max |x| <= 2^e, from the bits of the maximum
     const int E = (int)((mx >> 52) & 0x7FF);
-    const bool nonfinite = E == 0x7FF;  // the row's slices become NaN, so its products are NaN
+    const bool nonfinite = E == 0x7FF;  // the row's digits become NaN, so its products are NaN
     int e = 0;
     if (mx != 0 && !nonfinite) e = E == 0 ? -1022 : (E - 1023) + ((mx & 0xFFFFFFFFFFFFFull) != 0 ? 1 : 0);
     if (lane == 0) ge[(size_t)tile * kBN + row] = e;
 #pragma unroll
     for (int k = 0; k < kKP / 32; ++k) {
       const int p = lane + 32 * k;
-      long long v = rint_scaled(x[k], 8 * kSlices - e);
+      long long v = rint_scaled(x[k], kGreenBits - e);
 #pragma unroll
       for (int t = 0; t < kSlices; ++t) {
-        const int sh = 8 * (kSlices - 1 - t);
-        long long d = sh > 0 ? ((v + (1ll << (sh - 1))) >> sh) : v;
-        d = d > 255 ? 255 : (d < -255 ? -255 : d);
+        const int sh = kLowBits * (kSlices - 1 - t);
+        const long long d = sh > 0 ? ((v + (1ll << (sh - 1))) >> sh) : v;  // |d| <= 256 for every t
         v -= d << sh;
-        const __nv_bfloat16 h = __int2bfloat16_rn((int)d);
+        const __half h = __int2half_rn((int)d);
         gq[(((size_t)tile * kSlices + t) * 2 + (p >> 6)) * kBN * kKH + img_idx64(row, p & 63)] =
-            nonfinite ? (uint16_t)0x7FC0u : *reinterpret_cast<const uint16_t*>(&h);
+            nonfinite ? (uint16_t)0x7E00u : __half_as_ushort(h);
       }
     }
   }
@@ -314,16 +314,16 @@ green_slices_kernel(int N, int n, int n_pad, int WB, int W, int ntot, int off, c
 // ------------------------------------------------------------------ exact exchange / trace kernel
 // A persistent CTA walks work items = (tile of gb Cholesky vectors: 128 rows
 // (g, i), run of walker tiles: WB walkers x S rows = kBN = 96 MMA columns).
-// Warp 16 (one lane) is the producer: it bulk-copies the five rot_chol slices of
-// the item's Cholesky tile into shared memory, streams the Green's-function
-// slices of each walker tile as 64-wide K halves through a 2-slot ring, and
-// issues the MMAs: products q_t (rot) x q_u (green) with t + u = d accumulate
-// exactly in TMEM group d (d = 0..4).  One accumulator buffer (5 x 96 columns):
+// Warp 16 (one lane) is the producer: it bulk-copies the five FP16 rot_chol digit
+// planes of the item's Cholesky tile into shared memory, streams the Green's-function
+// digit planes of each walker tile as 64-wide K halves through a 2-slot ring, and
+// issues the FP16 MMAs: products q_t (rot) x q_u (green) with t + u = d accumulate
+// in TMEM group d (d = 0..4), exactly for d <= 1 (every partial sum stays below 2^24).  One accumulator buffer (5 x 96 columns):
 // the epilogue copies a tile's values out of TMEM into registers and releases it
 // at once, so the MMAs of the next tile overlap the epilogue's arithmetic.
 // Warps 0-15 are the epilogue (four warps per TMEM lane quadrant, each taking a
 // quarter of the columns j): they rebuild
-// f_g[i][j] = 2^(eA + eB - 16) sum_d 2^(-8 d) A_d in float-float and form, per
+// f_g[i][j] = 2^(eA + eB - 17) sum_d 2^(-9 d) A_d in float-float and form, per
 // walker, the exchange sum_g sum_ij f_gij f_gji (trot/meas/rhf.py:33-60) and the
 // traces c_g = sum_i f_gii (Coulomb / force bias, trot/meas/rhf.py:119-125).
 struct ExArgs {
@@ -338,6 +338,7 @@ struct ExArgs {
   double2* xpart;
   int nblk_total;
   int* status;
+  int test_timeout_polls;  // > 0: the producer's first wait is on a barrier nothing arrives on
 };
 
 static constexpr int kExThreads = 544;  // 16 epilogue warps + 1 producer warp
@@ -371,6 +372,8 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 11);
   int* flag = reinterpret_cast<int*>(bars + 12);  // epilogue go/stop broadcast
   uint64_t* a_free = bars + 13;     // the MMAs of the previous work item are done with sA
+  uint64_t* never = bars + 14;      // nothing arrives on it (the status-path test's wait)
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 9);  // producer gave up: epilogue stops
   constexpr int WBT = 24 / (2 * JH);  // walkers per tile: kBN / (2 n_pad) with n_pad = 4 JH
 
   const SpinLayout& L = a.L;
@@ -387,6 +390,8 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
     }
     tc::mbar_init(acc_full, 1);
     tc::mbar_init(acc_empty, 16);
+    tc::mbar_init(never, 1);
+    *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   tc::fence_before_sync();
@@ -398,7 +403,7 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
     // ------------------------------------------------ producer: loads + MMAs (one lane)
     if (lane == 0) {
       bool ok = true;
-      const uint32_t idesc = tc::idesc_bf16_f32(128, kBN);
+      const uint32_t idesc = tc::idesc_f16_f32(128, kBN);
       const uint32_t sA_u = tc::smem_u32(sA), ring_u = tc::smem_u32(ring);
       const uint64_t ad0 = tc::smem_desc(sA_u, 128, kKP * 16);
       const uint32_t adlo = (uint32_t)ad0, ahi = (uint32_t)(ad0 >> 32);
@@ -406,6 +411,9 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
       const uint32_t bhi = (uint32_t)(bd0 >> 32);
       constexpr int kUnits = kSlices * 2;  // ring units per tile: (slice u, K-half h)
       int g_issue = 0, g_base = 0, tg = 0, kitem = 0;  // CTA-wide unit / tile / item counters
+      // status-path test (TROT_TUNE_TEST_TIMEOUT): a bounded wait on a barrier nothing
+      // arrives on runs out before any copy or MMA is issued
+      if (a.test_timeout_polls > 0) ok = tc::mbar_wait(never, 0u, (uint32_t)a.test_timeout_polls);
       for (int item = blockIdx.x; item < a.n_items && ok; item += gridDim.x, ++kitem) {
         const int blk = item / a.chunks;
         const int t0 = (item % a.chunks) * a.tiles_per_item, t1 = min(L.ntiles, t0 + a.tiles_per_item);
@@ -461,9 +469,13 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
         tg += ntl;
       }
       if (!ok) {
-        atomicExch(a.status, (int)TROT_ERR_DEVICE_TIMEOUT);
+        report_timeout(a.status);
         // let issued copies / MMAs drain (bounded) before the CTA frees its memory
-        for (int k = 0; k < kSlots; ++k) tc::mbar_wait(&empty[k], 0u, 1000000u);
+        if (g_issue > 0)
+          for (int k = 0; k < kSlots; ++k) tc::mbar_wait(&empty[k], 0u, 1000000u);
+        // release the epilogue: its next accumulator wait completes and it stops
+        *abort_flag = 1;
+        tc::mbar_arrive(acc_full);
       }
     }
     __syncwarp();
@@ -485,10 +497,10 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
     const int ea = a.rot_e[(size_t)blk * 128 + r];
     for (int it = 0; it < ntl; ++it, ++tgl) {
       const int tile = t0 + it;
-      if (etid == 0) *flag = tc::mbar_wait(acc_full, (uint32_t)(tgl & 1)) ? 1 : 0;
+      if (etid == 0) *flag = (tc::mbar_wait(acc_full, (uint32_t)(tgl & 1)) && *abort_flag == 0) ? 1 : 0;
       tc::named_bar(1, kExEpi);
       if (!*flag) {
-        if (etid == 0) atomicExch(a.status, (int)TROT_ERR_DEVICE_TIMEOUT);
+        if (etid == 0) report_timeout(a.status);
         stop = true;
         break;
       }
@@ -519,13 +531,16 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
               asm volatile("" : "+r"(v));  // consume after tcgen05.wait::ld
               g[d] = __uint_as_float(v);
             }
-            ff x = ff_two_sum(g[0], g[1] * 0.00390625f);
-            float lo = x.lo + g[2] * 1.52587890625e-05f;
-            lo += g[3] * 5.9604644775390625e-08f;
-            lo += g[4] * 2.3283064365386963e-10f;
+            // sum_d 2^(-9 d) A_d: the 2^-9d scalings are exact, the leading pair error-free
+            ff x = ff_two_sum(g[0], g[1] * 1.953125e-03f);
+            float lo = x.lo + g[2] * 3.814697265625e-06f;
+            lo += g[3] * 7.450580596923828125e-09f;
+            lo += g[4] * 1.4551915228366852e-11f;
             x = ff_fast(x.hi, lo);
-            const float sc = pow2f(ea + eB[bl * L.S + c * L.n_pad + j0 + jj] - 16);
-            const ff y{x.hi * sc, x.lo * sc};
+            // times 2^(eA - 9) 2^(eB - 8), as two exact power-of-two factors
+            const float sc = pow2f(ea - kRotTopBits);
+            const float sb = pow2f(eB[bl * L.S + c * L.n_pad + j0 + jj] - kGreenTopBits);
+            const ff y{x.hi * sc * sb, x.lo * sc * sb};
             if (c == 0) fre[bl][jj] = y; else fim[bl][jj] = y;
           }
       }
@@ -730,7 +745,7 @@ vhs_gemm_kernel(int mtiles, int ntiles, int gpad, int n2pad, const uint16_t* __r
         if (ok) tc::mma_commit(&acc_full[abuf]);
       }
       if (!ok) {
-        atomicExch(status, (int)TROT_ERR_DEVICE_TIMEOUT);
+        report_timeout(status);
         for (int k = 0; k < 2; ++k) tc::mbar_wait(&empty[k], 0u, 1000000u);
       }
     }
@@ -744,7 +759,7 @@ vhs_gemm_kernel(int mtiles, int ntiles, int gpad, int n2pad, const uint16_t* __r
       if (tid == 0) *flag = tc::mbar_wait(&acc_full[abuf], (uint32_t)((nt / 2) & 1)) ? 1 : 0;
       tc::named_bar(1, 128);
       if (!*flag) {
-        if (tid == 0) atomicExch(status, (int)TROT_ERR_DEVICE_TIMEOUT);
+        if (tid == 0) report_timeout(status);
         break;
       }
       tc::fence_after_sync();
@@ -1071,7 +1086,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, Tro
         }
       }
       if (!ok) {
-        atomicExch(g.status, (int)TROT_ERR_DEVICE_TIMEOUT);
+        report_timeout(g.status);
         // let copies / MMAs already issued land before the tensor memory is released
         for (int k = 0; k < 2; ++k) tc::mbar_wait(&empty[k], 0u, 1000000u);
         for (int k = 0; k < 2; ++k) tc::mbar_wait(&full[k], 0u, 1000000u);
@@ -1116,7 +1131,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, Tro
       for (int wi = 0; wi < WPC; ++wi) {
         if (wi >= nw) break;
         if (!tc::mbar_wait(&acc_full[wi], (uint32_t)(step & 1))) {
-          atomicExch(g.status, (int)TROT_ERR_DEVICE_TIMEOUT);
+          report_timeout(g.status);
           ok = false;
           break;
         }
@@ -1292,8 +1307,10 @@ static int check_mixed_shapes(const trot_system* s, const Spins& sp) {
   if (s->norb > kKP) { set_error("mixed path: norb %d > %d", s->norb, kKP); return TROT_ERR_UNSUPPORTED; }
   for (int q = 0; q < sp.nspin; ++q)
     if (sp.n[q] > kMaxOcc) { set_error("mixed path: nocc %d > %d", sp.n[q], kMaxOcc); return TROT_ERR_UNSUPPORTED; }
-  if (s->mixed->kpad != kKP || s->mixed->slices != kSlices || s->mixed->max_order != kGroups - 1) {
-    set_error("mixed context layout mismatch");
+  if (s->mixed->kpad != kKP || s->mixed->slices != kSlices || s->mixed->max_order != kGroups - 1 ||
+      s->mixed->digit_format != kDigitFormat) {
+    set_error("mixed context layout mismatch (kpad %d, digits %d, order %d, digit format %d)", s->mixed->kpad,
+              s->mixed->slices, s->mixed->max_order, s->mixed->digit_format);
     return TROT_ERR_BAD_SHAPE;
   }
   return TROT_OK;
@@ -1351,6 +1368,7 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
     a.xpart = m.xpart;
     a.nblk_total = m.nblk_total;
     a.status = m.status;
+    a.test_timeout_polls = tune_get(TROT_TUNE_TEST_TIMEOUT);
     const int gknob = tune_get(TROT_TUNE_EXCHANGE_GRID);
     dim3 grid(std::min(a.n_items, gknob > 0 ? gknob : 152));
     TROT_TIMED("exchange_exact_tc", st, launch_exchange_exact(L.n_pad / 4, grid, a, st));
@@ -1506,7 +1524,7 @@ static int begin(const trot_system* s, const Spins& sp, Carver& c, MixedBuffers&
     set_error("workspace too small: %zu < %zu", c.size, c.used);
     return TROT_ERR_WORKSPACE_TOO_SMALL;
   }
-  cudaMemsetAsync(m.status, 0, 4 * sizeof(int), st);
+  cudaMemsetAsync(m.status, 0, sizeof(int), st);  // this call's status word (the sticky one persists)
   return TROT_OK;
 }
 
@@ -1530,7 +1548,7 @@ int mixed_local_energy(const trot_system* s, const Spins& sp, const double2* wa,
   TROT_TRY(launch_green_ff(sp, s->n_walkers, s->norb, wa, wb, m.green, m.e1, st));
   TROT_TRY(run_slices_and_exchange(s, sp, m, st));
   return launch_energy_combine(s->n_walkers, s->nchol, m.nblk_total, s->h0, m.fb, m.e1, sp.nspin, m.xpart, energy,
-                               st);
+                               st, m.status);
 }
 
 int mixed_apply_trotter(const trot_system* s, const Spins& sp, const double2* xs, const TrotterArgs& a, void* ws,
@@ -1541,7 +1559,7 @@ int mixed_apply_trotter(const trot_system* s, const Spins& sp, const double2* xs
   MixedBuffers m;
   carve_mixed(s, sp, c, m, TROT_OP_APPLY_TROTTER);
   if (!c.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, c.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
-  cudaMemsetAsync(m.status, 0, 4 * sizeof(int), st);
+  cudaMemsetAsync(m.status, 0, sizeof(int), st);
   TROT_TRY(run_vhs(s, m, xs, st));
   return run_trotter(s, sp, a, m, st);
 }
@@ -1558,7 +1576,8 @@ int mixed_prop_step(const trot_system* s, const Spins& sp, const trot_state* sta
   TROT_TRY(run_slices_and_exchange(s, sp, m, st));
   if (energy_out)
     TROT_TIMED("energy_combine", st,
-               launch_energy_combine(W, G, m.nblk_total, s->h0, m.fb, m.e1, sp.nspin, m.xpart, energy_out, st));
+               launch_energy_combine(W, G, m.nblk_total, s->h0, m.fb, m.e1, sp.nspin, m.xpart, energy_out, st,
+                                     m.status));
   TROT_TIMED("fields", st, launch_fields(W, G, s->sqrt_dt, m.fb, s->mf_shifts_im, fields, m.xs, m.shift_term,
                                          m.fb_term, st));
   TROT_TRY(run_vhs(s, m, m.xs, st));
@@ -1571,7 +1590,7 @@ int mixed_prop_step(const trot_system* s, const Spins& sp, const trot_state* sta
   TROT_TRY(run_trotter(s, sp, a, m, st));
   TROT_TIMED("step_finalize", st, launch_step_finalize(W, state->weights, state->scalars,
                                                        (long long*)state->node_encounters, m.node_flag,
-                                                       s->pop_control_damping, s->dt, st));
+                                                       s->pop_control_damping, s->dt, st, m.status));
   return TROT_OK;
 }
 

@@ -17,14 +17,24 @@
 //  * at most kNoAllocScratchBytes (32 MiB) of scratch; larger systems are
 //    rejected with TROT_ERR_WORKSPACE_TOO_SMALL (use trot_local_energy with a
 //    caller workspace instead);
-//  * the first call on each device looks up the array's device address with
-//    cudaGetSymbolAddress while that device is current; make that first call
-//    before any stream capture begins;
+//  * a call outside stream capture looks up the array's device address with
+//    cudaGetSymbolAddress on the current device and caches it; a call under
+//    capture uses the cached address, so the first call on each device must
+//    come before any stream capture begins.  Under CUDA's lazy module loading
+//    (the default) that first lookup also loads the library's device code and
+//    so reserves the 32 MiB on that device: make it before a framework
+//    pre-allocates the GPU's memory, or set CUDA_MODULE_LOADING=EAGER.  After
+//    cudaDeviceReset (or any destruction of the primary context) the next call
+//    outside capture resolves the address again;
 //  * every call on a device shares the same array and leaves its contents
-//    behind.  No byte of it has to start at zero: each call writes every
-//    scratch value before reading it.  Calls whose kernels overlap on the GPU
-//    (different streams, or different host threads without ordering) race on
-//    the array: order them on one stream;
+//    behind.  The array starts zero-filled; each call writes every scratch
+//    value it reads, except the status block at its start: int 0 is reset by
+//    each call and int 3 keeps a sticky record of device timeouts, which
+//    trot_local_energy_noalloc_status reads (and clears).  A mixed-precision
+//    call whose tensor-core kernel timed out returns NaN energies, never stale
+//    numbers.  Calls whose kernels overlap on the GPU (different streams, or
+//    different host threads without ordering) race on the array: order them
+//    on one stream;
 //  * nothing here calls cudaMalloc, cudaFree or any allocating routine.
 #include <mutex>
 
@@ -41,8 +51,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 std::mutex g_setup_mu;
 void* g_scratch_addr[kMaxDevices] = {};
 
-// Device address of g_noalloc_scratch on the current device (looked up once per device).
-int scratch_for_current_device(void** out) {
+// Device address of g_noalloc_scratch on the current device: looked up again
+// whenever `stream` is not capturing (so a re-created context is followed), the
+// cached value under capture.
+int scratch_for_current_device(cudaStream_t stream, void** out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
@@ -50,12 +62,19 @@ int scratch_for_current_device(void** out) {
     set_error("device ordinal %d outside the %d devices the no-alloc scratch table covers", dev, kMaxDevices);
     return TROT_ERR_UNSUPPORTED;
   }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(stream, &cap);
+  if (e != cudaSuccess) return cuda_status(e, "cudaStreamIsCapturing");
   std::lock_guard<std::mutex> lk(g_setup_mu);
-  if (g_scratch_addr[dev] == nullptr) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(no-alloc scratch)");
     g_scratch_addr[dev] = p;
+  } else if (g_scratch_addr[dev] == nullptr) {
+    set_error("trot_local_energy_noalloc: first call on device %d is under stream capture; make one call "
+              "before capturing", dev);
+    return TROT_ERR_UNSUPPORTED;
   }
   *out = g_scratch_addr[dev];
   return TROT_OK;
@@ -78,7 +97,16 @@ extern "C" int trot_local_energy_noalloc(const trot_system* sys, const double* w
     return TROT_ERR_WORKSPACE_TOO_SMALL;
   }
   void* scratch = nullptr;
-  int rc = scratch_for_current_device(&scratch);
+  int rc = scratch_for_current_device((cudaStream_t)stream, &scratch);
   if (rc != TROT_OK) return rc;
   return trot_local_energy(sys, walkers_a, walkers_b, energy_out, scratch, kNoAllocScratchBytes, stream);
+}
+
+extern "C" int trot_local_energy_noalloc_status(int clear, int* status_out) {
+  using namespace trot;
+  if (!status_out) { set_error("null pointer"); return TROT_ERR_NULL_PTR; }
+  void* scratch = nullptr;
+  int rc = scratch_for_current_device((cudaStream_t)0, &scratch);
+  if (rc != TROT_OK) return rc;
+  return trot_workspace_timeouts(scratch, clear, status_out);
 }

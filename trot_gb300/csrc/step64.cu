@@ -126,9 +126,16 @@ int launch_trotter(const Spins& sp, const TrotterArgs& a, cudaStream_t st) {
 // ------------------------------------------------------------------ population control
 // trot/prop/afqmc.py:126,132-134: nodes += count(flag); E_shift = e_est - damping log(max(mean w, 1e-300)) / dt
 __global__ void __launch_bounds__(1024)
-step_finalize_kernel(int W, const double* __restrict__ weights, double* __restrict__ scalars,
-                     long long* __restrict__ nodes, const int* __restrict__ node_flag, double damping, double dt) {
+step_finalize_kernel(int W, double* __restrict__ weights, double* __restrict__ scalars,
+                     long long* __restrict__ nodes, const int* __restrict__ node_flag, double damping, double dt,
+                     const int* __restrict__ status) {
   __shared__ double2 red[32];
+  if (status && status[0] != 0) {  // a tensor-core kernel of this step timed out: no numbers
+    const double nan = __longlong_as_double(0x7FF8000000000000ll);
+    for (int i = threadIdx.x; i < W; i += blockDim.x) weights[i] = nan;
+    if (threadIdx.x == 0) scalars[0] = nan;
+    return;
+  }
   double2 acc = cmk(0.0, 0.0);  // (sum w, node count)
   for (int i = threadIdx.x; i < W; i += blockDim.x) {
     acc.x += weights[i];
@@ -144,8 +151,8 @@ step_finalize_kernel(int W, const double* __restrict__ weights, double* __restri
 }
 
 int launch_step_finalize(int W, double* weights, double* scalars, long long* nodes, const int* node_flag,
-                         double damping, double dt, cudaStream_t st) {
-  step_finalize_kernel<<<1, 1024, 0, st>>>(W, weights, scalars, nodes, node_flag, damping, dt);
+                         double damping, double dt, cudaStream_t st, const int* status) {
+  step_finalize_kernel<<<1, 1024, 0, st>>>(W, weights, scalars, nodes, node_flag, damping, dt, status);
   TROT_CHECK_LAUNCH("step_finalize_kernel");
   return TROT_OK;
 }
@@ -218,9 +225,14 @@ int launch_exchange(const Spins& sp, int W, int N, int G, const double2* green, 
 __global__ void __launch_bounds__(256)
 energy_combine_kernel(int G, int nchunks, double h0, const double2* __restrict__ fb,
                       const double2* __restrict__ e1, int e1_parts, const double2* __restrict__ partial,
-                      double2* __restrict__ energy) {
+                      double2* __restrict__ energy, const int* __restrict__ status) {
   __shared__ double2 red[32];
   const int b = blockIdx.x;
+  if (status && status[0] != 0) {  // the exchange / force-bias kernel timed out: no numbers
+    const double nan = __longlong_as_double(0x7FF8000000000000ll);
+    if (threadIdx.x == 0) energy[b] = cmk(nan, nan);
+    return;
+  }
   double2 c = cmk(0.0, 0.0), x = cmk(0.0, 0.0);
   for (int g = threadIdx.x; g < G; g += blockDim.x) {
     const double2 f = fb[(size_t)b * G + g];
@@ -237,9 +249,23 @@ energy_combine_kernel(int G, int nchunks, double h0, const double2* __restrict__
 }
 
 int launch_energy_combine(int W, int G, int nchunks, double h0, const double2* fb, const double2* e1, int e1_parts,
-                          const double2* partial, double2* energy, cudaStream_t st) {
-  energy_combine_kernel<<<W, 256, 0, st>>>(G, nchunks, h0, fb, e1, e1_parts, partial, energy);
+                          const double2* partial, double2* energy, cudaStream_t st, const int* status) {
+  energy_combine_kernel<<<W, 256, 0, st>>>(G, nchunks, h0, fb, e1, e1_parts, partial, energy, status);
   TROT_CHECK_LAUNCH("energy_combine_kernel");
+  return TROT_OK;
+}
+
+__global__ void status_merge_kernel(const int* __restrict__ src, int* __restrict__ dst) {
+  const int v = src[0];
+  if (v != 0) {
+    dst[0] = v;
+    dst[3] = v;
+  }
+}
+
+int launch_status_merge(const int* src, int* dst, cudaStream_t st) {
+  status_merge_kernel<<<1, 1, 0, st>>>(src, dst);
+  TROT_CHECK_LAUNCH("status_merge_kernel");
   return TROT_OK;
 }
 

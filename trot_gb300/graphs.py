@@ -56,7 +56,13 @@ class GraphedBlock:
             self._energy = obs.scalars["energy"]
             self._weight = obs.scalars["weight"]
 
-    def replay(self) -> dict:
-        """Run one block; returns its device scalars {"energy", "weight"}."""
+    def replay(self, check: bool = False) -> dict:
+        """Run one block; returns its device scalars {"energy", "weight"}.  With
+        ``check`` the host waits for the block and raises TrotError(DEVICE_TIMEOUT)
+        if a tensor-core kernel of it timed out (its results are NaN then)."""
         self.graph.replay()
+        if check:
+            from . import native
+
+            native.check_device_timeouts("graphed block")
         return {"energy": self._energy, "weight": self._weight}

@@ -86,6 +86,8 @@ def force_bias_batched(walkers, ham_data, meas_ctx, trial_data, walker_kind, pre
     ws, nws = native.ws_for(s, _lib.OP_FORCE_BIAS)
     _lib.call("trot_force_bias", ctypes.byref(s), native.ptr(wa), native.ptr(wb), out.data_ptr(), ws, nws,
               native.stream_ptr())
+    if precision == _lib.MIXED:
+        native.raise_on_timeout(ws, "force bias")
     return out
 
 
@@ -103,6 +105,9 @@ def local_energy_batched(walkers, ham_data, meas_ctx, trial_data, walker_kind, p
     ws, nws = native.ws_for(s, _lib.OP_LOCAL_ENERGY)
     _lib.call("trot_local_energy", ctypes.byref(s), native.ptr(wa), native.ptr(wb), out.data_ptr(), ws, nws,
               native.stream_ptr())
+    if precision == _lib.MIXED:
+        # the sticky word also covers the asynchronous mixed steps issued before this call
+        native.raise_on_timeout(ws, "local energy")
     return out
 
 

@@ -2,10 +2,15 @@
 
 Built once per (trial, Hamiltonian, dt) on the host and kept on the device:
 
-* exact-slice BF16 copies of the half-rotated Cholesky vectors for the local
+* exact-digit FP16 copies of the half-rotated Cholesky vectors for the local
   energy / force bias: each row (g, i) over orbitals p is written as
-  sum_t 2^(e - 8(t+1)) q_t (t < 5) with integer slices |q_t| <= 255 and one
-  exponent per row, laid out as 128-row tiles of whole Cholesky vectors;
+  2^e (q_0 2^-9 + sum_{t=1..4} q_t 2^-(9 + 9 t)) with integer digits
+  |q_0| <= 512, |q_t| <= 256 (exact in FP16) and one exponent per row, laid
+  out as 128-row tiles of whole Cholesky vectors; a row whose top digits sum
+  (in absolute value) past 2^15 gets its exponent raised by one, which keeps
+  every partial sum of the two leading digit-product groups below 2^24 (exact
+  in the tensor core's FP32 accumulator) against Green's-function digits with
+  |q_0| <= 256, |q_t| <= 256;
 * a 3-term BF16 split (hi + mid + lo) of the Cholesky vectors, transposed to
   (N*N, G) and stored as the VHS kernel's shared-memory image (128 x 64
   tiles in core-matrix order);
@@ -29,21 +34,35 @@ MAX_ORDER = 4
 KPAD = 128
 VHS_SLICES = 3
 VHS_ORDER = 2
+# digit format of the exact product (trot_mixed.digit_format): FP16 digits, Cholesky
+# rows with a 9-bit leading digit, Green's-function rows (made on the device) with an
+# 8-bit leading digit, 9-bit lower digits for both
+DIGIT_FORMAT = 1
+ROT_TOP_BITS = 9
+GREEN_TOP_BITS = 8
+LOW_BITS = 9
+ROT_L1_CAP = 2 ** 15
 
 
-def exact_slices(x: np.ndarray, slices: int = SLICES, bits: int = 8):
-    """Fixed-point slices of the rows (last axis) of ``x``: returns
-    (q (slices, ...) float32 integers in [-255, 255], e int32 row exponents)
-    with x ~= sum_t q_t 2^(e - bits (t+1))."""
+def digit_slices(x: np.ndarray, slices: int = SLICES, top: int = ROT_TOP_BITS, low: int = LOW_BITS,
+                 l1_cap: float | None = ROT_L1_CAP):
+    """Exact integer digits of the rows (last axis) of ``x``: returns (q (slices,
+    ...) float32 integers, e int32 row exponents) with
+    x ~= 2^e sum_t q_t 2^-(top + low t), |q_0| <= 2^top and balanced lower digits
+    |q_t| <= 2^(low - 1); the representation error is at most 2^(e - top - low
+    (slices - 1) - 1) per element.  e is the smallest integer with max |x| <= 2^e,
+    raised by one for rows whose sum of |q_0| would exceed ``l1_cap``."""
     x = np.asarray(x, dtype=np.float64)
     mx = np.max(np.abs(x), axis=-1)
     e = np.where(mx > 0, np.ceil(np.log2(np.where(mx > 0, mx, 1.0))), 0.0).astype(np.int32)
+    if l1_cap is not None:
+        q0 = np.rint(x / np.ldexp(1.0, e - top)[..., None])
+        e = e + (np.sum(np.abs(q0), axis=-1) > l1_cap).astype(np.int32)
     r = x.copy()
     out = []
-    lim = float(2 ** bits - 1)
     for t in range(slices):
-        sc = np.ldexp(1.0, e - bits * (t + 1))[..., None]
-        q = np.clip(np.rint(r / sc), -lim, lim)
+        sc = np.ldexp(1.0, e - top - low * t)[..., None]
+        q = np.rint(r / sc)
         out.append(q.astype(np.float32))
         r = r - q * sc
     return np.stack(out), e
@@ -105,7 +124,7 @@ def gammas_per_block(n: int) -> int:
 
 
 def rot_tiles(rot_chol: np.ndarray):
-    """(G, n, N) -> bf16 slices in the kernel's shared-memory image layout
+    """(G, n, N) -> FP16 digits in the kernel's shared-memory image layout
     (nblk, SLICES, 128, KPAD) (each 128 x KPAD tile in 8 x 8 core-matrix order,
     K fastest) and row exponents (nblk, 128)."""
     G, n, N = rot_chol.shape
@@ -118,11 +137,11 @@ def rot_tiles(rot_chol: np.ndarray):
         g0, g1 = blk * gb, min(G, (blk + 1) * gb)
         r = rot_chol[g0:g1].reshape(-1, N)
         rows[blk, : r.shape[0], :N] = r
-    q, e = exact_slices(rows)  # (SLICES, nblk, 128, KPAD)
+    q, e = digit_slices(rows)  # (SLICES, nblk, 128, KPAD)
     # shared-memory image of the exchange kernel's A operand: [nblk][slice][core-matrix order]
     img = q.transpose(1, 0, 2, 3).reshape(nblk, SLICES, 16, 8, KPAD // 8, 8).transpose(0, 1, 2, 4, 3, 5)
     img = np.ascontiguousarray(img).reshape(nblk, SLICES, 128, KPAD)
-    return torch.from_numpy(img).to(torch.bfloat16), torch.from_numpy(e.astype(np.int32)), gb, nblk
+    return torch.from_numpy(img.astype(np.float16)), torch.from_numpy(e.astype(np.int32)), gb, nblk
 
 
 class MixedCtx:
@@ -132,6 +151,7 @@ class MixedCtx:
         dev = device()
         s = _lib.TrotMixed()
         s.slices, s.max_order, s.kpad = SLICES, MAX_ORDER, KPAD
+        s.digit_format = DIGIT_FORMAT
         self._keep = []
         for k, rc in enumerate((rot_a, rot_b)):
             if rc is None:

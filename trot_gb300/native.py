@@ -22,14 +22,47 @@ def ptr(t) -> int:
 def workspace(nbytes: int) -> torch.Tensor:
     """A cached uint8 device buffer of at least ``nbytes``, one per (device,
     stream): calls on one stream are ordered and may share it, calls running
-    concurrently on different streams (fragment batches) get their own."""
+    concurrently on different streams (fragment batches) get their own.  The
+    256-byte status block at the start of a new buffer is zero-filled, so its
+    sticky timeout word starts clear (a buffer replaced by a larger one starts
+    a new record)."""
     dev = torch.cuda.current_device()
     key = (dev, torch.cuda.current_stream().cuda_stream)
     buf = _workspaces.get(key)
     if buf is None or buf.numel() < nbytes:
-        buf = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=f"cuda:{dev}")
+        buf = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=f"cuda:{dev}")
+        buf[:256].zero_()
         _workspaces[key] = buf
     return buf
+
+
+def capturing() -> bool:
+    return torch.cuda.is_current_stream_capturing()
+
+
+def raise_on_timeout(ws_ptr: int, what: str) -> None:
+    """Read (and clear) the sticky timeout word of the workspace at ``ws_ptr``
+    after the work queued on the current stream; raise TrotError(DEVICE_TIMEOUT)
+    if a tensor-core kernel of any call that used it since the last check had
+    a bounded wait run out (those calls wrote NaN results).  Synchronises the
+    stream; a no-op under CUDA graph capture."""
+    if capturing():
+        return
+    torch.cuda.current_stream().synchronize()
+    st = ctypes.c_int(0)
+    _lib.call("trot_workspace_timeouts", ws_ptr, 1, ctypes.addressof(st))
+    if st.value != _lib.OK:
+        raise _lib.TrotError(st.value, f"{what}: a tensor-core kernel's bounded wait ran out; its results are NaN")
+
+
+def check_device_timeouts(what: str = "trot_gb300") -> None:
+    """raise_on_timeout for every cached workspace of the current device (one
+    check per block or per graph replay covers all the asynchronous steps
+    before it)."""
+    dev = torch.cuda.current_device()
+    for (d, _), buf in list(_workspaces.items()):
+        if d == dev:
+            raise_on_timeout(buf.data_ptr(), what)
 
 
 def kind_of(trial, walker_kind: str) -> int:
