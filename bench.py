@@ -273,6 +273,30 @@ def perturbed_trial_walkers(wl, noise, seed=21):
     return wa, torch.as_tensor(synthetic.perturbed_walkers(wl["ss"].mo_b, W, noise, seed + 1)).cuda()
 
 
+def fp64_self_noise(wl, m64, mc64, walkers, d, e64, emx, k=4, seed=3):
+    """For the k walkers with the largest mixed-vs-FP64 difference: a second FP64
+    evaluation of E_L on w U (U a random unitary per spin and walker; E_L is
+    invariant under w -> w A for any invertible A), whose difference from the
+    first estimates FP64's own rounding noise on that walker, plus its weight."""
+    import torch
+
+    idx = torch.argsort(d, descending=True)[:k]
+    g = torch.Generator().manual_seed(seed)
+
+    def rot(w):
+        n = w.shape[2]
+        z = torch.randn((len(idx), n, n), generator=g, dtype=torch.complex128)
+        q, _ = torch.linalg.qr(z)
+        return torch.matmul(w[idx], q.to(w.device)).contiguous()
+
+    wsub = tuple(rot(w) for w in walkers) if isinstance(walkers, tuple) else rot(walkers)
+    e64u = m64.kernels["energy"](wsub, wl["ham"], mc64, wl["trial"])
+    wts = wl["state"].weights
+    return [{"abs_dE_L_Ha": float(d[i]), "abs_E_L_Ha": float(e64[i].abs()),
+             "fp64_self_noise_Ha": float((e64u[j] - e64[i]).abs()), "weight": float(wts[i])}
+            for j, i in enumerate(idx.tolist())]
+
+
 def max_over_ranks(x: float, world: int, device="cuda") -> float:
     """Largest value of ``x`` over the ranks of the process group (the job's
     time is its slowest replica's); ``x`` itself when running alone."""
@@ -386,6 +410,127 @@ def adjoint_leg(chol_scale=0.1, seed=11, n_steps=None):
             "fd_lambda": eps}
 
 
+def _block_energy_host(e, weights, e_ref, dt):
+    """Block energy of trot/prop/blocks.py:236-251 on host arrays: non-finite or
+    outlying (|E - e_ref| > sqrt(2/dt)) energies replaced by e_ref, non-finite
+    walkers' weights zeroed, weighted mean (e_ref when the weights sum to 0)."""
+    e = np.real(e)
+    with np.errstate(invalid="ignore"):
+        bad = ~np.isfinite(e)
+        e = np.where(bad | (np.abs(e - e_ref) > np.sqrt(2.0 / dt)), e_ref, e)
+    w = np.where(bad, 0.0, weights)
+    ws = float(np.sum(w))
+    return e_ref if ws == 0 else float(np.sum(w * e) / ws)
+
+
+def precision_leg(chol_scale=0.1, n_steps=200, seed=5):
+    """Mixed vs FP64 along whole trajectories on the headline workload's shapes
+    (UHF N=120 (12,10) G=600 W=1024 dt=0.005, QR + block tail every 10 steps):
+    the mixed run, and an FP64 run, from the same initial walkers with identical
+    fields (seeded on the device per step) and identical SR zeta per block.
+    Reports per-walker |dE_L| between the mixed and the FP64 local energy of the
+    mixed run's walkers at every step (identical walkers), the block energies of
+    the mixed run computed from mixed and from FP64 local energies of the same
+    walkers and weights (clamp of trot/prop/blocks.py:236-251), and the block
+    energies of the independent FP64 run.  The Cholesky vectors of the recipe are
+    scaled by ``chol_scale``: unscaled, every walker weight hits the floor / cap
+    within a few steps (block energies would be the clamp value); at x0.1 the
+    population stays alive for the whole run."""
+    import torch
+
+    import trot_gb300 as tg
+    from trot_gb300 import _lib, native, synthetic
+
+    cfg = synthetic.CONFIGS["cfg2_uhf_n120"]
+    N, (na, nb), G, W, dt, qr = (cfg["norb"], cfg["nelec"], cfg["nchol"], cfg["n_walkers"], cfg["dt"],
+                                 cfg["qr_every"])
+    h0, h1, chol = synthetic.hamiltonian(N, G, cfg["decay"], 0, 0.0)
+    chol = chol * chol_scale
+    ca, cb = synthetic.scf(h1, chol, na, nb, 30)
+    sysm = tg.System(norb=N, nelec=(na, nb), walker_kind="unrestricted")
+    ham = tg.HamChol(h0=h0, h1=h1, chol=chol)
+    trial = tg.UhfTrial(ca, cb)
+    params = tg.QmcParams(dt=dt, n_walkers=W, n_prop_steps=qr, seed=1234)
+    trial_ops = tg.make_uhf_trial_ops(sysm)
+
+    def setup(mixed):
+        meas = tg.make_uhf_meas_ops(sysm, mixed_precision=mixed)
+        mctx = meas.build_meas_ctx(ham, trial)
+        pops = tg.make_prop_ops("restricted", "unrestricted", mixed_precision=mixed)
+        pctx = pops.build_prop_ctx(ham, trial_ops.get_rdm1(trial), params)
+        st = pops.init_prop_state(sys=sysm, ham_data=ham, trial_ops=trial_ops, trial_data=trial, meas_ops=meas,
+                                  params=params)
+        return dict(meas=meas, mctx=mctx, pops=pops, pctx=pctx, st=st)
+
+    runs = {"mixed": setup(True), "fp64": setup(False)}
+    obs = torch.empty(2, dtype=torch.float64, device="cuda")
+    gen = torch.Generator(device="cuda")
+    zetas = np.random.default_rng(seed).uniform(size=n_steps // qr)
+    e_mx = torch.empty(W, dtype=torch.complex128, device="cuda")
+    d_steps, e_abs = [], []
+    blk = {"mixed_from_mixed_E": [], "mixed_from_fp64_E": [], "fp64_run": []}
+    t0 = time.perf_counter()
+    for b in range(n_steps // qr):
+        for k in range(qr):
+            gen.manual_seed(seed * 1000003 + b * qr + k)
+            x = torch.randn((W, G), generator=gen, dtype=torch.float64, device="cuda")
+            r = runs["mixed"]
+            e64 = runs["fp64"]["meas"].kernels["energy"](r["st"].walkers, ham, runs["fp64"]["mctx"], trial)
+            r["st"] = r["pops"].step(r["st"], params=params, ham_data=ham, trial_data=trial, trial_ops=trial_ops,
+                                     meas_ops=r["meas"], meas_ctx=r["mctx"], prop_ctx=r["pctx"], fields=x,
+                                     energy_out=e_mx)
+            d_steps.append((e_mx - e64).abs().cpu().numpy())
+            e_abs.append(e64.abs().cpu().numpy())
+            f = runs["fp64"]
+            f["st"] = f["pops"].step(f["st"], params=params, ham_data=ham, trial_data=trial, trial_ops=trial_ops,
+                                     meas_ops=f["meas"], meas_ctx=f["mctx"], prop_ctx=f["pctx"], fields=x)
+        for name, r in runs.items():
+            st = r["st"]
+            walkers = tg.walkers.orthonormalize_(st.walkers, "unrestricted")
+            e = r["meas"].kernels["energy"](walkers, ham, r["mctx"], trial)
+            e_ref = float(st.e_estimate)
+            wts = st.weights.cpu().numpy()
+            if name == "mixed":
+                e_other = runs["fp64"]["meas"].kernels["energy"](walkers, ham, runs["fp64"]["mctx"], trial)
+                blk["mixed_from_mixed_E"].append(_block_energy_host(e.cpu().numpy(), wts, e_ref, dt))
+                blk["mixed_from_fp64_E"].append(_block_energy_host(e_other.cpu().numpy(), wts, e_ref, dt))
+            _lib.call("trot_block_energy", W, e.data_ptr(), st.weights.data_ptr(), st.scalars.data_ptr(), float(dt),
+                      float(params.shift_ema), obs.data_ptr(), native.stream_ptr())
+            if name == "fp64":
+                blk["fp64_run"].append(float(obs[0]))
+            w_sr, wts_sr = tg.walkers.stochastic_reconfiguration(walkers, st.weights, float(zetas[b]),
+                                                                 "unrestricted")
+            r["st"] = st._replace(walkers=w_sr, weights=wts_sr, overlaps=r["meas"].overlap(w_sr, trial))
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    d = np.concatenate(d_steps)
+    ea = np.concatenate(e_abs)
+    bm, bf, b64 = (np.array(blk[k]) for k in ("mixed_from_mixed_E", "mixed_from_fp64_E", "fp64_run"))
+    wm = runs["mixed"]["st"].walkers[0].cpu().numpy()
+    wf = runs["fp64"]["st"].walkers[0].cpu().numpy()
+    return {
+        "workload": f"uhf_u N={N} nelec=({na},{nb}) G={G} W={W} dt={dt}, {n_steps} steps, QR + block tail every "
+                    f"{qr}, Cholesky x{chol_scale}, identical device-seeded fields and SR zeta in both runs",
+        "per_walker_identical_walkers": {"max_abs_dE_L_Ha": float(np.nanmax(d)),
+                                         "p99_abs_dE_L_Ha": float(np.nanquantile(d, 0.99)),
+                                         "median_abs_dE_L_Ha": float(np.nanmedian(d)),
+                                         "max_abs_E_L_Ha": float(np.nanmax(ea)), "samples": int(d.size),
+                                         "on": "every step, the mixed run's incoming walkers: mixed E_L (from the "
+                                               "step) vs the FP64 E_L kernel"},
+        "block_energy_diff_mHa": 1e3 * abs(float(np.mean(bm)) - float(np.mean(bf))),
+        "max_block_energy_diff_mHa": 1e3 * float(np.max(np.abs(bm - bf))),
+        "block_energy_note": "block energies of the mixed run from mixed vs FP64 local energies of the same "
+                             "walkers and weights, averaged over the blocks",
+        "block_average_mixed_Ha": float(np.mean(bm)),
+        "fp64_run_block_average_Ha": float(np.mean(b64)),
+        "fp64_run_block_energy_diff_mHa": 1e3 * abs(float(np.mean(bm)) - float(np.mean(b64))),
+        "fp64_run_max_block_energy_diff_mHa": 1e3 * float(np.max(np.abs(bm - b64))),
+        "fp64_run_final_walker_rel_diff": float(np.max(np.abs(wm - wf)) / max(np.max(np.abs(wf)), 1e-300)),
+        "alive_walkers_end": int((runs["mixed"]["st"].weights > 0).sum().item()),
+        "seconds": secs,
+    }
+
+
 def cpu_cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -409,6 +554,10 @@ def main():
                     help="run only the config-3 energy-gradient leg and print its JSON (for profiling)")
     ap.add_argument("--adjoint-steps", type=int, default=0,
                     help="steps of the energy-gradient leg (default: the config's 200)")
+    ap.add_argument("--no-precision-leg", action="store_true",
+                    help="skip the 200-step mixed-vs-FP64 trajectory comparison")
+    ap.add_argument("--precision-only", action="store_true",
+                    help="run only the mixed-vs-FP64 trajectory comparison and print its JSON")
     ap.add_argument("--profile-run", action="store_true",
                     help="timed steps only (no e2e, FP64 comparison, precision check or CPU baseline): "
                          "for profiler launch lists")
@@ -462,6 +611,10 @@ def main():
     if args.adjoint_only:
         if rank == 0:
             print(json.dumps({"adjoint": adjoint_leg(n_steps=args.adjoint_steps)}), flush=True)
+        return
+    if args.precision_only:
+        if rank == 0:
+            print(json.dumps({"precision_trajectory": precision_leg()}), flush=True)
         return
     wl = build_workload(cfg, args.precision)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
@@ -532,9 +685,21 @@ def main():
         e64 = m64.kernels["energy"](st.walkers, wl["ham"], mc64, wl["trial"])
         emx = wl["meas_ops"].kernels["energy"](st.walkers, wl["ham"], wl["meas_ctx"], wl["trial"])
         d = (emx - e64).abs()
-        precision_info = {"max_abs_dE_L_Ha": float(d.max()), "median_abs_dE_L_Ha": float(d.median()),
-                          "max_abs_E_L_Ha": float(e64.abs().max()), "walkers": W,
-                          "on": "the benchmark's walkers after warm-up + timed + e2e steps (identical walkers)"}
+        live = st.weights > 0
+        dl = d[live]
+        precision_info = {
+            "max_abs_dE_L_Ha": float(dl.max()) if dl.numel() else 0.0,
+            "median_abs_dE_L_Ha": float(dl.median()) if dl.numel() else 0.0,
+            "max_abs_E_L_Ha": float(e64[live].abs().max()) if dl.numel() else 0.0,
+            "walkers": int(dl.numel()),
+            "on": "the benchmark's live walkers (weight > 0) after warm-up + timed + e2e steps, identical "
+                  "walkers; walkers of weight 0 enter no estimator and SR never selects them",
+            "all_walkers": {"max_abs_dE_L_Ha": float(d.max()), "median_abs_dE_L_Ha": float(d.median()),
+                            "max_abs_E_L_Ha": float(e64.abs().max()), "walkers": W,
+                            "above_1e-5": int((d > 1e-5).sum())},
+        }
+        if wl["kind"] != "cisd":
+            precision_info["all_walkers"]["worst"] = fp64_self_noise(wl, m64, mc64, st.walkers, d, e64, emx)
         # the seeded recipe's population decays within a few steps (|E_L| up to ~1e6 Ha), so the
         # same comparison is also made on walkers near the trial, where E_L is physical
         near = {}
@@ -613,6 +778,9 @@ def main():
         line["speedup_vs_fp64"] = value / fp64["value"]
     if precision_info is not None:
         line["precision_check"] = precision_info
+    if args.precision == "mixed" and not args.no_precision_leg and rank == 0 and world == 1 \
+            and args.config == "cfg2_uhf_n120":
+        line["precision_trajectory"] = precision_leg()
     if not args.no_adjoint and rank == 0 and world == 1:
         line["adjoint"] = adjoint_leg(n_steps=args.adjoint_steps)
     if not args.no_cpu_baseline:
