@@ -61,11 +61,12 @@ def test_rot_tiles_layout():
     G, n, N = 25, 12, 120
     rc = rng.normal(size=(G, n, N))
     img, e, gb, nblk = mixed.rot_tiles(rc)
+    ks = mixed.KPAD // 16
     assert gb == 10 and nblk == 3
-    assert tuple(img.shape) == (nblk, mixed.SLICES, 128, mixed.KPAD)
-    # undo the core-matrix order: index (rg, kg, ri, ki) -> (row 8 rg + ri, k 8 kg + ki)
-    im = img.to(torch.float64).numpy().reshape(nblk, mixed.SLICES, 16, 16, 8, 8)
-    qd = im.transpose(1, 0, 2, 4, 3, 5).reshape(mixed.SLICES, nblk, 128, mixed.KPAD)
+    assert tuple(img.shape) == (nblk, ks, mixed.SLICES, 128, 16)
+    # undo the core-matrix order: (blk, kstep, plane, rg, kg, ri, ki) -> (plane, blk, row 8 rg + ri, k 16 kstep + 8 kg + ki)
+    im = img.to(torch.float64).numpy().reshape(nblk, ks, mixed.SLICES, 16, 2, 8, 8)
+    qd = im.transpose(2, 0, 3, 5, 1, 4, 6).reshape(mixed.SLICES, nblk, 128, mixed.KPAD)
     # row (g=13, i=4) lives in block 1, row 3*12+4, orbitals 0..N-1; padding is zero
     sh = [mixed.ROT_TOP_BITS + mixed.LOW_BITS * t for t in range(mixed.SLICES)]
     rec = sum(qd[t, 1, 3 * n + 4, :N] * np.ldexp(1.0, int(e[1, 3 * n + 4]) - sh[t]) for t in range(mixed.SLICES))
@@ -73,6 +74,11 @@ def test_rot_tiles_layout():
     assert img.dtype == torch.float16
     assert np.all(qd[:, :, :, N:] == 0)
     assert np.all(qd[:, 2, 5 * n:, :] == 0)  # last block holds 5 vectors
+    # byte offset of element (row 8 rg + ri, k 8 kg + ki) inside a (kstep, plane) block
+    flat = img.numpy().reshape(nblk, ks, mixed.SLICES, 128 * 16)
+    r, k = 77, 13
+    off = (r >> 3) * 128 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7)
+    assert flat[1, 2, 3, off] == np.float16(qd[3, 1, r, 2 * 16 + k])
 
 
 @pytest.mark.parametrize("kchunk", [32, 64])

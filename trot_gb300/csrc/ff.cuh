@@ -97,4 +97,26 @@ TROT_D float d2f_bits(double x) {
   return __int_as_float((int)(sign | (((unsigned)ef << 23) + (unsigned)(r >> 29))));
 }
 
+
+// ---------------------------------------------------------------- fixed-point sums
+// Integer sums are associative, so fixed-point reductions give the same bits in any
+// order.  x 2^s rounded to the nearest int64 (the caller keeps |x 2^s| below 2^62);
+// s is split into two float scalings so each factor stays a normal float.
+TROT_D long long ff_to_fixed(ff x, int s) {
+  const int s1 = max(-126, min(127, s >> 1)), s2 = max(-126, min(127, s - (s >> 1)));
+  const float f1 = pow2f(s1), f2 = pow2f(s2);
+  return __float2ll_rn(__fmul_rn(__fmul_rn(x.hi, f1), f2)) + __float2ll_rn(__fmul_rn(__fmul_rn(x.lo, f1), f2));
+}
+// Sum of an int64 over the 32 lanes of a warp (|v| < 2^57 per lane): three 21-bit
+// chunks, each summed exactly by redux.sync.
+TROT_D long long warp_sum_i64(long long v) {
+  const int hi = (int)(v >> 42);
+  const unsigned mid = (unsigned)((v >> 21) & 0x1FFFFF), lo = (unsigned)(v & 0x1FFFFF);
+  const int shi = __reduce_add_sync(0xffffffffu, hi);
+  const unsigned smid = __reduce_add_sync(0xffffffffu, mid), slo = __reduce_add_sync(0xffffffffu, lo);
+  return ((long long)shi << 42) + ((long long)smid << 21) + (long long)slo;
+}
+// 2^e as a double for e in [-1022, 1023]
+TROT_D double pow2d(int e) { return __longlong_as_double((long long)(1023 + e) << 52); }
+
 }  // namespace trot

@@ -124,42 +124,46 @@ static int launch_green_ff(const Spins& sp, int W, int N, const double2* wa, con
 // ------------------------------------------------------------------ layouts
 static constexpr size_t kTcImgBytes = 3 * 128 * 256 * 2;  // [Vr | Vi] operand image of one walker (192 KB)
 static constexpr int kKP = 128;       // padded orbital dimension of the exact product
-static constexpr int kBN = 96;        // MMA N of the exchange tile (columns = walker rows)
-static constexpr int kKH = 64;        // K per half-slice of the Green's-function operand (ring unit)
+static constexpr int kKS = kKP / 16;  // K16 steps of the exact product
 static constexpr int kGroups = 5;     // accumulators for t + u = 0..4
 static constexpr int kSlices = 5;
-static constexpr int kSlots = 2;      // ring of Green's-function slice buffers
-static constexpr int kMaxOcc = 16;    // largest n the epilogue handles (2 * n_pad <= 32 columns per walker)
-// FP16 digit format of the exact product (trot_mixed.digit_format 1): Cholesky rows
+static constexpr int kMaxOcc = 16;    // largest n the exchange epilogue handles
+// FP16 digit format of the exact product (trot_mixed.digit_format 2): Cholesky rows
 // 2^eA sum_t qA_t 2^-(9 + 9t), Green's-function rows 2^eB sum_u qB_u 2^-(8 + 9u);
-// digit products of order d = t + u carry 2^(eA + eB - 17 - 9d)
-static constexpr int kDigitFormat = 1;
+// digit products of order d = t + u carry 2^(eA + eB - 17 - 9d).  Both operands are
+// stored per K16 step: [plane][rows][16] blocks in core-matrix order (see tile16_idx).
+static constexpr int kDigitFormat = 2;
 static constexpr int kRotTopBits = 9, kGreenTopBits = 8, kLowBits = 9;
 static constexpr int kGreenBits = kGreenTopBits + kLowBits * (kSlices - 1);  // 44 fixed-point bits per row
-static constexpr uint32_t kAImg = (uint32_t)kSlices * 128 * kKP * 2;  // 163840 B: 5 rot slices of a tile
-static constexpr uint32_t kBImg = (uint32_t)kBN * kKH * 2;            // 12288 B: one K-half of a green slice
+static constexpr uint32_t kAStep = (uint32_t)kSlices * 128 * 16 * 2;  // 20480 B: the 5 rot planes of one K16 step
+static constexpr uint32_t kAImg = (uint32_t)kKS * kAStep;             // 163840 B: a whole 128-row Cholesky tile
 
-// Row-major [rows x 128] bf16 tile -> core-matrix order (8 x 8 blocks, K fastest):
-// element (r, k) at 16-bit index (r/8)*1024 + (k/8)*64 + (r%8)*8 + k%8.
-TROT_HD uint32_t img_idx(int r, int k) {
-  return (uint32_t)((r >> 3) * 1024 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7));
+// Element (r, k) of a [rows x 16] K-major block in core-matrix order (8 rows x 8 K per
+// 128-byte core matrix; core matrices 128 B apart along K, 256 B apart along rows):
+// 16-bit index (r/8)*128 + (k/8)*64 + (r%8)*8 + k%8.  Descriptor LBO 128 B, SBO 256 B.
+TROT_HD uint32_t tile16_idx(int r, int k) {
+  return (uint32_t)((r >> 3) * 128 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7));
 }
-// Same for a [rows x 64] tile: element (r, k) at (r/8)*512 + (k/8)*64 + (r%8)*8 + k%8.
-TROT_HD uint32_t img_idx64(int r, int k) {
-  return (uint32_t)((r >> 3) * 512 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7));
-}
+
+// Walker tiles of the exchange product: the Green's-function rows (walker b, j, c) of
+// P = WBT * 2 n_pad columns; the five digit planes of a tile are stacked along the MMA's
+// N dimension (planes 0..4-t in one MMA with rot plane t), so P <= 51 and 2 x 5P TMEM
+// columns (double-buffered accumulators) fit the 512 columns.
+TROT_HD int ex_npad(int n) { return n <= 4 ? 4 : n <= 8 ? 8 : n <= 12 ? 12 : 16; }
+TROT_HD int ex_cols(int n_pad) { return n_pad == 16 ? 32 : 48; }
 
 struct SpinLayout {
-  int n, n_pad, S, WB, ntiles;  // rows per walker S = 2 n_pad, walkers per tile WB, walker tiles
+  int n, n_pad, S, P, WB, ntiles;  // columns per walker S = 2 n_pad, per tile P = WB S; walker tiles
   int gb, nblk, blk_off;        // Cholesky vectors per 128-row tile, tiles, offset in the partial array
 };
 
 static SpinLayout spin_layout(const trot_system* s, const Spins& sp, int q) {
   SpinLayout L{};
   L.n = sp.n[q];
-  L.n_pad = (L.n + 3) & ~3;  // 4 column quarters per walker in the exchange epilogue
+  L.n_pad = ex_npad(L.n);
   L.S = 2 * L.n_pad;
-  L.WB = kBN / L.S;
+  L.P = ex_cols(L.n_pad);
+  L.WB = L.P / L.S;
   L.ntiles = (s->n_walkers + L.WB - 1) / L.WB;
   const int mq = (s->kind == TROT_UHF_U) ? q : 0;
   L.gb = s->mixed->gammas_per_block[mq];
@@ -171,8 +175,8 @@ static SpinLayout spin_layout(const trot_system* s, const Spins& sp, int q) {
 struct MixedBuffers {
   double2* green;
   double2* e1;
-  uint16_t* gq[2];   // per spin: [tile][slice][kBN rows][kKP] in core-matrix order
-  int32_t* ge[2];    // per spin: [tile][kBN] row exponents
+  uint16_t* gq[2];   // per spin: [tile][K16 step][5 planes x P rows][16] in core-matrix order
+  int32_t* ge[2];    // per spin: [tile][P] row exponents
   double2* cs[2];
   double2* xpart;
   double2* fb;
@@ -200,8 +204,8 @@ static size_t carve_mixed(const trot_system* s, const Spins& sp, Carver& c, Mixe
     m.nblk_total = 0;
     for (int q = 0; q < sp.nspin; ++q) {
       SpinLayout L = spin_layout(s, sp, q);
-      m.gq[q] = c.take<uint16_t>((size_t)L.ntiles * kSlices * kBN * kKP);
-      m.ge[q] = c.take<int32_t>((size_t)L.ntiles * kBN);
+      m.gq[q] = c.take<uint16_t>((size_t)L.ntiles * kKS * kSlices * L.P * 16);
+      m.ge[q] = c.take<int32_t>((size_t)L.ntiles * L.P);
       m.cs[q] = c.take<double2>(W * G);
       m.nblk_total += L.nblk;
     }
@@ -255,23 +259,25 @@ TROT_D long long rint_scaled(double x, int s) {
 }
 
 // ------------------------------------------------------------------ Green's function digits
-// Rows (b, spin, c in {re, im}, j) of the half Green's function over orbitals
-// p, as exact integer FP16 digits: v = round(x 2^(44 - e)) (|v| <= 2^44, e the
-// smallest integer with max |x| <= 2^e), an 8-bit leading digit q_0 = round(v /
-// 2^36) (|q_0| <= 256) and balanced 9-bit digits q_1..q_4 (|q| <= 256), so
-// x ~= 2^e sum_t q_t 2^-(8 + 9 t).  Written straight into the shared-memory image
-// of the exchange kernel's B operand: per walker tile, per digit, per K-half, kBN
-// rows (walker bl, row c*n_pad + j) x 64 orbitals in core-matrix order; padding
-// rows are zero.  One CTA per tile.
+// Rows (b, spin, j, c in {re, im}) of the half Green's function over orbitals p, as
+// exact integer FP16 digits: v = round(x 2^(44 - e)) (|v| <= 2^44, e the smallest
+// integer with max |x| <= 2^e), an 8-bit leading digit q_0 = round(v / 2^36) (|q_0| <=
+// 256) and balanced 9-bit digits q_1..q_4 (|q| <= 256), so x ~= 2^e sum_t q_t 2^-(8 +
+// 9 t).  Written straight into the exchange kernel's B operand image: per walker tile
+// (P columns: walker bl, j, c at bl*2*n_pad + 2 j + c), per K16 step, the 5 digit planes
+// stacked as 5P rows (plane u at rows u*P ..) of 16 orbitals in core-matrix order; padding
+// rows (j >= n, walkers past W) and orbitals p >= N are zero.  One CTA per tile.
 __global__ void __launch_bounds__(256)
-green_slices_kernel(int N, int n, int n_pad, int WB, int W, int ntot, int off, const double2* __restrict__ green,
-                    uint16_t* __restrict__ gq, int32_t* __restrict__ ge) {
+green_slices_kernel(int N, int n, int n_pad, int P, int WB, int W, int ntot, int off,
+                    const double2* __restrict__ green, uint16_t* __restrict__ gq, int32_t* __restrict__ ge) {
   const int tile = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int S = 2 * n_pad;
-  for (int row = warp; row < kBN; row += blockDim.x >> 5) {
+  const size_t unit = (size_t)kSlices * P * 16;  // 16-bit entries per K16 step of the tile
+  uint16_t* out = gq + (size_t)tile * kKS * unit;
+  for (int row = warp; row < P; row += blockDim.x >> 5) {
     const int bl = row / S, rr = row % S;
     const int b = tile * WB + bl;
-    const int c = rr / n_pad, j = rr % n_pad;
+    const int j = rr >> 1, c = rr & 1;
     const bool valid = bl < WB && b < W && j < n;
     const double* src = valid ? reinterpret_cast<const double*>(green + (size_t)b * ntot * N + (size_t)(off + j) * N)
                               : nullptr;
@@ -293,47 +299,56 @@ green_slices_kernel(int N, int n, int n_pad, int WB, int W, int ntot, int off, c
     const bool nonfinite = E == 0x7FF;  // the row's digits become NaN, so its products are NaN
     int e = 0;
     if (mx != 0 && !nonfinite) e = E == 0 ? -1022 : (E - 1023) + ((mx & 0xFFFFFFFFFFFFFull) != 0 ? 1 : 0);
-    if (lane == 0) ge[(size_t)tile * kBN + row] = e;
+    if (lane == 0) ge[(size_t)tile * P + row] = e;
 #pragma unroll
     for (int k = 0; k < kKP / 32; ++k) {
       const int p = lane + 32 * k;
       long long v = rint_scaled(x[k], kGreenBits - e);
+      uint16_t* dst = out + (size_t)(p >> 4) * unit;
 #pragma unroll
       for (int t = 0; t < kSlices; ++t) {
         const int sh = kLowBits * (kSlices - 1 - t);
         const long long d = sh > 0 ? ((v + (1ll << (sh - 1))) >> sh) : v;  // |d| <= 256 for every t
         v -= d << sh;
         const __half h = __int2half_rn((int)d);
-        gq[(((size_t)tile * kSlices + t) * 2 + (p >> 6)) * kBN * kKH + img_idx64(row, p & 63)] =
-            nonfinite ? (uint16_t)0x7E00u : __half_as_ushort(h);
+        dst[tile16_idx(t * P + row, p & 15)] = nonfinite ? (uint16_t)0x7E00u : __half_as_ushort(h);
       }
     }
   }
 }
 
 // ------------------------------------------------------------------ exact exchange / trace kernel
-// A persistent CTA walks work items = (tile of gb Cholesky vectors: 128 rows
-// (g, i), run of walker tiles: WB walkers x S rows = kBN = 96 MMA columns).
-// Warp 16 (one lane) is the producer: it bulk-copies the five FP16 rot_chol digit
-// planes of the item's Cholesky tile into shared memory, streams the Green's-function
-// digit planes of each walker tile as 64-wide K halves through a 2-slot ring, and
-// issues the FP16 MMAs: products q_t (rot) x q_u (green) with t + u = d accumulate
-// in TMEM group d (d = 0..4), exactly for d <= 1 (every partial sum stays below 2^24).  One accumulator buffer (5 x 96 columns):
-// the epilogue copies a tile's values out of TMEM into registers and releases it
-// at once, so the MMAs of the next tile overlap the epilogue's arithmetic.
-// Warps 0-15 are the epilogue (four warps per TMEM lane quadrant, each taking a
-// quarter of the columns j): they rebuild
-// f_g[i][j] = 2^(eA + eB - 17) sum_d 2^(-9 d) A_d in float-float and form, per
-// walker, the exchange sum_g sum_ij f_gij f_gji (trot/meas/rhf.py:33-60) and the
-// traces c_g = sum_i f_gii (Coulomb / force bias, trot/meas/rhf.py:119-125).
+// f_g = rot_chol_g G^T (n x n per Cholesky vector g and walker) from exact FP16 digit
+// products on tcgen05, then per walker the exchange sum_g sum_ij f_gij f_gji
+// (trot/meas/rhf.py:33-60) and the traces c_g = sum_i f_gii (Coulomb / force bias,
+// trot/meas/rhf.py:119-125).
+//
+// A persistent CTA walks work items = (Cholesky tile: gb vectors x n orbitals = up to
+// 128 MMA rows (g, i), run of walker tiles of P columns).  Warp 16 (one lane) is the
+// producer.  The rot_chol digits of the item's tile (5 planes x 128 rows x 128 orbitals)
+// stay in shared memory, loaded per K16 step (20 KB chunks; each chunk is refilled for the
+// next item as soon as the last MMAs that read it have completed, so items do not drain
+// the tensor pipe); the Green's-function digits of each walker tile stream through a ring
+// of K16 steps (5 planes x P rows each).  Per K16 step the producer issues five MMAs:
+// rot plane t against Green's-function planes 0..4-t stacked along N (N = (5 - t) P),
+// which accumulates product (t, u) into TMEM group t + u (columns (t + u) P of the tile's
+// accumulator buffer) - exactly for t + u <= 1, where every partial sum stays below 2^24.
+// Two accumulator buffers (5P columns each, at columns 0 and 256) let the MMAs of the next
+// tile run during the epilogue of this one.
+//
+// Warps 0-15 are the epilogue, one walker of the tile at a time: warp w reads TMEM lane
+// quadrant w % 4 (rows r = (g, i)) and the columns of orbitals j in [JH (w / 4), JH (w / 4
+// + 1)) of the walker, re and im; it rebuilds f_g[i][j] = 2^(eA + eB - 17) sum_d 2^(-9 d)
+// A_d in float-float, stages f in shared memory for the transposed products f_gji, and
+// reduces the exchange and the traces in fixed order.
 struct ExArgs {
   SpinLayout L;
   int G, W, mult;
-  int tiles_per_item, chunks, n_items;  // work item = (Cholesky block, run of walker tiles)
-  const uint16_t* rot_img;   // [nblk][slices][128][kKP] core-matrix order
+  int tiles_per_item, chunks, n_items;  // work item = (Cholesky tile, run of walker tiles)
+  const uint16_t* rot_img;   // [nblk][kKS][5][128][16] core-matrix order
   const int32_t* rot_e;      // [nblk][128]
-  const uint16_t* green_img; // [ntiles][slices][kBN][kKP]
-  const int32_t* green_e;    // [ntiles][kBN]
+  const uint16_t* green_img; // [ntiles][kKS][5 P][16] core-matrix order
+  const int32_t* green_e;    // [ntiles][P]
   double2* cs;
   double2* xpart;
   int nblk_total;
@@ -341,40 +356,82 @@ struct ExArgs {
   int test_timeout_polls;  // > 0: the producer's first wait is on a barrier nothing arrives on
 };
 
-static constexpr int kExThreads = 544;  // 16 epilogue warps + 1 producer warp
+static constexpr int kExThreads = 608;  // 16 epilogue warps, the MMA warp, the reducer warp, the loader warp
 static constexpr int kExEpi = 512;      // epilogue threads
-static constexpr size_t kExOffRing = kAImg;
-static constexpr int kFS = kMaxOcc + 1;  // row stride of the f staging arrays (padded against bank conflicts)
-static constexpr size_t kExOffF = kExOffRing + (size_t)kSlots * kBImg;        // re, im: [128][kFS] ff each
-static constexpr size_t kExOffEA = kExOffF + (size_t)2 * 128 * kFS * sizeof(ff);
-static constexpr size_t kExOffC = kExOffEA + 128 * 4;                          // [128][2] ff traces
-static constexpr size_t kExOffRed = kExOffC + 128 * 2 * sizeof(ff);            // [16 warps][2] ff
-static constexpr size_t kExOffBar = kExOffRed + 16 * 2 * sizeof(ff);           // 11 mbarriers + flags
-static constexpr size_t kExSmem = kExOffBar + 16 * 8 + 64;
+static constexpr int kExSync = 544;     // epilogue + reducer: the per-tile and per-walker barriers
+static constexpr int kExSlots = 5;      // ring of Green's-function K16 steps
 
-// JH = n_pad / 4 columns j per epilogue warp (static so the per-row values stay
-// in registers); columns j >= n are exactly zero and contribute nothing.
-template <int JH>
+// One epilogue warp's exchange sum of a walker: fixed-point values V[c] with scale 2^-s[c]
+// (s[c] = kExNonFinite: a lane's value was not finite).
+struct ExWarpSum {
+  long long v[2];
+  int s[2];
+  int pad[2];
+};
+
+static constexpr int kExNonFinite = -0x7fffffff;
+
+// Sum over the warp of float-float values as a fixed-point int64 with the warp's own scale:
+// returns V with sum ~= V 2^-s (|V| < 2^54), s = kExNonFinite if a lane is not finite.
+// Each lane's value x 2^s (|x 2^s| < 2^48) is split into three int32 parts summed exactly by
+// redux.sync; only FP32 / int32 conversions are used (64-bit conversions run on the FP64 pipe).
+TROT_D long long ex_warp_sum(ff x, int& s_out) {
+  const unsigned E = __reduce_max_sync(0xffffffffu, (__float_as_uint(x.hi) >> 23) & 0xFFu);
+  if (E == 0xFFu) {
+    s_out = kExNonFinite;
+    return 0;
+  }
+  const int s = 174 - (int)E;  // |x| < 2^(E - 126)
+  const float f1 = pow2f(max(-126, min(127, s >> 1))), f2 = pow2f(max(-126, min(127, s - (s >> 1))));
+  const float h = __fmul_rn(__fmul_rn(x.hi, f1), f2), l = __fmul_rn(__fmul_rn(x.lo, f1), f2);
+  const float hA = rintf(h * 5.9604644775390625e-08f);      // h / 2^24, |hA| <= 2^24
+  const int A = (int)hA;
+  const int B = __float2int_rn(__fmaf_rn(-hA, 16777216.f, h));  // h - hA 2^24 is exact, |B| <= 2^23
+  const int Lo = __float2int_rn(l);                             // |Lo| <= 2^25
+  const int SA = __reduce_add_sync(0xffffffffu, A), SB = __reduce_add_sync(0xffffffffu, B);
+  const int SL = __reduce_add_sync(0xffffffffu, Lo);
+  s_out = s;
+  return ((long long)SA << 24) + (long long)SB + (long long)SL;
+}
+
+template <int NP>
+struct ExShape {
+  static constexpr int P = NP == 16 ? 32 : 48;        // columns per digit plane (= ex_cols)
+  static constexpr int WBT = P / (2 * NP);            // walkers per tile
+  static constexpr int JH = NP / 4;                   // orbitals j per epilogue thread
+  static constexpr uint32_t UB = (uint32_t)kSlices * P * 32;  // one K16 step of a walker tile
+  static constexpr int FS = NP + 1;                   // staging row stride (padded against bank conflicts)
+  static constexpr int KPT = (NP / 2 + 4) / 4;        // exchange pair offsets k per epilogue thread
+  static constexpr size_t offRing = kAImg;
+  static constexpr size_t offF = offRing + (size_t)kExSlots * UB;              // re, im: [128][FS] ff each
+  static constexpr size_t offRed = offF + (size_t)2 * 128 * FS * sizeof(ff);   // [16 warps] per-warp exchange sums
+  static constexpr size_t offBar = offRed + (size_t)16 * 32;                    // 34 mbarriers / words
+  static constexpr size_t bytes = offBar + 40 * 8 + 1024;                      // + base alignment
+};
+
+template <int NP>
 __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a) {
+  using X = ExShape<NP>;
+  constexpr int P = X::P, WBT = X::WBT, JH = X::JH, FS = X::FS;
+  constexpr uint32_t UB = X::UB;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
   unsigned char* sA = base;
-  unsigned char* ring = base + kExOffRing;
-  ff* sF = reinterpret_cast<ff*>(base + kExOffF);
-  ff* sC = reinterpret_cast<ff*>(base + kExOffC);
-  ff* sRed = reinterpret_cast<ff*>(base + kExOffRed);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(base + kExOffBar);
-  uint64_t* a_full = bars;
-  uint64_t* full = bars + 1;        // [kSlots <= 3]
-  uint64_t* empty = bars + 4;       // [kSlots <= 3]
-  uint64_t* acc_full = bars + 7;    // the tile's accumulators are complete
-  uint64_t* acc_empty = bars + 8;   // the epilogue has copied them out of TMEM
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 11);
-  int* flag = reinterpret_cast<int*>(bars + 12);  // epilogue go/stop broadcast
-  uint64_t* a_free = bars + 13;     // the MMAs of the previous work item are done with sA
-  uint64_t* never = bars + 14;      // nothing arrives on it (the status-path test's wait)
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 9);  // producer gave up: epilogue stops
-  constexpr int WBT = 24 / (2 * JH);  // walkers per tile: kBN / (2 n_pad) with n_pad = 4 JH
+  unsigned char* ring = base + X::offRing;
+  ff* sF = reinterpret_cast<ff*>(base + X::offF);
+  ExWarpSum* sRed = reinterpret_cast<ExWarpSum*>(base + X::offRed);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + X::offBar);
+  static_assert(2 * kKS + 2 * kExSlots + 10 <= 40, "exchange kernel: barrier table");
+  uint64_t* a_full = bars;                         // [kKS] chunk k of the Cholesky tile has landed
+  uint64_t* a_free = bars + kKS;                   // [kKS] the MMAs reading chunk k of the item are done
+  uint64_t* full = bars + 2 * kKS;                 // [kExSlots]
+  uint64_t* empty = full + kExSlots;               // [kExSlots]
+  uint64_t* acc_full = empty + kExSlots;           // [2] a tile's accumulators are complete
+  uint64_t* acc_empty = acc_full + 2;              // [2] the epilogue has read them out of TMEM
+  uint64_t* never = acc_empty + 2;                 // nothing but the abort path's commit arrives on it
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(never + 1);
+  volatile int* flag = reinterpret_cast<volatile int*>(never + 2);        // epilogue go/stop broadcast
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(never + 3);  // a producer gave up: epilogue stops
 
   const SpinLayout& L = a.L;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -382,14 +439,18 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
 
   if (warp == 16) tc::tmem_alloc(tslot, 512);
   if (tid == kExEpi) {
-    tc::mbar_init(a_full, 1);
-    tc::mbar_init(a_free, 1);
-    for (int k = 0; k < kSlots; ++k) {
+    for (int k = 0; k < kKS; ++k) {
+      tc::mbar_init(&a_full[k], 1);
+      tc::mbar_init(&a_free[k], 1);
+    }
+    for (int k = 0; k < kExSlots; ++k) {
       tc::mbar_init(&full[k], 1);
       tc::mbar_init(&empty[k], 1);
     }
-    tc::mbar_init(acc_full, 1);
-    tc::mbar_init(acc_empty, 16);
+    for (int k = 0; k < 2; ++k) {
+      tc::mbar_init(&acc_full[k], 1);
+      tc::mbar_init(&acc_empty[k], 16);
+    }
     tc::mbar_init(never, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -400,225 +461,275 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
   const uint32_t taddr = *tslot;
 
   if (warp == 16) {
-    // ------------------------------------------------ producer: loads + MMAs (one lane)
+    // ------------------------------------------------ MMA issuer (one lane)
     if (lane == 0) {
       bool ok = true;
-      const uint32_t idesc = tc::idesc_f16_f32(128, kBN);
-      const uint32_t sA_u = tc::smem_u32(sA), ring_u = tc::smem_u32(ring);
-      const uint64_t ad0 = tc::smem_desc(sA_u, 128, kKP * 16);
-      const uint32_t adlo = (uint32_t)ad0, ahi = (uint32_t)(ad0 >> 32);
-      const uint64_t bd0 = tc::smem_desc(ring_u, 128, kKH * 16);
-      const uint32_t bhi = (uint32_t)(bd0 >> 32);
-      constexpr int kUnits = kSlices * 2;  // ring units per tile: (slice u, K-half h)
-      int g_issue = 0, g_base = 0, tg = 0, kitem = 0;  // CTA-wide unit / tile / item counters
+      uint32_t idesc[kSlices];
+#pragma unroll
+      for (int t = 0; t < kSlices; ++t) idesc[t] = tc::idesc_f16_f32(128, (kSlices - t) * P);
+      // both operands: LBO 128 B (K-adjacent core matrices), SBO 256 B (8-row groups), so the
+      // descriptors share their high word and only the start-address words advance
+      const uint64_t ad0 = tc::smem_desc(tc::smem_u32(sA), 128, 256);
+      const uint64_t bd0 = tc::smem_desc(tc::smem_u32(ring), 128, 256);
+      const uint32_t adlo = (uint32_t)ad0, bdlo = (uint32_t)bd0, dhi = (uint32_t)(ad0 >> 32);
+      int gs = 0, tg = 0, kitem = 0;  // CTA-wide unit / tile / item counters
       // status-path test (TROT_TUNE_TEST_TIMEOUT): a bounded wait on a barrier nothing
-      // arrives on runs out before any copy or MMA is issued
+      // arrives on runs out before any MMA is issued
       if (a.test_timeout_polls > 0) ok = tc::mbar_wait(never, 0u, (uint32_t)a.test_timeout_polls);
       for (int item = blockIdx.x; item < a.n_items && ok; item += gridDim.x, ++kitem) {
-        const int blk = item / a.chunks;
         const int t0 = (item % a.chunks) * a.tiles_per_item, t1 = min(L.ntiles, t0 + a.tiles_per_item);
-        const int ntl = t1 - t0, total = ntl * kUnits;
-        if (kitem > 0) ok = tc::mbar_wait(a_free, (uint32_t)((kitem - 1) & 1));
-        if (!ok) break;
-        tc::mbar_expect_tx(a_full, kAImg);
-        tc::bulk_g2s(sA, a.rot_img + (size_t)blk * (kAImg / 2), kAImg, a_full);
-        for (int sidx = 0; sidx < total && ok; ++sidx) {
-          const int i = sidx / kUnits, uh = sidx % kUnits, u = uh >> 1, h = uh & 1;
-          // keep up to kSlots ring units of this item in flight ahead of the MMAs
-          while (g_issue < g_base + total && g_issue < g_base + sidx + kSlots && ok) {
-            const int slot = g_issue % kSlots;
-            if (g_issue >= kSlots) ok = tc::mbar_wait(&empty[slot], (uint32_t)((g_issue / kSlots - 1) & 1));
-            if (!ok) break;
-            const int li = g_issue - g_base;
-            const int ti = t0 + li / kUnits, tuh = li % kUnits;
-            tc::mbar_expect_tx(&full[slot], kBImg);
-            tc::bulk_g2s(ring + (size_t)slot * kBImg, a.green_img + ((size_t)ti * kUnits + tuh) * (kBImg / 2), kBImg,
-                         &full[slot]);
-            ++g_issue;
-          }
-          if (!ok) break;
-          const int tgi = tg + i;
-          if (uh == 0) {
-            if (i == 0) ok = tc::mbar_wait(a_full, (uint32_t)(kitem & 1));
-            // one accumulator buffer: the epilogue copies a tile out of TMEM before the next one starts
-            if (ok && tgi >= 1) ok = tc::mbar_wait(acc_empty, (uint32_t)((tgi - 1) & 1));
+        const int ntl = t1 - t0;
+        for (int i = 0; i < ntl && ok; ++i) {
+          const int tgi = tg + i, buf = tgi & 1;
+          // the epilogue has read this accumulator buffer's previous tile out of TMEM
+          if (tgi >= 2) {
+            ok = tc::mbar_wait(&acc_empty[buf], (uint32_t)(((tgi >> 1) - 1) & 1));
             if (!ok) break;
           }
-          const int gs = g_base + sidx, slot = gs % kSlots;
-          ok = tc::mbar_wait(&full[slot], (uint32_t)((gs / kSlots) & 1));
-          if (!ok) break;
-          tc::fence_after_sync();
-          // slice u of the Green's function meets the rot_chol slices t <= 4 - u; products with
-          // t + u = d accumulate into group d.  Descriptors advance by constants.
-          const uint32_t blo = (uint32_t)bd0 + (uint32_t)(slot * kBImg / 16);
-          const uint32_t dcol = taddr + (uint32_t)(u * kBN);
-          const int tmax = (kGroups - 1) - u;
-          for (int t = 0; t <= tmax; ++t) {
-            const uint32_t alo = adlo + (uint32_t)((t * 128 * kKP * 2 + h * kKH * 16) / 16);
-            const uint32_t dt = dcol + (uint32_t)(t * kBN);
+          const uint32_t dcol = taddr + (uint32_t)(buf * 256);
+          for (int k = 0; k < kKS; ++k, ++gs) {
+            if (i == 0) {
+              ok = tc::mbar_wait(&a_full[k], (uint32_t)(kitem & 1));
+              if (!ok) break;
+            }
+            const int slot = gs % kExSlots;
+            ok = tc::mbar_wait(&full[slot], (uint32_t)((gs / kExSlots) & 1));
+            if (!ok) break;
+            tc::fence_after_sync();
+            const uint32_t alo = adlo + (uint32_t)(k * kAStep / 16);
+            const uint32_t blo = bdlo + (uint32_t)(slot * UB / 16);
 #pragma unroll
-            for (int ks = 0; ks < kKH / 16; ++ks)
-              tc::mma_bf16_lo2(dt, alo + (uint32_t)(ks * 16), ahi, blo + (uint32_t)(ks * 16), bhi, idesc,
-                               (u == 0 && h == 0 && ks == 0) ? 0u : 1u);
+            for (int t = 0; t < kSlices; ++t)
+              tc::mma_bf16_lo(dcol + (uint32_t)(t * P), alo + (uint32_t)(t * 256), blo, dhi, idesc[t],
+                              (k > 0 || t > 0) ? 1u : 0u);
+            tc::mma_commit(&empty[slot]);
+            if (i == ntl - 1) tc::mma_commit(&a_free[k]);  // chunk k of the Cholesky tile may be refilled
           }
-          tc::mma_commit(&empty[slot]);
-          if (uh == kUnits - 1) tc::mma_commit(acc_full);
+          if (ok) tc::mma_commit(&acc_full[buf]);
         }
-        if (ok) tc::mma_commit(a_free);
-        g_base += total;
         tg += ntl;
       }
       if (!ok) {
         report_timeout(a.status);
-        // let issued copies / MMAs drain (bounded) before the CTA frees its memory
-        if (g_issue > 0)
-          for (int k = 0; k < kSlots; ++k) tc::mbar_wait(&empty[k], 0u, 1000000u);
-        // release the epilogue: its next accumulator wait completes and it stops
         *abort_flag = 1;
-        tc::mbar_arrive(acc_full);
+        // the issued MMAs complete (a commit on a barrier nothing else arrives on) before the
+        // epilogue is released: its next accumulator wait completes and it stops
+        tc::mma_commit(never);
+        tc::mbar_wait(never, 0u, 1000000u);
+        tc::mbar_arrive(&acc_full[0]);
+        tc::mbar_arrive(&acc_full[1]);
+      }
+    }
+    __syncwarp();
+  } else if (warp == 18) {
+    // ------------------------------------------------ loader (one lane): Green's-function K16 steps
+    // into the ring as slots free up, and the next item's Cholesky chunks as soon as the MMAs
+    // reading each chunk completed; non-blocking polls, so neither stream waits on the other
+    if (lane == 0) {
+      bool ok = a.test_timeout_polls == 0;
+      // B stream: item bi (k-th of this CTA), unit bu of it; A stream: item ai (ka-th), chunk ak
+      int bi = blockIdx.x, bu = 0, bg = 0;
+      int ai = blockIdx.x, ka = 0, ak = 0;
+      uint32_t idle = 0, pend_mask = 0, pend_par = 0;
+      auto units_of = [&](int item) {
+        const int t0 = (item % a.chunks) * a.tiles_per_item;
+        return (min(L.ntiles, t0 + a.tiles_per_item) - t0) * kKS;
+      };
+      int btot = bi < a.n_items ? units_of(bi) : 0;
+      while (ok && (bi < a.n_items || ai < a.n_items)) {
+        bool progress = false;
+        if (bi < a.n_items) {
+          const int slot = bg % kExSlots;
+          if (bg < kExSlots || tc::mbar_try_wait(&empty[slot], (uint32_t)((bg / kExSlots - 1) & 1))) {
+            const int t0 = (bi % a.chunks) * a.tiles_per_item;
+            const int ti = t0 + bu / kKS, tk = bu % kKS;
+            tc::mbar_expect_tx(&full[slot], UB);
+            tc::bulk_g2s(ring + (size_t)slot * UB, a.green_img + ((size_t)ti * kKS + tk) * (UB / 2), UB, &full[slot]);
+            ++bg;
+            if (++bu == btot) {
+              bu = 0;
+              bi += gridDim.x;
+              btot = bi < a.n_items ? units_of(bi) : 0;
+            }
+            progress = true;
+          }
+        }
+        if (ai < a.n_items && (ka == 0 || tc::mbar_try_wait(&a_free[ak], (uint32_t)((ka - 1) & 1)))) {
+          const int blk = ai / a.chunks;
+          tc::mbar_expect_tx(&a_full[ak], kAStep);
+          tc::bulk_g2s(sA + (size_t)ak * kAStep, a.rot_img + ((size_t)blk * kAImg + (size_t)ak * kAStep) / 2, kAStep,
+                       &a_full[ak]);
+          pend_mask |= 1u << ak;
+          pend_par = (pend_par & ~(1u << ak)) | ((uint32_t)(ka & 1) << ak);
+          if (++ak == kKS) {
+            ak = 0;
+            ai += gridDim.x;
+            ++ka;
+          }
+          progress = true;
+        }
+        if (progress) {
+          idle = 0;
+        } else if (++idle > 40000000u || *abort_flag) {
+          ok = false;
+        }
+      }
+      if (!ok) {
+        if (a.test_timeout_polls == 0) report_timeout(a.status);
+        // bounded drain of the copies in flight before the CTA releases its memory
+        for (int u = max(0, bg - kExSlots); u < bg; ++u)
+          tc::mbar_wait(&full[u % kExSlots], (uint32_t)((u / kExSlots) & 1), 1000000u);
+        for (int k = 0; k < kKS; ++k)
+          if (pend_mask & (1u << k)) tc::mbar_wait(&a_full[k], (pend_par >> k) & 1u, 1000000u);
       }
     }
     __syncwarp();
   } else {
-    // ------------------------------------------------ epilogue: 16 warps (lane quarter q, column quarter h)
-    const int q = warp & 3, h = warp >> 2;
+    // ------------------------------------------------ epilogue: 16 warps (lane quarter q, orbital range h)
+    // and the reducer (warp 17): traces from the staged diagonals, then the walker's exchange
+    // from the 16 warp sums, while the epilogue warps move on to the next walker
+    constexpr int KPT = X::KPT;
+    const bool reducer = warp == 17;
+    const int q = warp & 3, h = (warp >> 2) & 3;
     const int r = q * 32 + lane;
-    const int i = r % L.n, gl = r / L.n;
+    const int n = L.n;
+    const int i = r % n, gl = r / n;
     const int j0 = h * JH;
-    const int etid = tid;  // 0..511
+    const uint32_t tlane = taddr + ((uint32_t)(q * 32) << 16);
+    ff* sFr = sF;
+    ff* sFi = sF + 128 * FS;
+    // Exchange sum_ij f_ij f_ji over unordered pairs: row i takes the pairs (i, (i + k) mod n)
+    // for k = h, h + 4, ... <= n / 2; weight 2 where 0 < k < n - k (the pair's other order is
+    // never visited), 1 for k = 0 and k = n / 2 (visited from both of its rows)
+    const int nk = n / 2 + 1;
     bool stop = false;
-    int tgl = 0;  // CTA-wide tile counter (accumulator phase)
+    int tgl = 0;  // CTA-wide tile counter (accumulator buffer and phase)
     for (int item = blockIdx.x; item < a.n_items && !stop; item += gridDim.x) {
-    const int blk = item / a.chunks;
-    const int t0 = (item % a.chunks) * a.tiles_per_item, t1 = min(L.ntiles, t0 + a.tiles_per_item);
-    const int ntl = t1 - t0;
-    const int rows_valid = min(L.gb, a.G - blk * L.gb) * L.n;
-    const bool rvalid = r < rows_valid;
-    const int ea = a.rot_e[(size_t)blk * 128 + r];
-    for (int it = 0; it < ntl; ++it, ++tgl) {
-      const int tile = t0 + it;
-      if (etid == 0) *flag = (tc::mbar_wait(acc_full, (uint32_t)(tgl & 1)) && *abort_flag == 0) ? 1 : 0;
-      tc::named_bar(1, kExEpi);
-      if (!*flag) {
-        if (etid == 0) report_timeout(a.status);
-        stop = true;
-        break;
-      }
-      tc::fence_after_sync();
-      const uint32_t tlane = taddr + ((uint32_t)(q * 32) << 16);
-      const int32_t* eB = a.green_e + (size_t)tile * kBN;
-      // copy every walker's f values of my row / column quarter out of TMEM, then release it
-      ff fre[WBT][JH], fim[WBT][JH];
+      const int blk = item / a.chunks;
+      const int t0 = (item % a.chunks) * a.tiles_per_item, t1 = min(L.ntiles, t0 + a.tiles_per_item);
+      const int ntl = t1 - t0;
+      const int nvec = min(L.gb, a.G - blk * L.gb);
+      const int rows_valid = nvec * n;
+      const bool rvalid = r < rows_valid;
+      const float sa = pow2f(a.rot_e[(size_t)blk * 128 + r] - kRotTopBits);
+      for (int it = 0; it < ntl; ++it, ++tgl) {
+        const int tile = t0 + it, buf = tgl & 1;
+        if (tid == 0) *flag = (tc::mbar_wait(&acc_full[buf], (uint32_t)((tgl >> 1) & 1)) && *abort_flag == 0) ? 1 : 0;
+        tc::named_bar(1, kExSync);
+        if (!*flag) {
+          if (tid == 0) report_timeout(a.status);
+          stop = true;
+          break;
+        }
+        tc::fence_after_sync();
+        const int nw = min(WBT, a.W - tile * WBT);
+        const int32_t* eB = a.green_e + (size_t)tile * P;
+#pragma unroll 1
+        for (int bl = 0; bl < WBT; ++bl) {
+          if (bl >= nw) break;  // uniform across the CTA
+          const int b = tile * WBT + bl;
+          if (!reducer) {
+            const int cb = bl * 2 * NP + 2 * j0;  // this thread's first column: (j0, re)
+            uint32_t raw[kGroups][2 * JH];
 #pragma unroll
-      for (int bl = 0; bl < WBT; ++bl) {
-        uint32_t raw[2][kGroups][JH];
+            for (int d = 0; d < kGroups; ++d)
 #pragma unroll
-        for (int c = 0; c < 2; ++c)
-#pragma unroll
-          for (int d = 0; d < kGroups; ++d)
+              for (int x = 0; x < JH; ++x)
+                tc::tmem_ld2(tlane + (uint32_t)(buf * 256 + d * P + cb + 2 * x), raw[d][2 * x], raw[d][2 * x + 1]);
+            tc::tmem_wait_ld();
+            if (bl == nw - 1) {  // the tile's last walker is in registers: release the buffer
+              tc::fence_before_sync();
+              __syncwarp();
+              if (lane == 0) tc::mbar_arrive(&acc_empty[buf]);
+            }
 #pragma unroll
             for (int jj = 0; jj < JH; ++jj)
-              raw[c][d][jj] = tc::tmem_ld1(tlane + (uint32_t)(d * kBN + bl * L.S + c * L.n_pad + j0 + jj));
-        tc::tmem_wait_ld();
 #pragma unroll
-        for (int c = 0; c < 2; ++c)
+              for (int c = 0; c < 2; ++c) {
+                float g[kGroups];
 #pragma unroll
-          for (int jj = 0; jj < JH; ++jj) {
-            float g[kGroups];
+                for (int d = 0; d < kGroups; ++d) {
+                  uint32_t v = raw[d][2 * jj + c];
+                  asm volatile("" : "+r"(v));  // consume after tcgen05.wait::ld
+                  g[d] = __uint_as_float(v);
+                }
+                // sum_d 2^(-9 d) A_d: the 2^-9d scalings are exact, the leading pair error-free
+                ff x = ff_two_sum(g[0], g[1] * 1.953125e-03f);
+                float lo = x.lo + g[2] * 3.814697265625e-06f;
+                lo += g[3] * 7.450580596923828125e-09f;
+                lo += g[4] * 1.4551915228366852e-11f;
+                x = ff_fast(x.hi, lo);
+                // times 2^(eA - 9) 2^(eB - 8), as two exact power-of-two factors
+                const float sb = pow2f(eB[cb + 2 * jj + c] - kGreenTopBits);
+                (c == 0 ? sFr : sFi)[r * FS + j0 + jj] = ff{x.hi * sa * sb, x.lo * sa * sb};
+              }
+          }
+          tc::named_bar(1, kExSync);
+          if (!reducer) {
+            // exchange products over this row's pairs; f_ij and f_ji both from the staging rows
+            const int brow = gl * n;
+            ff xr{0.f, 0.f}, xi{0.f, 0.f};
+            if (rvalid) {
 #pragma unroll
-            for (int d = 0; d < kGroups; ++d) {
-              uint32_t v = raw[c][d][jj];
-              asm volatile("" : "+r"(v));  // consume after tcgen05.wait::ld
-              g[d] = __uint_as_float(v);
+              for (int kk = 0; kk < KPT; ++kk) {
+                const int k = h + 4 * kk;
+                if (k >= nk) break;
+                int j = i + k;
+                if (j >= n) j -= n;
+                ff ar = sFr[r * FS + j], ai = sFi[r * FS + j];
+                const ff br = sFr[(brow + j) * FS + i], bi = sFi[(brow + j) * FS + i];
+                if (k != 0 && 2 * k != n) {  // exact doubling
+                  ar = ff{2.f * ar.hi, 2.f * ar.lo};
+                  ai = ff{2.f * ai.hi, 2.f * ai.lo};
+                }
+                // (a + ib)(c + id) = (ac - bd) + i(ad + bc)
+                ff_mad(xr, ar, br);
+                ff_mad(xr, ff{-ai.hi, -ai.lo}, bi);
+                ff_mad(xi, ar, bi);
+                ff_mad(xi, ai, br);
+              }
             }
-            // sum_d 2^(-9 d) A_d: the 2^-9d scalings are exact, the leading pair error-free
-            ff x = ff_two_sum(g[0], g[1] * 1.953125e-03f);
-            float lo = x.lo + g[2] * 3.814697265625e-06f;
-            lo += g[3] * 7.450580596923828125e-09f;
-            lo += g[4] * 1.4551915228366852e-11f;
-            x = ff_fast(x.hi, lo);
-            // times 2^(eA - 9) 2^(eB - 8), as two exact power-of-two factors
-            const float sc = pow2f(ea - kRotTopBits);
-            const float sb = pow2f(eB[bl * L.S + c * L.n_pad + j0 + jj] - kGreenTopBits);
-            const ff y{x.hi * sc * sb, x.lo * sc * sb};
-            if (c == 0) fre[bl][jj] = y; else fim[bl][jj] = y;
+            int sx0, sx1;
+            const long long V0 = ex_warp_sum(ff_fast(xr.hi, xr.lo), sx0);
+            const long long V1 = ex_warp_sum(ff_fast(xi.hi, xi.lo), sx1);
+            if (lane == 0) sRed[warp] = ExWarpSum{{V0, V1}, {sx0, sx1}, {0, 0}};
+          } else {
+            // traces c_g = sum_i f_gii of the tile's vectors, float-float in fixed order
+            for (int v = lane; v < nvec; v += 32) {
+              ff tr{0.f, 0.f}, ti{0.f, 0.f};
+              for (int ii = 0; ii < n; ++ii) {
+                const int rr = v * n + ii;
+                tr = ff_add(tr, sFr[rr * FS + ii]);
+                ti = ff_add(ti, sFi[rr * FS + ii]);
+              }
+              a.cs[(size_t)b * a.G + blk * L.gb + v] = make_double2(ff_d(tr), ff_d(ti));
+            }
           }
-      }
-      tc::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(acc_empty);
+          tc::named_bar(1, kExSync);
+          if (reducer) {
+            // the 16 warp sums aligned to the coarsest scale, then one exact integer sum
+            double val[2];
+            bool bad = false;
 #pragma unroll
-      for (int bl = 0; bl < WBT; ++bl) {
-        const int b = tile * WBT + bl;
-        if (b >= a.W) break;  // uniform across the epilogue warps
-        // exchange sum_j f_ij f_ji: stage re and im of this row's f values, one barrier
-        const int brow = gl * L.n;
-        ff* sFr = sF;
-        ff* sFi = sF + 128 * kFS;
-#pragma unroll
-        for (int jj = 0; jj < JH; ++jj) {
-          sFr[r * kFS + j0 + jj] = fre[bl][jj];
-          sFi[r * kFS + j0 + jj] = fim[bl][jj];
-        }
-        tc::named_bar(1, kExEpi);
-        ff xr{0.f, 0.f}, xi{0.f, 0.f};
-        if (rvalid) {
-#pragma unroll
-          for (int jj = 0; jj < JH; ++jj) {
-            // padding columns j >= n contribute nothing; their row brow + j may lie past this
-            // Cholesky vector (or past row 127), so they are skipped rather than multiplied by 0
-            if (j0 + jj >= L.n) break;
-            const ff orr = sFr[(brow + j0 + jj) * kFS + i], oi = sFi[(brow + j0 + jj) * kFS + i];
-            // (a + ib)(c + id) = (ac - bd) + i(ad + bc)
-            ff_mad(xr, fre[bl][jj], orr);
-            ff_mad(xr, ff{-fim[bl][jj].hi, -fim[bl][jj].lo}, oi);
-            ff_mad(xi, fre[bl][jj], oi);
-            ff_mad(xi, fim[bl][jj], orr);
+            for (int c = 0; c < 2; ++c) {
+              long long V = lane < 16 ? sRed[lane].v[c] : 0ll;
+              const int sw = lane < 16 ? sRed[lane].s[c] : 0x7fffffff;
+              const bool badc = __any_sync(0xffffffffu, sw == kExNonFinite);
+              bad = bad || badc;
+              const int smin = __reduce_min_sync(0xffffffffu, sw == kExNonFinite ? 0x7fffffff : sw);
+              const int sh = sw - smin;
+              V = (sw == kExNonFinite || sh >= 62) ? 0ll : (sh > 0 ? (V + (1ll << (sh - 1))) >> sh : V);
+              const long long T = warp_sum_i64(V);
+              val[c] = T == 0 ? 0.0 : (double)T * pow2d(max(-1022, min(1023, -smin)));
+            }
+            if (lane == 0) {
+              const double nan = __longlong_as_double(0x7FF8000000000000ll);
+              a.xpart[(size_t)b * a.nblk_total + L.blk_off + blk] =
+                  bad ? make_double2(nan, nan) : make_double2((double)a.mult * val[0], (double)a.mult * val[1]);
+            }
           }
-          if (h == 0) {  // f_ii of this row for the trace (force bias)
-            sC[2 * r] = sFr[r * kFS + i];
-            sC[2 * r + 1] = sFi[r * kFS + i];
-          }
-        }
-        xr = ff_fast(xr.hi, xr.lo);
-        xi = ff_fast(xi.hi, xi.lo);
-        for (int o = 16; o > 0; o >>= 1) {
-          xr = ff_add(xr, ff_shfl_xor(xr, o));
-          xi = ff_add(xi, ff_shfl_xor(xi, o));
-        }
-        if (lane == 0) {
-          sRed[2 * warp] = xr;
-          sRed[2 * warp + 1] = xi;
-        }
-        tc::named_bar(1, kExEpi);
-        // per-walker results; the next walker's staging writes come after its own barrier
-        if (warp == 0) {
-          ff tr = lane < 16 ? sRed[2 * lane] : ff{0.f, 0.f};
-          ff ti = lane < 16 ? sRed[2 * lane + 1] : ff{0.f, 0.f};
-          for (int o = 8; o > 0; o >>= 1) {
-            tr = ff_add(tr, ff_shfl_xor(tr, o));
-            ti = ff_add(ti, ff_shfl_xor(ti, o));
-          }
-          if (lane == 0)
-            a.xpart[(size_t)b * a.nblk_total + L.blk_off + blk] =
-                make_double2((double)a.mult * ff_d(tr), (double)a.mult * ff_d(ti));
-        }
-        // traces: 16 lanes per Cholesky vector of the block, 32 vectors per pass
-        for (int gbase = 0; gbase < L.gb; gbase += kExEpi / 16) {
-          if (gbase + 2 * warp >= L.gb) continue;  // warp-uniform: no vector of this pass in this warp
-          const int gv = gbase + (etid >> 4), ii = etid & 15;
-          const int g = blk * L.gb + gv;
-          const bool ok = gv < L.gb && ii < L.n && g < a.G;
-          ff tr = ok ? sC[2 * (gv * L.n + ii)] : ff{0.f, 0.f};
-          ff ti = ok ? sC[2 * (gv * L.n + ii) + 1] : ff{0.f, 0.f};
-          for (int o = 8; o > 0; o >>= 1) {
-            tr = ff_add(tr, ff_shfl_xor(tr, o));
-            ti = ff_add(ti, ff_shfl_xor(ti, o));
-          }
-          if (ii == 0 && gv < L.gb && g < a.G) a.cs[(size_t)b * a.G + g] = make_double2(ff_d(tr), ff_d(ti));
         }
       }
-    }
     }
   }
   tc::fence_before_sync();
@@ -1316,23 +1427,25 @@ static int check_mixed_shapes(const trot_system* s, const Spins& sp) {
   return TROT_OK;
 }
 
-template <int JH>
+template <int NP>
 static void exchange_exact_launch(dim3 grid, const ExArgs& a, cudaStream_t st) {
+  constexpr size_t smem = ExShape<NP>::bytes;
+  static_assert(smem <= 232448, "exchange kernel: shared memory above the 227 KB limit");
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(exchange_exact_kernel<JH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kExSmem + 1024);
+    cudaFuncSetAttribute(exchange_exact_kernel<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr_set = true;
   }
-  exchange_exact_kernel<JH><<<grid, kExThreads, kExSmem + 1024, st>>>(a);
+  exchange_exact_kernel<NP><<<grid, kExThreads, smem, st>>>(a);
 }
 
-static int launch_exchange_exact(int jh, dim3 grid, const ExArgs& a, cudaStream_t st) {
-  switch (jh) {
-    case 1: exchange_exact_launch<1>(grid, a, st); break;
-    case 2: exchange_exact_launch<2>(grid, a, st); break;
-    case 3: exchange_exact_launch<3>(grid, a, st); break;
+static int launch_exchange_exact(int n_pad, dim3 grid, const ExArgs& a, cudaStream_t st) {
+  switch (n_pad) {
     case 4: exchange_exact_launch<4>(grid, a, st); break;
-    default: set_error("exchange: n_pad/4 = %d unsupported", jh); return TROT_ERR_UNSUPPORTED;
+    case 8: exchange_exact_launch<8>(grid, a, st); break;
+    case 12: exchange_exact_launch<12>(grid, a, st); break;
+    case 16: exchange_exact_launch<16>(grid, a, st); break;
+    default: set_error("exchange: n_pad = %d unsupported", n_pad); return TROT_ERR_UNSUPPORTED;
   }
   TROT_CHECK_LAUNCH("exchange_exact_kernel");
   return TROT_OK;
@@ -1343,7 +1456,7 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
   for (int q = 0; q < sp.nspin; ++q) {
     SpinLayout L = spin_layout(s, sp, q);
     TROT_TIMED("green_slices", st, ([&]() -> int {
-      green_slices_kernel<<<L.ntiles, 256, 0, st>>>(N, L.n, L.n_pad, L.WB, W, sp.ntot, sp.off[q], m.green, m.gq[q],
+      green_slices_kernel<<<L.ntiles, 256, 0, st>>>(N, L.n, L.n_pad, L.P, L.WB, W, sp.ntot, sp.off[q], m.green, m.gq[q],
                                                     m.ge[q]);
       TROT_CHECK_LAUNCH("green_slices_kernel");
       return TROT_OK;
@@ -1355,7 +1468,7 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
     ExArgs a{};
     a.L = L;
     a.G = G; a.W = W; a.mult = sp.mult[q];
-    // persistent grid: one CTA per SM walks (Cholesky block, 16 walker tiles) items
+    // persistent grid: one CTA per SM walks (Cholesky tile, run of 8 walker tiles) items
     const int tpi = tune_get(TROT_TUNE_EXCHANGE_TILES);
     a.tiles_per_item = std::min(tpi > 0 ? tpi : 8, L.ntiles);
     a.chunks = (L.ntiles + a.tiles_per_item - 1) / a.tiles_per_item;
@@ -1371,7 +1484,7 @@ static int run_slices_and_exchange(const trot_system* s, const Spins& sp, MixedB
     a.test_timeout_polls = tune_get(TROT_TUNE_TEST_TIMEOUT);
     const int gknob = tune_get(TROT_TUNE_EXCHANGE_GRID);
     dim3 grid(std::min(a.n_items, gknob > 0 ? gknob : 152));
-    TROT_TIMED("exchange_exact_tc", st, launch_exchange_exact(L.n_pad / 4, grid, a, st));
+    TROT_TIMED("exchange_exact_tc", st, launch_exchange_exact(L.n_pad, grid, a, st));
   }
   const int n = W * G;
   fb_combine_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, sp.nspin, sp.mult[0], sp.mult[1], m.cs[0],

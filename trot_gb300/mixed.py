@@ -37,7 +37,7 @@ VHS_ORDER = 2
 # digit format of the exact product (trot_mixed.digit_format): FP16 digits, Cholesky
 # rows with a 9-bit leading digit, Green's-function rows (made on the device) with an
 # 8-bit leading digit, 9-bit lower digits for both
-DIGIT_FORMAT = 1
+DIGIT_FORMAT = 2
 ROT_TOP_BITS = 9
 GREEN_TOP_BITS = 8
 LOW_BITS = 9
@@ -124,9 +124,12 @@ def gammas_per_block(n: int) -> int:
 
 
 def rot_tiles(rot_chol: np.ndarray):
-    """(G, n, N) -> FP16 digits in the kernel's shared-memory image layout
-    (nblk, SLICES, 128, KPAD) (each 128 x KPAD tile in 8 x 8 core-matrix order,
-    K fastest) and row exponents (nblk, 128)."""
+    """(G, n, N) -> FP16 digits in the exchange kernel's shared-memory image
+    layout (nblk, KSTEPS, SLICES, 128, 16): per 128-row tile of whole Cholesky
+    vectors, per K16 step, per digit plane a 128 x 16 block in 8 x 8 core-matrix
+    order (K fastest; core matrices 128 B apart along K, 256 B apart along rows),
+    so one K16 step of all planes is one contiguous 20 KB chunk; and the row
+    exponents (nblk, 128)."""
     G, n, N = rot_chol.shape
     if n > 16 or N > KPAD:
         raise NotImplementedError(f"mixed path: n={n}, N={N} outside the tensor-core tile limits (n<=16, N<={KPAD})")
@@ -138,9 +141,10 @@ def rot_tiles(rot_chol: np.ndarray):
         r = rot_chol[g0:g1].reshape(-1, N)
         rows[blk, : r.shape[0], :N] = r
     q, e = digit_slices(rows)  # (SLICES, nblk, 128, KPAD)
-    # shared-memory image of the exchange kernel's A operand: [nblk][slice][core-matrix order]
-    img = q.transpose(1, 0, 2, 3).reshape(nblk, SLICES, 16, 8, KPAD // 8, 8).transpose(0, 1, 2, 4, 3, 5)
-    img = np.ascontiguousarray(img).reshape(nblk, SLICES, 128, KPAD)
+    ks = KPAD // 16
+    # (plane, blk, row group, row, kstep, k group, k) -> (blk, kstep, plane, row group, k group, row, k)
+    img = q.reshape(SLICES, nblk, 16, 8, ks, 2, 8).transpose(1, 4, 0, 2, 5, 3, 6)
+    img = np.ascontiguousarray(img).reshape(nblk, ks, SLICES, 128, 16)
     return torch.from_numpy(img.astype(np.float16)), torch.from_numpy(e.astype(np.int32)), gb, nblk
 
 
