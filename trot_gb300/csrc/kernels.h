@@ -85,10 +85,19 @@ int launch_step_finalize(int W, double* weights, double* scalars, long long* nod
 int exchange_chunks(int G);
 int launch_exchange(const Spins& sp, int W, int N, int G, const double2* green, double2* partial,
                     cudaStream_t st);
+// Fixed-point partial sum of the tensor-core exchange kernel: value v[c] 2^-s[c] (c = re, im);
+// s[c] = kExchangeNonFinite marks a non-finite contribution (the energy becomes NaN).
+struct ExFixed {
+  long long v[2];
+  int s[2];
+};
+static constexpr int kExchangeNonFinite = -0x7fffffff;
 // e1: e1_parts consecutive arrays of W values (one per spin for the mixed path), added in order
 // status (optional): as for launch_step_finalize; the energies become NaN when status[0] is set
+// partial: nchunks double2 per walker, or (xfixed != null) nchunks ExFixed per walker instead
 int launch_energy_combine(int W, int G, int nchunks, double h0, const double2* fb, const double2* e1, int e1_parts,
-                          const double2* partial, double2* energy, cudaStream_t st, const int* status = nullptr);
+                          const double2* partial, double2* energy, cudaStream_t st, const int* status = nullptr,
+                          const ExFixed* xfixed = nullptr);
 // dst[0] = dst[3] = src[0] when src[0] is set (status words of two workspace regions, see report_timeout)
 int launch_status_merge(const int* src, int* dst, cudaStream_t st);
 

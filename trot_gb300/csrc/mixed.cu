@@ -177,8 +177,8 @@ struct MixedBuffers {
   double2* e1;
   uint16_t* gq[2];   // per spin: [tile][K16 step][5 planes x P rows][16] in core-matrix order
   int32_t* ge[2];    // per spin: [tile][P] row exponents
-  double2* cs[2];
-  double2* xpart;
+  float4* cs[2];     // per spin: traces c_g per (walker, g) as float-float (re.hi, re.lo, im.hi, im.lo)
+  ExFixed* xpart;    // exchange partial sums per (walker, Cholesky tile)
   double2* fb;
   double2* xs;
   double2 *shift_term, *fb_term;
@@ -206,10 +206,10 @@ static size_t carve_mixed(const trot_system* s, const Spins& sp, Carver& c, Mixe
       SpinLayout L = spin_layout(s, sp, q);
       m.gq[q] = c.take<uint16_t>((size_t)L.ntiles * kKS * kSlices * L.P * 16);
       m.ge[q] = c.take<int32_t>((size_t)L.ntiles * L.P);
-      m.cs[q] = c.take<double2>(W * G);
+      m.cs[q] = c.take<float4>(W * G);
       m.nblk_total += L.nblk;
     }
-    m.xpart = c.take<double2>(W * m.nblk_total);
+    m.xpart = c.take<ExFixed>(W * m.nblk_total);
     m.fb = c.take<double2>(W * G);
   }
   if (op == TROT_OP_APPLY_TROTTER || op == TROT_OP_PROP_STEP) {
@@ -349,17 +349,20 @@ struct ExArgs {
   const int32_t* rot_e;      // [nblk][128]
   const uint16_t* green_img; // [ntiles][kKS][5 P][16] core-matrix order
   const int32_t* green_e;    // [ntiles][P]
-  double2* cs;
-  double2* xpart;
+  float4* cs;
+  ExFixed* xpart;
   int nblk_total;
   int* status;
   int test_timeout_polls;  // > 0: the producer's first wait is on a barrier nothing arrives on
 };
 
-static constexpr int kExThreads = 608;  // 16 epilogue warps, the MMA warp, the reducer warp, the loader warp
+static constexpr int kExLoaders = 2;     // loader warps: bulk copies issued by one warp complete one after
+                                        // another (~700 cycles each), copies of different warps overlap
+static constexpr int kExThreads = 32 * (18 + kExLoaders);  // 16 epilogue warps, the MMA warp, the reducer, the loaders
 static constexpr int kExEpi = 512;      // epilogue threads
 static constexpr int kExSync = 544;     // epilogue + reducer: the per-tile and per-walker barriers
-static constexpr int kExSlots = 5;      // ring of Green's-function K16 steps
+static constexpr int kExKU = 2;         // K16 steps per ring unit (one bulk copy; larger copies stream faster)
+static constexpr int kExSlots = 2;      // ring of Green's-function units
 
 // One epilogue warp's exchange sum of a walker: fixed-point values V[c] with scale 2^-s[c]
 // (s[c] = kExNonFinite: a lane's value was not finite).
@@ -369,7 +372,7 @@ struct ExWarpSum {
   int pad[2];
 };
 
-static constexpr int kExNonFinite = -0x7fffffff;
+static constexpr int kExNonFinite = kExchangeNonFinite;
 
 // Sum over the warp of float-float values as a fixed-point int64 with the warp's own scale:
 // returns V with sum ~= V 2^-s (|V| < 2^54), s = kExNonFinite if a lane is not finite.
@@ -403,7 +406,8 @@ struct ExShape {
   static constexpr int FS = NP + 1;                   // staging row stride (padded against bank conflicts)
   static constexpr int KPT = (NP / 2 + 4) / 4;        // exchange pair offsets k per epilogue thread
   static constexpr size_t offRing = kAImg;
-  static constexpr size_t offF = offRing + (size_t)kExSlots * UB;              // re, im: [128][FS] ff each
+  static constexpr uint32_t UU = kExKU * UB;                                   // one ring unit
+  static constexpr size_t offF = offRing + (size_t)kExSlots * UU;              // re, im: [128][FS] ff each
   static constexpr size_t offRed = offF + (size_t)2 * 128 * FS * sizeof(ff);   // [16 warps] per-warp exchange sums
   static constexpr size_t offBar = offRed + (size_t)16 * 32;                    // 34 mbarriers / words
   static constexpr size_t bytes = offBar + 40 * 8 + 1024;                      // + base alignment
@@ -413,7 +417,8 @@ template <int NP>
 __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a) {
   using X = ExShape<NP>;
   constexpr int P = X::P, WBT = X::WBT, JH = X::JH, FS = X::FS;
-  constexpr uint32_t UB = X::UB;
+  constexpr uint32_t UB = X::UB, UU = X::UU;
+  constexpr int kUnits = kKS / kExKU;  // ring units per walker tile
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
   unsigned char* sA = base;
@@ -492,17 +497,19 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
               ok = tc::mbar_wait(&a_full[k], (uint32_t)(kitem & 1));
               if (!ok) break;
             }
-            const int slot = gs % kExSlots;
-            ok = tc::mbar_wait(&full[slot], (uint32_t)((gs / kExSlots) & 1));
-            if (!ok) break;
+            const int ug = gs / kExKU, slot = ug % kExSlots, kj = gs % kExKU;
+            if (kj == 0) {
+              ok = tc::mbar_wait(&full[slot], (uint32_t)((ug / kExSlots) & 1));
+              if (!ok) break;
+            }
             tc::fence_after_sync();
             const uint32_t alo = adlo + (uint32_t)(k * kAStep / 16);
-            const uint32_t blo = bdlo + (uint32_t)(slot * UB / 16);
+            const uint32_t blo = bdlo + (uint32_t)((slot * UU + kj * UB) / 16);
 #pragma unroll
             for (int t = 0; t < kSlices; ++t)
               tc::mma_bf16_lo(dcol + (uint32_t)(t * P), alo + (uint32_t)(t * 256), blo, dhi, idesc[t],
                               (k > 0 || t > 0) ? 1u : 0u);
-            tc::mma_commit(&empty[slot]);
+            if (kj == kExKU - 1) tc::mma_commit(&empty[slot]);
             if (i == ntl - 1) tc::mma_commit(&a_free[k]);  // chunk k of the Cholesky tile may be refilled
           }
           if (ok) tc::mma_commit(&acc_full[buf]);
@@ -521,40 +528,48 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
       }
     }
     __syncwarp();
-  } else if (warp == 18) {
-    // ------------------------------------------------ loader (one lane): Green's-function K16 steps
-    // into the ring as slots free up, and the next item's Cholesky chunks as soon as the MMAs
-    // reading each chunk completed; non-blocking polls, so neither stream waits on the other
+  } else if (warp >= 18) {
+    // ------------------------------------------------ loaders (one lane per warp): Green's-function K16
+    // step pairs into the ring as slots free up (unit g by loader g % kExLoaders), and (loader 0) the next
+    // item's Cholesky chunks as soon as the MMAs reading each chunk completed; non-blocking tests
+    // (test_wait), so no stream waits on another
     if (lane == 0) {
+      const int w = warp - 18;
       bool ok = a.test_timeout_polls == 0;
-      // B stream: item bi (k-th of this CTA), unit bu of it; A stream: item ai (ka-th), chunk ak
+      // B stream: item bi, unit bu of it, global unit bg; A stream: item ai (ka-th of this CTA), chunk ak
       int bi = blockIdx.x, bu = 0, bg = 0;
-      int ai = blockIdx.x, ka = 0, ak = 0;
+      int ai = w == 0 ? blockIdx.x : a.n_items, ka = 0, ak = 0;
       uint32_t idle = 0, pend_mask = 0, pend_par = 0;
+      int last_b = -1;  // this loader's last issued unit
       auto units_of = [&](int item) {
         const int t0 = (item % a.chunks) * a.tiles_per_item;
-        return (min(L.ntiles, t0 + a.tiles_per_item) - t0) * kKS;
+        return (min(L.ntiles, t0 + a.tiles_per_item) - t0) * kUnits;
       };
       int btot = bi < a.n_items ? units_of(bi) : 0;
+      auto advance_b = [&]() {
+        ++bg;
+        if (++bu == btot) {
+          bu = 0;
+          bi += gridDim.x;
+          btot = bi < a.n_items ? units_of(bi) : 0;
+        }
+      };
+      while (bi < a.n_items && bg % kExLoaders != w) advance_b();
       while (ok && (bi < a.n_items || ai < a.n_items)) {
         bool progress = false;
         if (bi < a.n_items) {
           const int slot = bg % kExSlots;
-          if (bg < kExSlots || tc::mbar_try_wait(&empty[slot], (uint32_t)((bg / kExSlots - 1) & 1))) {
+          if (bg < kExSlots || tc::mbar_test_wait(&empty[slot], (uint32_t)((bg / kExSlots - 1) & 1))) {
             const int t0 = (bi % a.chunks) * a.tiles_per_item;
-            const int ti = t0 + bu / kKS, tk = bu % kKS;
-            tc::mbar_expect_tx(&full[slot], UB);
-            tc::bulk_g2s(ring + (size_t)slot * UB, a.green_img + ((size_t)ti * kKS + tk) * (UB / 2), UB, &full[slot]);
-            ++bg;
-            if (++bu == btot) {
-              bu = 0;
-              bi += gridDim.x;
-              btot = bi < a.n_items ? units_of(bi) : 0;
-            }
+            const int ti = t0 + bu / kUnits, tk = (bu % kUnits) * kExKU;
+            tc::mbar_expect_tx(&full[slot], UU);
+            tc::bulk_g2s(ring + (size_t)slot * UU, a.green_img + ((size_t)ti * kKS + tk) * (UB / 2), UU, &full[slot]);
+            last_b = bg;
+            do advance_b(); while (bi < a.n_items && bg % kExLoaders != w);
             progress = true;
           }
         }
-        if (ai < a.n_items && (ka == 0 || tc::mbar_try_wait(&a_free[ak], (uint32_t)((ka - 1) & 1)))) {
+        if (ai < a.n_items && (ka == 0 || tc::mbar_test_wait(&a_free[ak], (uint32_t)((ka - 1) & 1)))) {
           const int blk = ai / a.chunks;
           tc::mbar_expect_tx(&a_full[ak], kAStep);
           tc::bulk_g2s(sA + (size_t)ak * kAStep, a.rot_img + ((size_t)blk * kAImg + (size_t)ak * kAStep) / 2, kAStep,
@@ -570,14 +585,14 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
         }
         if (progress) {
           idle = 0;
-        } else if (++idle > 40000000u || *abort_flag) {
+        } else if (++idle > 100000000u || *abort_flag) {  // ~1-2 s of non-blocking polls
           ok = false;
         }
       }
       if (!ok) {
         if (a.test_timeout_polls == 0) report_timeout(a.status);
-        // bounded drain of the copies in flight before the CTA releases its memory
-        for (int u = max(0, bg - kExSlots); u < bg; ++u)
+        // bounded drain of this loader's copies in flight before the CTA releases its memory
+        for (int u = last_b; u >= 0 && u > last_b - kExSlots; u -= kExLoaders)
           tc::mbar_wait(&full[u % kExSlots], (uint32_t)((u / kExSlots) & 1), 1000000u);
         for (int k = 0; k < kKS; ++k)
           if (pend_mask & (1u << k)) tc::mbar_wait(&a_full[k], (pend_par >> k) & 1u, 1000000u);
@@ -694,38 +709,44 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
             const long long V1 = ex_warp_sum(ff_fast(xi.hi, xi.lo), sx1);
             if (lane == 0) sRed[warp] = ExWarpSum{{V0, V1}, {sx0, sx1}, {0, 0}};
           } else {
-            // traces c_g = sum_i f_gii of the tile's vectors, float-float in fixed order
-            for (int v = lane; v < nvec; v += 32) {
+            // traces c_g = sum_i f_gii of the tile's vectors, float-float in fixed order: S lanes
+            // per vector (a power of two) sum every S-th diagonal term, then S-lane shuffles
+            int S = 1;
+            while (S * 2 * nvec <= 32) S *= 2;
+            for (int v0 = 0; v0 < nvec; v0 += 32 / S) {
+              const int v = v0 + lane / S, sub = lane % S;
               ff tr{0.f, 0.f}, ti{0.f, 0.f};
-              for (int ii = 0; ii < n; ++ii) {
-                const int rr = v * n + ii;
-                tr = ff_add(tr, sFr[rr * FS + ii]);
-                ti = ff_add(ti, sFi[rr * FS + ii]);
+              if (v < nvec)
+                for (int ii = sub; ii < n; ii += S) {
+                  const int rr = v * n + ii;
+                  tr = ff_add(tr, sFr[rr * FS + ii]);
+                  ti = ff_add(ti, sFi[rr * FS + ii]);
+                }
+              for (int o = S / 2; o > 0; o >>= 1) {
+                tr = ff_add(tr, ff_shfl_xor(tr, o));
+                ti = ff_add(ti, ff_shfl_xor(ti, o));
               }
-              a.cs[(size_t)b * a.G + blk * L.gb + v] = make_double2(ff_d(tr), ff_d(ti));
+              if (sub == 0 && v < nvec) a.cs[(size_t)b * a.G + blk * L.gb + v] = make_float4(tr.hi, tr.lo, ti.hi, ti.lo);
             }
           }
           tc::named_bar(1, kExSync);
           if (reducer) {
-            // the 16 warp sums aligned to the coarsest scale, then one exact integer sum
-            double val[2];
-            bool bad = false;
-#pragma unroll
-            for (int c = 0; c < 2; ++c) {
-              long long V = lane < 16 ? sRed[lane].v[c] : 0ll;
-              const int sw = lane < 16 ? sRed[lane].s[c] : 0x7fffffff;
-              const bool badc = __any_sync(0xffffffffu, sw == kExNonFinite);
-              bad = bad || badc;
-              const int smin = __reduce_min_sync(0xffffffffu, sw == kExNonFinite ? 0x7fffffff : sw);
-              const int sh = sw - smin;
-              V = (sw == kExNonFinite || sh >= 62) ? 0ll : (sh > 0 ? (V + (1ll << (sh - 1))) >> sh : V);
-              const long long T = warp_sum_i64(V);
-              val[c] = T == 0 ? 0.0 : (double)T * pow2d(max(-1022, min(1023, -smin)));
-            }
-            if (lane == 0) {
-              const double nan = __longlong_as_double(0x7FF8000000000000ll);
-              a.xpart[(size_t)b * a.nblk_total + L.blk_off + blk] =
-                  bad ? make_double2(nan, nan) : make_double2((double)a.mult * val[0], (double)a.mult * val[1]);
+            // the 16 warp sums (lanes 0-15: re, 16-31: im) aligned to the coarsest scale of each
+            // half, then one exact integer sum per half; converted to FP64 by the energy combine
+            const int c = lane >> 4;
+            long long V = sRed[lane & 15].v[c];
+            const int sw = sRed[lane & 15].s[c];
+            const unsigned badm = __ballot_sync(0xffffffffu, sw == kExNonFinite);
+            int smin = sw == kExNonFinite ? 0x7fffffff : sw;
+            for (int o = 8; o > 0; o >>= 1) smin = min(smin, __shfl_xor_sync(0xffffffffu, smin, o));
+            const int sh = sw == kExNonFinite ? 62 : sw - smin;
+            V = sh >= 62 ? 0ll : (sh > 0 ? (V + (1ll << (sh - 1))) >> sh : V);
+            for (int o = 8; o > 0; o >>= 1) V += __shfl_xor_sync(0xffffffffu, V, o);
+            if ((lane & 15) == 0) {
+              ExFixed* out = a.xpart + (size_t)b * a.nblk_total + L.blk_off + blk;
+              const bool bad = ((badm >> (16 * c)) & 0xFFFFu) != 0;
+              out->v[c] = V * a.mult;
+              out->s[c] = (bad || smin == 0x7fffffff) ? (bad ? kExNonFinite : 0) : smin;
             }
           }
         }
@@ -738,12 +759,17 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
 }
 
 // fb = sum_s mult_s c_s   (complex, W x G)
-__global__ void fb_combine_kernel(int n, int nspin, int m0, int m1, const double2* __restrict__ c0,
-                                  const double2* __restrict__ c1, double2* __restrict__ fb) {
+// (the traces arrive as float-float pairs (re.hi, re.lo, im.hi, im.lo))
+__global__ void fb_combine_kernel(int n, int nspin, int m0, int m1, const float4* __restrict__ c0,
+                                  const float4* __restrict__ c1, double2* __restrict__ fb) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  double2 v = cscale(c0[k], (double)m0);
-  if (nspin == 2) v = cadd(v, cscale(c1[k], (double)m1));
+  const float4 a = c0[k];
+  double2 v = cscale(cmk(ff_d(ff{a.x, a.y}), ff_d(ff{a.z, a.w})), (double)m0);
+  if (nspin == 2) {
+    const float4 b = c1[k];
+    v = cadd(v, cscale(cmk(ff_d(ff{b.x, b.y}), ff_d(ff{b.z, b.w})), (double)m1));
+  }
   fb[k] = v;
 }
 
@@ -1660,8 +1686,8 @@ int mixed_local_energy(const trot_system* s, const Spins& sp, const double2* wa,
   TROT_TRY(begin(s, sp, c, m, TROT_OP_LOCAL_ENERGY, st));
   TROT_TRY(launch_green_ff(sp, s->n_walkers, s->norb, wa, wb, m.green, m.e1, st));
   TROT_TRY(run_slices_and_exchange(s, sp, m, st));
-  return launch_energy_combine(s->n_walkers, s->nchol, m.nblk_total, s->h0, m.fb, m.e1, sp.nspin, m.xpart, energy,
-                               st, m.status);
+  return launch_energy_combine(s->n_walkers, s->nchol, m.nblk_total, s->h0, m.fb, m.e1, sp.nspin, nullptr, energy,
+                               st, m.status, m.xpart);
 }
 
 int mixed_apply_trotter(const trot_system* s, const Spins& sp, const double2* xs, const TrotterArgs& a, void* ws,
@@ -1689,8 +1715,8 @@ int mixed_prop_step(const trot_system* s, const Spins& sp, const trot_state* sta
   TROT_TRY(run_slices_and_exchange(s, sp, m, st));
   if (energy_out)
     TROT_TIMED("energy_combine", st,
-               launch_energy_combine(W, G, m.nblk_total, s->h0, m.fb, m.e1, sp.nspin, m.xpart, energy_out, st,
-                                     m.status));
+               launch_energy_combine(W, G, m.nblk_total, s->h0, m.fb, m.e1, sp.nspin, nullptr, energy_out, st,
+                                     m.status, m.xpart));
   TROT_TIMED("fields", st, launch_fields(W, G, s->sqrt_dt, m.fb, s->mf_shifts_im, fields, m.xs, m.shift_term,
                                          m.fb_term, st));
   TROT_TRY(run_vhs(s, m, m.xs, st));

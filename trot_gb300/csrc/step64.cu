@@ -225,7 +225,8 @@ int launch_exchange(const Spins& sp, int W, int N, int G, const double2* green, 
 __global__ void __launch_bounds__(256)
 energy_combine_kernel(int G, int nchunks, double h0, const double2* __restrict__ fb,
                       const double2* __restrict__ e1, int e1_parts, const double2* __restrict__ partial,
-                      double2* __restrict__ energy, const int* __restrict__ status) {
+                      double2* __restrict__ energy, const int* __restrict__ status,
+                      const ExFixed* __restrict__ xfixed) {
   __shared__ double2 red[32];
   const int b = blockIdx.x;
   if (status && status[0] != 0) {  // the exchange / force-bias kernel timed out: no numbers
@@ -238,7 +239,19 @@ energy_combine_kernel(int G, int nchunks, double h0, const double2* __restrict__
     const double2 f = fb[(size_t)b * G + g];
     cfma(c, f, f);
   }
-  for (int k = threadIdx.x; k < nchunks; k += blockDim.x) x = cadd(x, partial[(size_t)b * nchunks + k]);
+  if (xfixed) {
+    const double nan = __longlong_as_double(0x7FF8000000000000ll);
+    for (int k = threadIdx.x; k < nchunks; k += blockDim.x) {
+      const ExFixed f = xfixed[(size_t)b * nchunks + k];
+      double v[2];
+      for (int c = 0; c < 2; ++c)  // v 2^-s, with 2^-s formed from its exponent bits (|s| < 1000)
+        v[c] = f.s[c] == kExchangeNonFinite ? nan
+                                             : (double)f.v[c] * __longlong_as_double((long long)(1023 - f.s[c]) << 52);
+      x = cadd(x, cmk(v[0], v[1]));
+    }
+  } else {
+    for (int k = threadIdx.x; k < nchunks; k += blockDim.x) x = cadd(x, partial[(size_t)b * nchunks + k]);
+  }
   c = block_sum2(c, red);
   x = block_sum2(x, red);
   if (threadIdx.x == 0) {
@@ -249,8 +262,9 @@ energy_combine_kernel(int G, int nchunks, double h0, const double2* __restrict__
 }
 
 int launch_energy_combine(int W, int G, int nchunks, double h0, const double2* fb, const double2* e1, int e1_parts,
-                          const double2* partial, double2* energy, cudaStream_t st, const int* status) {
-  energy_combine_kernel<<<W, 256, 0, st>>>(G, nchunks, h0, fb, e1, e1_parts, partial, energy, status);
+                          const double2* partial, double2* energy, cudaStream_t st, const int* status,
+                          const ExFixed* xfixed) {
+  energy_combine_kernel<<<W, 256, 0, st>>>(G, nchunks, h0, fb, e1, e1_parts, partial, energy, status, xfixed);
   TROT_CHECK_LAUNCH("energy_combine_kernel");
   return TROT_OK;
 }
