@@ -20,13 +20,11 @@
 namespace trot {
 
 // ------------------------------------------------------------------ Green's functions in float-float
-// Same quantities as green_kernel (green.cu): M_s = C_s^T w_s in FP64, M_s^{-1} by
-// FP64 Gauss-Jordan, G_s = (w_s M_s^{-1})^T and e1 = sum_s mult_s sum G_s o rot_h1_s,
-// with the N x n^2 product G_s in float-float (FP32 pairs, ~2^-44 relative) on the
-// FP32 pipe.  M_s stays FP64: its rounding error is amplified by the condition
-// number of M_s (10^4 - 10^5 for walkers far from the trial), and a float-float M_s
-// moved such walkers' local energies by up to 5e-5 Ha at |E_L| ~ 5e5 Ha.  One CTA per
-// (walker, spin).
+// Same quantities as green_kernel (green.cu): M_s = C_s^T w_s, M_s^{-1} by FP64
+// Gauss-Jordan, G_s = (w_s M_s^{-1})^T and e1 = sum_s mult_s sum G_s o rot_h1_s, with
+// the two N x n^2 products in float-float (FP32 pairs, ~2^-44 relative) on the FP32
+// pipe: this GPU's FP64 pipe retires about two FMAs per clock per SM, so an FP64 M_s
+// alone would cost more than the rest of the kernel.  One CTA per (walker, spin).
 __global__ void __launch_bounds__(256)
 green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* __restrict__ wb,
                 double2* __restrict__ green, double2* __restrict__ e1_out) {
@@ -36,7 +34,8 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
   const int b = blockIdx.x, s = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
   const int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
   ffc* Wf = reinterpret_cast<ffc*>(smem_raw);                    // N x n
-  double2* Md = reinterpret_cast<double2*>(Wf + (size_t)N * nmax);  // n x n
+  ff* Cf = reinterpret_cast<ff*>(Wf + (size_t)N * nmax);          // N x n
+  double2* Md = reinterpret_cast<double2*>(Cf + (size_t)N * nmax + ((N * nmax) & 1));  // n x n
   double2* Mi = Md + nmax * nmax;                                 // n x n
   ffc* Mif = reinterpret_cast<ffc*>(Mi + nmax * nmax);            // n x n
   ff e1r{0.f, 0.f}, e1i{0.f, 0.f};
@@ -48,30 +47,39 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
     for (int e = tid; e < N * n; e += nt) {
       const double2 x = w[e];
       Wf[e] = ffc{ff_from_d(x.x), ff_from_d(x.y)};
+      Cf[e] = ff_from_d(C[e]);
     }
     __syncthreads();
     for (int e = tid; e < n * n; e += nt) {
-      // M[i][j] = sum_p C[p][i] w[p][j] in FP64 from the walker in global memory (L1-resident
-      // after the staging loop); two independent accumulator pairs over p (mod 2) in a fixed
-      // order, so the result is the same on every run
+      // M[i][j] = sum_p C[p][i] w[p][j] in float-float on the FP32 pipe (four accumulator pairs over
+      // p mod 4 against the latency chains, combined in a fixed order)
       const int i = e / n, j = e % n;
-      double ar0 = 0.0, ai0 = 0.0, ar1 = 0.0, ai1 = 0.0;
+      ff ar[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      ff ai[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
       int p = 0;
-      for (; p + 2 <= N; p += 2) {
-        const double c0 = C[p * n + i], c1 = C[(p + 1) * n + i];
-        const double2 x0 = w[p * n + j], x1 = w[(p + 1) * n + j];
-        ar0 = fma(c0, x0.x, ar0);
-        ai0 = fma(c0, x0.y, ai0);
-        ar1 = fma(c1, x1.x, ar1);
-        ai1 = fma(c1, x1.y, ai1);
+      for (; p + 4 <= N; p += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const ff c = Cf[(p + u) * n + i];
+          const ffc x = Wf[(p + u) * n + j];
+          ff_mad(ar[u], c, x.re);
+          ff_mad(ai[u], c, x.im);
+        }
       }
-      if (p < N) {
-        const double c0 = C[p * n + i];
-        const double2 x0 = w[p * n + j];
-        ar0 = fma(c0, x0.x, ar0);
-        ai0 = fma(c0, x0.y, ai0);
+      for (; p < N; ++p) {
+        const ff c = Cf[p * n + i];
+        const ffc x = Wf[p * n + j];
+        ff_mad(ar[0], c, x.re);
+        ff_mad(ai[0], c, x.im);
       }
-      Md[e] = make_double2(ar0 + ar1, ai0 + ai1);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        ar[u] = ff_fast(ar[u].hi, ar[u].lo);
+        ai[u] = ff_fast(ai[u].hi, ai[u].lo);
+      }
+      const ff sr = ff_add(ff_add(ar[0], ar[1]), ff_add(ar[2], ar[3]));
+      const ff si = ff_add(ff_add(ai[0], ai[1]), ff_add(ai[2], ai[3]));
+      Md[e] = make_double2(ff_d(sr), ff_d(si));
     }
     __syncthreads();
     block_gauss_jordan(Md, n, n, Mi, &piv, red);
@@ -110,7 +118,7 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
 static int launch_green_ff(const Spins& sp, int W, int N, const double2* wa, const double2* wb, double2* green,
                            double2* e1_out, cudaStream_t st) {
   const int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
-  const size_t smem = (size_t)N * nmax * sizeof(ffc) + (size_t)nmax * nmax * 3 * 16;
+  const size_t smem = (size_t)N * nmax * (sizeof(ffc) + sizeof(ff)) + 16 + (size_t)nmax * nmax * 3 * 16;
   if (smem > 200 * 1024) {
     set_error("green_ff: %zu bytes of shared memory needed", smem);
     return TROT_ERR_UNSUPPORTED;
