@@ -1,14 +1,14 @@
 """Generate golden vectors by running the reference's own trot modules.
 
-Run in a container that has the trot sources (argument 1, default
-/root/reference) but no jax: ``_jaxshim`` supplies numpy-backed jax names, and
+Run in a container that has the trot sources (argument 1, or the TROT_REFERENCE
+environment variable; required) but no jax: ``_jaxshim`` supplies numpy-backed jax names, and
 the reference functions (trot/meas/{rhf,uhf}.py, trot/trial/{rhf,uhf}.py,
 trot/prop/{afqmc,chol_afqmc_ops,blocks}.py, trot/walkers.py) run unmodified.
 Fields and SR zeta are injected. Outputs go to tests/golden/*.npz next to this
 script; the tests read only those files (the reference is not needed at test
 time).
 
-    python tests/golden/make_golden.py [/path/to/trot]
+    python tests/golden/make_golden.py /path/to/trot [fp|cisd]
 """
 from __future__ import annotations
 
@@ -24,7 +24,10 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 import _jaxshim  # noqa: E402
 
 _jaxshim.install()
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TROT_REFERENCE", "")
+if not REF or not os.path.isdir(os.path.join(REF, "trot")):
+    sys.exit("usage: make_golden.py /path/to/trot [fp|cisd]  (the directory that holds the trot package; "
+             "or set TROT_REFERENCE)")
 sys.path.insert(0, REF)
 
 from trot.core.system import System  # noqa: E402
