@@ -546,6 +546,63 @@ def precision_leg(chol_scale=0.1, n_steps=200, seed=5):
     }
 
 
+def fragments_leg(n_steps=10, warmup=3, n_walkers=128, n_fragments=24):
+    """The batched uneven-fragment workload (24 LNO-style RHF fragments, N ~ U[30, 160],
+    nocc = round(0.12 N), G = 4 N, 128 walkers each): one phaseless step + local energy
+    of every fragment per step, each fragment on its own stream, the whole batch captured
+    as one CUDA graph and replayed; the tensor-core path for fragments with N <= 128 and
+    nocc <= 16 (the mixed batch), the FP64 kernels for all of them (the FP64 batch).
+    Per-walker |dE_L| mixed vs FP64 on identical walkers near the trial, per mixed fragment."""
+    import torch
+
+    from trot_gb300 import fragments as fr
+    from trot_gb300 import synthetic
+    from trot_gb300.meas import make_rhf_meas_ops
+
+    sizes = fr.lno_fragment_sizes(n_fragments)
+    out = {"workload": f"{n_fragments} RHF fragments, N ~ U[30, 160] (seeded draw), nocc = round(0.12 N), "
+                       f"G = 4 N, W = {n_walkers} each, dt = 0.005, one graph replay per step",
+           "sizes_N": [int(sz[0]) for sz in sizes]}
+    for mixed in (True, False):
+        t0 = time.perf_counter()
+        batch = fr.FragmentBatch([fr.make_fragment(N, n, G, n_walkers, seed=k, mixed=mixed)
+                                  for k, (N, n, G) in enumerate(sizes)])
+        t_build = time.perf_counter() - t0
+        for _ in range(warmup):
+            batch.step()
+        batch.capture()
+        batch.step()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(n_steps):
+            batch.step()
+        ev1.record()
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        leg = {"value": batch.walker_steps_per_step * n_steps / (ms / 1e3), "unit": "walker-steps/s",
+               "ms_per_step": ms / n_steps, "steps": n_steps, "setup_s": t_build,
+               "tensor_core_fragments": int(sum(f.mixed for f in batch.fragments))}
+        if mixed:
+            worst = 0.0
+            for f in batch.fragments:
+                if not f.mixed:
+                    continue
+                m64 = make_rhf_meas_ops(f.sys)
+                mc64 = m64.build_meas_ctx(f.ham, f.trial)
+                w = torch.as_tensor(synthetic.perturbed_walkers(f.trial.mo_coeff.cpu().numpy(), 16, 0.1, 3)).cuda()
+                e64 = m64.kernels["energy"](w, f.ham, mc64, f.trial)
+                emx = f.meas_ops.kernels["energy"](w, f.ham, f.meas_ctx, f.trial)
+                worst = max(worst, float((emx - e64).abs().max()))
+            leg["precision_check"] = {"max_abs_dE_L_Ha": worst,
+                                      "on": "16 walkers near the trial (noise 0.1) per tensor-core fragment"}
+        out["mixed" if mixed else "fp64"] = leg
+        del batch
+        torch.cuda.empty_cache()
+    out["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
 def cpu_cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -573,6 +630,9 @@ def main():
                     help="skip the 200-step mixed-vs-FP64 trajectory comparison")
     ap.add_argument("--precision-only", action="store_true",
                     help="run only the mixed-vs-FP64 trajectory comparison and print its JSON")
+    ap.add_argument("--no-fragments", action="store_true", help="skip the 24-fragment batch leg")
+    ap.add_argument("--fragments-only", action="store_true",
+                    help="run only the 24-fragment batch leg and print its JSON")
     ap.add_argument("--profile-run", action="store_true",
                     help="timed steps only (no e2e, FP64 comparison, precision check or CPU baseline): "
                          "for profiler launch lists")
@@ -626,6 +686,10 @@ def main():
     if args.adjoint_only:
         if rank == 0:
             print(json.dumps({"adjoint": adjoint_leg(n_steps=args.adjoint_steps)}), flush=True)
+        return
+    if args.fragments_only:
+        if rank == 0:
+            print(json.dumps({"fragments": fragments_leg()}), flush=True)
         return
     if args.precision_only:
         if rank == 0:
@@ -808,6 +872,8 @@ def main():
                                     "selections (precision_trajectory)")
     if not args.no_adjoint and rank == 0 and world == 1:
         line["adjoint"] = adjoint_leg(n_steps=args.adjoint_steps)
+    if not args.no_fragments and rank == 0 and world == 1 and args.config == "cfg2_uhf_n120":
+        line["fragments"] = fragments_leg()
     if not args.no_cpu_baseline:
         sample = args.cpu_sample or 64
         r, secs, ks = cpu_port_rate(cfg, sample, 2, min_seconds=10.0)

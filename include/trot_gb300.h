@@ -61,7 +61,8 @@ typedef enum {
   TROT_OP_PROP_STEP = 3,
   TROT_OP_QR = 4,
   TROT_OP_SR = 5,
-  TROT_OP_OVERLAP = 6
+  TROT_OP_OVERLAP = 6,
+  TROT_OP_RDM1 = 7
 } trot_op;
 
 /* Operands of the mixed-precision path, prepared once per (trial,
@@ -245,6 +246,18 @@ int trot_sr_resample(const trot_system* sys, const double* weights_in, const dou
  * obs_out (float64 [2], device) receives [e_block, sum of weights]. */
 int trot_block_energy(int n_walkers, const double* energy, double* weights, double* scalars, double dt,
                       double shift_ema, double* obs_out, void* stream);
+
+/* The block's rdm1 observable (trot/prop/blocks.py:259-268 with
+ * rdm1_kernel_rw / _uw, trot/meas/rhf.py:191-216, trot/meas/uhf.py:97-110):
+ * rdm1_s = sum_w wt_w G_ws^T C_s^H / sum_w wt_w, complex128 (2, norb, norb)
+ * (restricted walkers: the same matrix for both spins), zero when the weights
+ * sum to 0.  green: trot_half_green's output for the block's walkers (after the
+ * block's orthonormalisation); weights / obs: the guarded weights and the
+ * [e_block, sum of weights] that trot_block_energy wrote (as in the reference,
+ * a walker of weight 0 with a non-finite Green's function makes the sum NaN).
+ * Workspace: trot_workspace_size(sys, TROT_OP_RDM1).  FP64. */
+int trot_block_rdm1(const trot_system* sys, const double* green, const double* weights, const double* obs,
+                    double* rdm1_out, void* workspace, size_t workspace_bytes, void* stream);
 
 /* Auxiliary fields N(0, 1), float64 (W, G), drawn on the device from the
  * sub-key of `key` (int64 [2] device array holding two uint32 words,

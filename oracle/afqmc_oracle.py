@@ -370,6 +370,18 @@ class Model:
     def walker_kind(self):
         return "restricted" if self.kind == "rhf_r" else "unrestricted"
 
+    def rdm1(self, w):
+        """Per-walker one-body RDMs (W, 2, N, N): ``rdm1_kernel_rw`` / ``_uw``
+        (trot/meas/rhf.py:191-216, trot/meas/uhf.py:97-110): G_s^T C_s^H per spin,
+        the same matrix twice for restricted walkers."""
+        if self.kind == "rhf_r":
+            g = np.swapaxes(half_green(w, self.mo), -1, -2) @ np.conj(self.mo).T
+            return np.stack([g, g], axis=1)
+        ma, mb = (self.mo, self.mo) if self.kind == "rhf_u" else self.mo
+        da = np.swapaxes(half_green(w[0], ma), -1, -2) @ np.conj(ma).T
+        db = np.swapaxes(half_green(w[1], mb), -1, -2) @ np.conj(mb).T
+        return np.stack([da, db], axis=1)
+
 
 def afqmc_step(state: State, model: Model, params: Params, fields) -> State:
     """``afqmc_step`` (trot/prop/afqmc.py:79-144) with injected fields (W, G)."""
@@ -434,10 +446,12 @@ def stochastic_reconfiguration(w, weights, zeta, walker_kind):
     return wn, np.full((n,), avg, dtype=weights.dtype), idx
 
 
-def block(state: State, model: Model, params: Params, fields_seq, zeta):
+def block(state: State, model: Model, params: Params, fields_seq, zeta, rdm1=False):
     """``block`` (trot/prop/blocks.py:195-287): n_prop_steps steps with injected
     fields, orthonormalise, energy with outlier clamp, EMA of e_estimate, SR with
-    injected zeta. Returns (state, e_block, w_sum)."""
+    injected zeta. Returns (state, e_block, w_sum), and with ``rdm1`` also the
+    block's rdm1 observable (blocks.py:259-268): sum_w wt_w rdm1_w / sum_w wt_w
+    over the guarded weights (zeros when they sum to 0; 0 x NaN stays NaN, as there)."""
     for x in fields_seq:
         state = afqmc_step(state, model, params, x)
     w = orthonormalize(state.walkers, model.walker_kind)
@@ -456,9 +470,15 @@ def block(state: State, model: Model, params: Params, fields_seq, zeta):
         e_block = e_ref
     alpha = params.shift_ema
     e_est = (1.0 - alpha) * state.e_estimate + alpha * e_block
+    if rdm1:
+        samples = model.rdm1(w)
+        num = np.einsum("b,bsij->sij", weights, samples)
+        obs_rdm1 = np.zeros_like(num) if w_sum == 0 else num / w_safe
     w_sr, weights_sr, _ = stochastic_reconfiguration(w, weights, zeta, model.walker_kind)
     ov_sr = model.overlap(w_sr)
     st = State(w_sr, weights_sr, ov_sr, state.pop_control_ene_shift, e_est, state.node_encounters)
+    if rdm1:
+        return st, e_block, w_sum, obs_rdm1
     return st, e_block, w_sum
 
 

@@ -134,6 +134,15 @@ def case(name, norb, nelec, nchol, n_walkers, kind, dt=0.01, n_steps=3, h0=0.7, 
     _save_state(out, "block_", sb, kind)
     out["block_energy"] = float(obs.scalars["energy"])
     out["block_weight"] = float(obs.scalars["weight"])
+    # the same block with the rdm1 observable (weighted average of rdm1_kernel_* over the walkers)
+    for k in range(n_steps):
+        INJ.append(step_fields[k])
+    INJ.append(np.asarray(zeta))
+    _, obs_r = blocks.block(state, sys=sysm, params=params, ham_data=ham, trial_data=trial,
+                            trial_ops=trial_ops, meas_ops=meas_ops, meas_ctx=meas_ctx,
+                            prop_ops=prop_ops, prop_ctx=prop_ctx, observable_names=("rdm1",))
+    assert not INJ
+    out["block_rdm1"] = np.asarray(obs_r.observables["rdm1"])
 
     # QR with phase convention, SR alone
     q, norm = wk.orthogonalize(walkers, walker_kind)

@@ -90,6 +90,20 @@ def test_block_vs_golden(golden):
     assert abs(float(obs.scalars["weight"]) - float(golden["block_weight"])) < 1e-11 * float(golden["block_weight"])
 
 
+def test_block_rdm1_vs_golden(golden):
+    """The block's rdm1 observable (the reference's weighted rdm1_kernel_* average)."""
+    import trot_gb300 as tg
+
+    S = Setup.from_golden(golden)
+    params = tg.QmcParams(dt=float(golden["dt"]), n_prop_steps=golden["step_fields"].shape[0],
+                          n_walkers=S.params.n_walkers, seed=1)
+    _, obs = tg.block(_state(S, golden), sys=S.sys, params=params, ham_data=S.ham, trial_data=S.trial,
+                      trial_ops=S.trial_ops, meas_ops=S.meas_ops, meas_ctx=S.meas_ctx, prop_ops=S.prop_ops,
+                      prop_ctx=S.prop_ctx, fields_seq=dev(golden["step_fields"]), zeta=float(golden["zeta"]),
+                      observable_names=("rdm1",))
+    assert rel(cpu(obs.observables["rdm1"]), golden["block_rdm1"]) < 1e-10
+
+
 def test_qr_sr_vs_golden(golden):
     import trot_gb300 as tg
 

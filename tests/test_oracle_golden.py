@@ -70,6 +70,15 @@ def test_block(golden):
     assert abs(w_sum - float(golden["block_weight"])) < 1e-12 * max(1, w_sum)
 
 
+def test_block_rdm1(golden):
+    """The block's rdm1 observable (weighted average of rdm1_kernel_rw / _uw)."""
+    m = model_from_golden(golden)
+    params = orc.Params(dt=float(golden["dt"]))
+    _, _, _, rdm1 = orc.block(state_from_golden(golden), m, params, golden["step_fields"], float(golden["zeta"]),
+                              rdm1=True)
+    assert rel_err(rdm1, golden["block_rdm1"]) < 1e-11
+
+
 def test_qr_and_sr(golden):
     m = model_from_golden(golden)
     w = walkers_from_golden(golden)

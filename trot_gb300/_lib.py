@@ -24,7 +24,7 @@ TUNE_EXCHANGE_TILES, TUNE_EXCHANGE_GRID, TUNE_TEST_TIMEOUT = 0, 1, 2
 # trot_precision
 FP64, MIXED = 0, 1
 # trot_op
-OP_FORCE_BIAS, OP_LOCAL_ENERGY, OP_APPLY_TROTTER, OP_PROP_STEP, OP_QR, OP_SR, OP_OVERLAP = range(7)
+OP_FORCE_BIAS, OP_LOCAL_ENERGY, OP_APPLY_TROTTER, OP_PROP_STEP, OP_QR, OP_SR, OP_OVERLAP, OP_RDM1 = range(8)
 
 _p = ctypes.c_void_p
 _d = ctypes.c_double
@@ -97,6 +97,7 @@ _SIGNATURES = {
     "trot_sr_resample": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _d, _p, _p, _p, _p, _p, _p, _p,
                               ctypes.c_size_t, _p]),
     "trot_block_energy": (_i, [_i, _p, _p, _p, _d, _d, _p, _p]),
+    "trot_block_rdm1": (_i, [ctypes.POINTER(TrotSystem), _p, _p, _p, _p, _p, ctypes.c_size_t, _p]),
     "trot_sample_normal_fields": (_i, [_p, _i, _i, _p, _p]),
     "trot_sample_uniform": (_i, [_p, _i, _p, _p]),
     "trot_split_key": (_i, [_p, _p]),

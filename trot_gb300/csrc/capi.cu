@@ -1,5 +1,6 @@
 // extern "C" entry points (include/trot_gb300.h): argument checks, workspace
 // carving and the launch sequence of each op.
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -122,6 +123,51 @@ static int force_bias_from_green(const trot_system* s, const Spins& sp, const do
   return TROT_OK;
 }
 
+// ------------------------------------------------------------------ block rdm1 observable
+// Chunks of walkers per Green's-function row, so that rows x chunks covers the GPU.
+static int rdm1_chunks(const trot_system* s, const Spins& sp) {
+  const int want = (2 * 152 + sp.ntot - 1) / sp.ntot;
+  return std::max(1, std::min(std::min(64, want), s->n_walkers));
+}
+
+static size_t rdm1_workspace_size(const trot_system* s, const Spins& sp) {
+  return (size_t)rdm1_chunks(s, sp) * sp.ntot * s->norb * sizeof(double2);
+}
+
+// part[c][row][p] = sum over the walkers of chunk c (in order) of wt_w G_w[row][p]
+__global__ void rdm1_partial_kernel(int W, int rows, int N, int wchunk, const double2* __restrict__ green,
+                                    const double* __restrict__ weights, double2* __restrict__ part) {
+  const int row = blockIdx.x, c = blockIdx.y;
+  const int w0 = c * wchunk, w1 = min(W, w0 + wchunk);
+  for (int p = threadIdx.x; p < N; p += blockDim.x) {
+    double2 acc = cmk(0.0, 0.0);
+    for (int w = w0; w < w1; ++w) acc = cadd(acc, cscale(green[((size_t)w * rows + row) * N + p], weights[w]));
+    part[((size_t)c * rows + row) * N + p] = acc;
+  }
+}
+
+// out[s][p][q] = sum_i Gbar_s[i][p] conj(C_s[q][i]) / w_sum with Gbar = sum_c part[c] (fixed order)
+__global__ void rdm1_finish_kernel(Spins sp, int N, int nchunk, const double2* __restrict__ part,
+                                   const double* __restrict__ obs, double2* __restrict__ out) {
+  extern __shared__ double2 gbar[];  // [n]
+  const int so = blockIdx.x, p = blockIdx.y;
+  const int s = sp.nspin == 1 ? 0 : so;
+  const int n = sp.n[s], off = sp.off[s];
+  const double* C = sp.mo[s];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double2 acc = cmk(0.0, 0.0);
+    for (int c = 0; c < nchunk; ++c) acc = cadd(acc, part[((size_t)c * sp.ntot + off + i) * N + p]);
+    gbar[i] = acc;
+  }
+  __syncthreads();
+  const double wsum = obs[1];
+  for (int q = threadIdx.x; q < N; q += blockDim.x) {
+    double2 v = cmk(0.0, 0.0);
+    for (int i = 0; i < n; ++i) v = cadd(v, cscale(gbar[i], C[(size_t)q * n + i]));
+    out[((size_t)so * N + p) * N + q] = wsum == 0.0 ? cmk(0.0, 0.0) : cmk(v.x / wsum, v.y / wsum);
+  }
+}
+
 }  // namespace trot
 
 using namespace trot;
@@ -136,12 +182,37 @@ size_t trot_workspace_size(const trot_system* s, int op) {
   Spins sp = make_spins(s);
   Carver c(nullptr, 0);
   StepBuffers b;
+  if (op == TROT_OP_RDM1) return rdm1_workspace_size(s, sp) + 256;
   if (s->precision == TROT_MIXED && op != TROT_OP_SR && op != TROT_OP_QR) {
     if (!s->mixed) return 0;
     return mixed_workspace_size(s, op) + 256;
   }
   size_t n = carve_step(s, sp, c, b, op);
   return n + 256;
+}
+
+int trot_block_rdm1(const trot_system* s, const double* green, const double* weights, const double* obs,
+                    double* rdm1_out, void* ws, size_t ws_bytes, void* stream) {
+  TROT_TRY(check_system(s));
+  if (!green || !weights || !obs || !rdm1_out || !ws) { set_error("null rdm1 buffer"); return TROT_ERR_NULL_PTR; }
+  Spins sp = make_spins(s);
+  const size_t need = rdm1_workspace_size(s, sp) + 256;
+  if (ws_bytes < need) {
+    set_error("workspace too small: %zu < %zu", ws_bytes, need);
+    return TROT_ERR_WORKSPACE_TOO_SMALL;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int W = s->n_walkers, N = s->norb, nchunk = rdm1_chunks(s, sp);
+  const int wchunk = (W + nchunk - 1) / nchunk;
+  double2* part = reinterpret_cast<double2*>(static_cast<char*>(ws) + 256);
+  rdm1_partial_kernel<<<dim3(sp.ntot, nchunk), 128, 0, st>>>(W, sp.ntot, N, wchunk, (const double2*)green, weights,
+                                                            part);
+  TROT_CHECK_LAUNCH("rdm1_partial_kernel");
+  const int nmax = std::max(sp.n[0], sp.n[1]);
+  rdm1_finish_kernel<<<dim3(2, N), 128, (size_t)nmax * sizeof(double2), st>>>(sp, N, nchunk, part, obs,
+                                                                            (double2*)rdm1_out);
+  TROT_CHECK_LAUNCH("rdm1_finish_kernel");
+  return TROT_OK;
 }
 
 int trot_overlap(const trot_system* s, const double* wa, const double* wb, double* out, void* stream) {
