@@ -70,21 +70,24 @@ def flops_per_walker_step_cisd(N, n, G, nterms=6):
 
 
 # DRAM bytes per launch of the dominant kernel, measured by ncu on the named workload (one counter
-# pass; command and table in profiles/dram_traffic_uhf_n120_w1024_mixed.md)
-NCU_DRAM_BYTES = {("cfg2_uhf_n120", "mixed", "exchange_exact_tc"): ((41.47 + 0.26) + (39.87 + 0.02)) / 2 * 1e6}
+# pass; command and numbers in profiles/exchange_exact_tc_uhf_n120_w256.md, full-size launch)
+NCU_DRAM_BYTES = {("cfg2_uhf_n120", "mixed", "exchange_exact_tc"): ((41.464 + 0.320) + (39.818 + 0.017)) / 2 * 1e6}
 
 
 def exchange_tensor_flops(cfg, W):
-    """BF16 tensor flops the exact-slice exchange kernel issues per launch (mean over spins):
-    15 products of 128 x 48 x 128 per (Cholesky block, walker tile)."""
+    """FP16 tensor flops the exact-digit exchange kernel issues per launch (mean over spins):
+    per (128-row Cholesky tile, walker tile of P columns) the 15 digit products t + u <= 4 of
+    128 x P x 128, issued as five MMAs per K16 step with the Green's-function planes stacked
+    along N (P = 48; 32 for n_pad = 16; n_pad = 4, 8, 12 or 16)."""
     N, (na, nb), G = cfg["norb"], cfg["nelec"], cfg["nchol"]
     spins = [na] if cfg["kind"] == "rhf_r" else [na, nb]
     tot = 0
     for n in spins:
-        n_pad = (n + 3) & ~3
-        wb = 48 // (2 * n_pad)
+        n_pad = 4 if n <= 4 else 8 if n <= 8 else 12 if n <= 12 else 16
+        P = 32 if n_pad == 16 else 48
+        wb = P // (2 * n_pad)
         gb = max(1, 128 // n)
-        tot += 15 * 2 * 128 * 48 * 128 * ((W + wb - 1) // wb) * ((G + gb - 1) // gb)
+        tot += 15 * 2 * 128 * P * 128 * ((W + wb - 1) // wb) * ((G + gb - 1) // gb)
     return tot / len(spins)
 
 
@@ -463,13 +466,26 @@ def precision_leg(chol_scale=0.1, n_steps=200, seed=5):
                                   params=params)
         return dict(meas=meas, mctx=mctx, pops=pops, pctx=pctx, st=st)
 
-    runs = {"mixed": setup(True), "fp64": setup(False)}
+    runs = {"mixed": setup(True), "fp64": setup(False), "fp64u": setup(False)}
+    # control: an FP64 run from w U (a random unitary U per walker and spin), mathematically the
+    # same trajectory (G, E_L, force bias, overlap ratios and weights are invariant under w -> w U)
+    # with different rounding: its block energies against the plain FP64 run measure how far FP64
+    # trajectories themselves drift apart
+    gu = torch.Generator().manual_seed(seed + 17)
+
+    def _unitary(w):
+        z = torch.randn((w.shape[0], w.shape[2], w.shape[2]), generator=gu, dtype=torch.complex128)
+        return torch.matmul(w, torch.linalg.qr(z)[0].to(w.device)).contiguous()
+
+    st_u = runs["fp64u"]["st"]
+    wu_rot = tuple(_unitary(w) for w in st_u.walkers)
+    runs["fp64u"]["st"] = st_u._replace(walkers=wu_rot, overlaps=runs["fp64u"]["meas"].overlap(wu_rot, trial))
     obs = torch.empty(2, dtype=torch.float64, device="cuda")
     gen = torch.Generator(device="cuda")
     zetas = np.random.default_rng(seed).uniform(size=n_steps // qr)
     e_mx = torch.empty(W, dtype=torch.complex128, device="cuda")
     d_steps, e_abs = [], []
-    blk = {"mixed_from_mixed_E": [], "mixed_from_fp64_E": [], "fp64_run": []}
+    blk = {"mixed_from_mixed_E": [], "mixed_from_fp64_E": [], "fp64_run": [], "fp64u_run": []}
     t0 = time.perf_counter()
     for b in range(n_steps // qr):
         for k in range(qr):
@@ -482,9 +498,10 @@ def precision_leg(chol_scale=0.1, n_steps=200, seed=5):
                                      energy_out=e_mx)
             d_steps.append((e_mx - e64).abs().cpu().numpy())
             e_abs.append(e64.abs().cpu().numpy())
-            f = runs["fp64"]
-            f["st"] = f["pops"].step(f["st"], params=params, ham_data=ham, trial_data=trial, trial_ops=trial_ops,
-                                     meas_ops=f["meas"], meas_ctx=f["mctx"], prop_ctx=f["pctx"], fields=x)
+            for name in ("fp64", "fp64u"):
+                f = runs[name]
+                f["st"] = f["pops"].step(f["st"], params=params, ham_data=ham, trial_data=trial, trial_ops=trial_ops,
+                                         meas_ops=f["meas"], meas_ctx=f["mctx"], prop_ctx=f["pctx"], fields=x)
         for name, r in runs.items():
             st = r["st"]
             walkers = tg.walkers.orthonormalize_(st.walkers, "unrestricted")
@@ -497,8 +514,8 @@ def precision_leg(chol_scale=0.1, n_steps=200, seed=5):
                 blk["mixed_from_fp64_E"].append(_block_energy_host(e_other.cpu().numpy(), wts, e_ref, dt))
             _lib.call("trot_block_energy", W, e.data_ptr(), st.weights.data_ptr(), st.scalars.data_ptr(), float(dt),
                       float(params.shift_ema), obs.data_ptr(), native.stream_ptr())
-            if name == "fp64":
-                blk["fp64_run"].append(float(obs[0]))
+            if name in ("fp64", "fp64u"):
+                blk[name + "_run"].append(float(obs[0]))
             if name == "mixed":
                 w_sr, wts_sr = tg.walkers.stochastic_reconfiguration(walkers, st.weights, float(zetas[b]),
                                                                      "unrestricted")
@@ -515,7 +532,8 @@ def precision_leg(chol_scale=0.1, n_steps=200, seed=5):
     secs = time.perf_counter() - t0
     d = np.concatenate(d_steps)
     ea = np.concatenate(e_abs)
-    bm, bf, b64 = (np.array(blk[k]) for k in ("mixed_from_mixed_E", "mixed_from_fp64_E", "fp64_run"))
+    bm, bf, b64, b64u = (np.array(blk[k]) for k in ("mixed_from_mixed_E", "mixed_from_fp64_E", "fp64_run",
+                                                    "fp64u_run"))
     wm = runs["mixed"]["st"].walkers[0].cpu().numpy()
     wf = runs["fp64"]["st"].walkers[0].cpu().numpy()
     return {
@@ -540,6 +558,12 @@ def precision_leg(chol_scale=0.1, n_steps=200, seed=5):
         "fp64_run_max_block_energy_diff_mHa": 1e3 * float(np.max(np.abs(bm - b64))),
         "fp64_run_note": "block energies of an independent FP64 run (same fields, zeta and SR selections) "
                          "against the mixed run's, averaged over the blocks",
+        "fp64_control_block_energy_diff_mHa": 1e3 * abs(float(np.mean(b64u)) - float(np.mean(b64))),
+        "fp64_control_block_energy_diff_stderr_mHa": 1e3 * float(np.std(b64u - b64, ddof=1) / np.sqrt(len(b64))),
+        "fp64_control_block_energy_diffs_mHa": [round(1e3 * float(x), 6) for x in (b64u - b64)],
+        "fp64_control_note": "the same comparison between two FP64 runs of the same trajectory (the second from "
+                             "w U, U a random unitary per walker and spin: identical in exact arithmetic): the "
+                             "trajectory-noise floor of FP64 itself",
         "fp64_run_final_walker_rel_diff": float(np.max(np.abs(wm - wf)) / max(np.max(np.abs(wf)), 1e-300)),
         "alive_walkers_end": int((runs["mixed"]["st"].weights > 0).sum().item()),
         "seconds": secs,
@@ -838,7 +862,7 @@ def main():
         roofline["executed_bf16_tflops"] = ex / per_launch_s / 1e12
         roofline["executed_frac"] = ex / per_launch_s / 1e12 / peak
         roofline["traffic_note"] = ("DRAM bytes per launch (mean of the two spin launches) measured by ncu on this "
-                                    "workload: profiles/dram_traffic_uhf_n120_w1024_mixed.md")
+                                    "workload: profiles/exchange_exact_tc_uhf_n120_w256.md")
     step_flops = sum(fl.values()) * W
     kernels = {k: {"ms_total": round(v[0], 4), "launches": v[1], "ms_per_launch": round(v[0] / max(v[1], 1), 5)}
                for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
@@ -866,6 +890,7 @@ def main():
             precision_info["max_abs_dE_L_Ha"] = pw["max_abs_dE_L_Ha"]
             precision_info["block_energy_diff_mHa"] = traj["fp64_run_block_energy_diff_mHa"]
             precision_info["block_energy_diff_stderr_mHa"] = traj["fp64_run_block_energy_diff_stderr_mHa"]
+            precision_info["fp64_control_block_energy_diff_mHa"] = traj["fp64_control_block_energy_diff_mHa"]
             precision_info["on"] = ("200-step trajectory on the headline shapes with live walkers (Cholesky x0.1): "
                                     f"{pw['samples']} per-walker samples of mixed vs FP64 E_L on identical walkers; "
                                     "block energies of an independent FP64 run with the same fields, zeta and SR "

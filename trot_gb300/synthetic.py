@@ -57,11 +57,16 @@ def hamiltonian(norb: int, nchol: int, decay: float = 30.0, seed: int = 0, h0: f
 
 
 def _coulomb(chol, dm):
-    return np.tensordot(np.einsum("gkl,lk->g", chol, dm), chol, axes=1)
+    G = chol.shape[0]
+    return np.tensordot(chol.reshape(G, -1) @ dm.T.reshape(-1), chol, axes=1)
 
 
-def _exchange(chol, dm):
-    return np.einsum("gik,gkj->ij", chol @ dm, chol)
+def _exchange(chol, c):
+    """sum_g L_g (c c^T) L_g for occupied orbitals c (N, n): X X^T with X_g = L_g c,
+    one (N, G n) x (G n, N) product."""
+    G, N, _ = chol.shape
+    x = (chol.reshape(G * N, N) @ c).reshape(G, N, c.shape[1]).transpose(1, 0, 2).reshape(N, G * c.shape[1])
+    return x @ x.T
 
 
 def scf(h1, chol, na: int, nb: int, iters: int = 30):
@@ -73,8 +78,8 @@ def scf(h1, chol, na: int, nb: int, iters: int = 30):
     for _ in range(iters):
         da, db = ca @ ca.T, cb @ cb.T
         j = _coulomb(chol, da + db)
-        fa = h1 + j - _exchange(chol, da)
-        fb = h1 + j - _exchange(chol, db)
+        fa = h1 + j - _exchange(chol, ca)
+        fb = h1 + j - _exchange(chol, cb)
         ca = np.linalg.eigh(fa)[1][:, :na]
         cb = np.linalg.eigh(fb)[1][:, :nb]
     return np.ascontiguousarray(ca), np.ascontiguousarray(cb)
@@ -87,7 +92,7 @@ def scf_rhf_full(h1, chol, n: int, iters: int = 30):
     co = c[:, :n]
     for _ in range(iters):
         d = co @ co.T
-        f = h1 + 2.0 * _coulomb(chol, d) - _exchange(chol, d)
+        f = h1 + 2.0 * _coulomb(chol, d) - _exchange(chol, co)
         eps, c = np.linalg.eigh(f)
         co = c[:, :n]
     return np.ascontiguousarray(c), eps
