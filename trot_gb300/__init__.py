@@ -4,7 +4,7 @@ prop / meas / trial / walker call signatures.
 All compute runs in ``lib/libtrot_gb300.so`` (hand-written CUDA behind the C
 ABI of ``include/trot_gb300.h``); importing the package does not touch the GPU.
 """
-from . import _lib, rng, synthetic
+from . import _lib, h5file, rng, staging, synthetic
 from .blocks import BlockObs, block
 from .core import (HamChol, MeasOps, PropOps, PropState, QmcParams, QmcParamsBase, QmcParamsFp, System,
                    TrialOps, k_energy, k_force_bias)
@@ -21,6 +21,6 @@ __all__ = [
     "k_energy", "k_force_bias", "RhfMeasCtx", "UhfMeasCtx", "build_rhf_meas_ctx", "build_uhf_meas_ctx",
     "make_rhf_meas_ops", "make_uhf_meas_ops", "CholAfqmcCtx", "afqmc_step", "init_prop_state", "make_prop_ops",
     "make_trotter_ops", "RhfTrial", "UhfTrial", "get_rdm1", "make_rhf_trial_ops", "make_uhf_trial_ops",
-    "walkers", "rng", "synthetic", "block", "BlockObs", "CisdTrial", "CisdMeasCtx", "make_cisd_meas_ops",
+    "walkers", "rng", "synthetic", "staging", "h5file", "block", "BlockObs", "CisdTrial", "CisdMeasCtx", "make_cisd_meas_ops",
     "make_cisd_trial_ops", "QmcParamsFp", "afqmc_step_fp", "make_prop_ops_fp",
 ]

@@ -249,6 +249,14 @@ def _rdm1(walkers, ham_data, meas_ctx, trial_data):
     return rdm1_batched(walkers, ham_data, meas_ctx, trial_data)
 
 
+def make_cisd_trial_data(data: dict, sys: System) -> CisdTrial:
+    """trot/trial/cisd.py:203-213."""
+    def count(key):
+        return int(np.asarray(data[key].cpu() if isinstance(data.get(key), torch.Tensor) else data.get(key, 0)).item())
+    return CisdTrial(ci1=data["ci1"], ci2=data["ci2"], nocc_t_core=count("nocc_t_core"),
+                     nvir_t_outer=count("nvir_t_outer"))
+
+
 def make_cisd_trial_ops(sys: System, memory_mode: str = "high") -> TrialOps:
     """trot/trial/cisd.py:189-201."""
     if sys.nup != sys.ndn:
