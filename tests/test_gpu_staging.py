@@ -77,5 +77,12 @@ def test_staged_cisd_vs_oracle():
     e = cpu(meas_ops.kernels["energy"](wd, ham, meas_ctx, trial))
     assert rel(ov, co.overlap(w, tr)) < 1e-11
     fb = cpu(meas_ops.kernels["force_bias"](wd, ham, meas_ctx, trial))
-    assert rel(e, co.energy(w, tr, host.ham.h0, host.ham.h1, host.ham.chol)) < 1e-10
+    e_ref = co.energy(w, tr, host.ham.h0, host.ham.h1, host.ham.chol)
+    # the bundle's meas ops keep the reference's default (testing=False: the l2ci2 quadratic
+    # forms in 32-bit arithmetic, trot/meas/cisd.py:823-839), so the energy is FP32-class
+    assert rel(e, e_ref) < 1e-6
     assert rel(fb, co.force_bias(w, tr, host.ham.chol)) < 1e-10
+    import trot_gb300 as tg
+    m64 = tg.make_cisd_meas_ops(sys_, mixed_precision=False, testing=True)
+    e64 = cpu(m64.kernels["energy"](wd, ham, m64.build_meas_ctx(ham, trial), trial))
+    assert rel(e64, e_ref) < 1e-10

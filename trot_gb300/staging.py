@@ -211,7 +211,7 @@ def _to_device(ds: h5file.Dataset, device: torch.device, chunk_bytes: int) -> to
         host = np.asarray(ds[...])
         if tdt is None:
             raise TypeError(f"{ds.name}: dtype {ds.dtype} has no device counterpart")
-        return torch.from_numpy(np.ascontiguousarray(host)).to(device)
+        return torch.from_numpy(np.array(host, order="C")).to(device)  # a writable copy; keeps 0-d shapes
     off, n = ext
     out = torch.empty(ds.shape, dtype=tdt, device=device)
     flat = out.view(-1).view(torch.uint8)
