@@ -1092,28 +1092,56 @@ __global__ void __launch_bounds__(256) trotter32_kernel(Spins sp, Trot32Args a32
 //   step 0:          T0 = E w                      (E = exp(-dt/2 h1_eff), real)
 //   steps k=1..K:    T_k = (i sqrt(dt)/k) V T_{k-1}, O = T0 + ... + T_K
 //   step K+1:        w' = E O
-// The A operand (128 rows p x K) is streamed from global memory in 32-wide K
-// chunks of 3 BF16 slices (24 KB, 2-stage ring): E (K = 128, 4 chunks, shared by
-// all walkers) or the walker's [Vr | Vi] (K = 256, 8 chunks).  The B operand
-// (NB rows x K, 3 slices) holds the previous term T in shared memory, row 2j
-// giving the real and row 2j + 1 the imaginary part of output column j: for a V
-// step row 2j = [Re T_j ; -Im T_j] and row 2j + 1 = [Im T_j ; Re T_j] over
-// K = [Re rows 0..127 ; Im rows 128..255], for an E step rows 2j / 2j + 1 =
-// Re / Im T_j over K = 128.  3-term BF16 splits of both operands, products
-// t + u <= 2 (6 MMAs per 16-wide K step), FP32 accumulation in TMEM (~2^-24
+// The A operand (128 rows p x K) is streamed from global memory in 32-wide K chunks of
+// 3 BF16 slices (24 KB each): E (K = 128, 4 chunks, shared by all walkers) or the
+// walker's [Vr | Vi] (8 chunks: 0-3 are Vr, 4-7 are Vi).  The B operand (NB rows x
+// K = 128, 3 slices) holds the previous term T in shared memory, row 2j = Re T_j and row
+// 2j + 1 = Im T_j.  A V step accumulates Vr B (chunks 0-3) and Vi B (chunks 4-7) into two
+// TMEM accumulators D1, D2, and the epilogue forms V T = (D1[2j] - D2[2j+1]) +
+// i (D1[2j+1] + D2[2j]); an E step uses D1 only.  3-term BF16 splits of both operands,
+// products t + u <= 2 (6 MMAs per 16-wide K step), FP32 accumulation in TMEM (~2^-24
 // relative, the FP32 path's accuracy).
-// Each CTA carries WPC walkers through the steps in lockstep: while the
-// epilogue turns walker 0's accumulator into its next B operand the tensor core
-// runs walker 1's step, and vice versa.  Warp 8 lane 0 streams A and issues
-// the MMAs; warps 0-7 are the epilogue (warp w: TMEM lanes / orbital rows
-// 32 (w % 4) .., output columns of half w / 4), accumulating O in registers.
-// The new overlaps and phaseless weights are computed afterwards by the FP64
-// determinant kernel (full occupancy) and phaseless_update.
-static constexpr int kTcThreads = 288;
+// Warps: 0-15 epilogue (warp w: TMEM lanes / orbital rows 32 (w % 4) .., output columns of
+// quarter w / 4, accumulating O in registers), warp 16 lane 0 issues the MMAs, warps 17-19
+// lane 0 load A chunks into a ring of kTcStages<NB> slots (chunk c by loader c % 3; bulk copies of
+// different warps are in flight together, copies of one warp complete one after another).
+// Each CTA carries WPC walkers through the steps in lockstep: while the epilogue turns
+// walker 0's accumulators into its next B operand the tensor core runs walker 1's step.
+// The new overlaps and phaseless weights are computed afterwards by the float-float
+// determinant kernel (overlap_weight_ff_kernel).
+static constexpr int kTcLoaders = 3;
+static constexpr int kTcEpi = 512;                              // epilogue threads (16 warps)
+static constexpr int kTcThreads = kTcEpi + 32 * (1 + kTcLoaders);
 static constexpr int kTcKC = 32;                                // K per A / B chunk
 static constexpr uint32_t kTcSlice = 128 * kTcKC * 2;           // 8 KB: one slice of one A chunk
 static constexpr uint32_t kTcChunk = 3 * kTcSlice;              // 24 KB
-static constexpr int kTcStages = 2;
+static constexpr int kTcWPC = 2;                                // walkers per CTA
+static constexpr int kTcMaxStages = 9;
+
+// B operand layout: K-major core matrices (8 rows x 16 B) with the K-adjacent ones 144 B
+// apart (LBO) and 8-row groups 576 B apart (SBO).  The 16 B of padding per core matrix put
+// the four 8-lane groups of an epilogue warp's stores (lanes = K) on distinct banks.
+static constexpr uint32_t kTcBLbo = 144, kTcBSbo = 4 * kTcBLbo;
+__host__ __device__ __forceinline__ uint32_t tc_b_off(int r, int k) {
+  return (uint32_t)((r >> 3) * kTcBSbo + (k >> 3) * kTcBLbo + (r & 7) * 16 + (k & 7) * 2);
+}
+
+template <int NB>
+struct TcShape {
+  static constexpr uint32_t BSlice = (uint32_t)(NB / 8) * kTcBSbo;  // one slice of one K chunk
+  static constexpr uint32_t BBytes = 4u * 3u * BSlice;                // B image of one walker (K = 128)
+  static constexpr size_t budget = 227 * 1024 - 1024 - 128 - (size_t)kTcWPC * BBytes;
+  // a multiple of the loader count, so every ring slot is refilled by one loader only
+  static constexpr int fit = (int)(budget / kTcChunk);
+  static constexpr int Stages = (fit > kTcMaxStages ? kTcMaxStages : fit) / kTcLoaders * kTcLoaders;
+  static constexpr size_t smem = 128 + (size_t)Stages * kTcChunk + (size_t)kTcWPC * BBytes;
+  // per walker two accumulators (Vr / E products, Vi products) of two column blocks each
+  static constexpr int WalkerCols = 4 * NB;
+  static constexpr uint32_t TmemCols = kTcWPC * WalkerCols <= 128 ? 128 : (kTcWPC * WalkerCols <= 256 ? 256 : 512);
+  static_assert(Stages >= kTcLoaders, "tensor-core Trotter: ring");
+  static_assert(smem <= 227 * 1024, "tensor-core Trotter shared memory");
+  static_assert(kTcWPC * WalkerCols <= 512, "tensor-core Trotter TMEM columns");
+};
 
 struct TrotTcArgs {
   TrotterArgs t;
@@ -1132,48 +1160,63 @@ __device__ __forceinline__ void split3_bf16(float x, uint16_t& h, uint16_t& m, u
   l = *reinterpret_cast<const uint16_t*>(&bl);
 }
 
-// B element (row j, k) = x as 3 slices; B image = [kchunk][slice][NB rows][32]
+// B element (row j, k < 128) = x as 3 slices; B image = [kchunk][slice][NB rows][32]
 template <int NB>
 __device__ __forceinline__ void put_b(unsigned char* B, int j, int k, float x) {
   uint16_t h, m, l;
   split3_bf16(x, h, m, l);
-  constexpr uint32_t sl = (uint32_t)NB * kTcKC * 2;  // bytes of one slice of one chunk
-  unsigned char* c = B + (size_t)(k / kTcKC) * 3 * sl + tc::tile_off32(j, k % kTcKC);
+  constexpr uint32_t sl = TcShape<NB>::BSlice;  // bytes of one slice of one chunk
+  unsigned char* c = B + (size_t)(k / kTcKC) * 3 * sl + tc_b_off(j, k % kTcKC);
   *reinterpret_cast<uint16_t*>(c) = h;
   *reinterpret_cast<uint16_t*>(c + sl) = m;
   *reinterpret_cast<uint16_t*>(c + 2 * sl) = l;
 }
 
-template <int NBT, int WPC>
+// A chunk c of a CTA's sequence (steps x walkers x chunks): the source image address.
+__device__ __forceinline__ const uint16_t* tc_chunk_src(const TrotTcArgs& g, int b0, int step, int wi, int kc,
+                                                        int nterms) {
+  const bool vterm = step > 0 && step <= nterms;
+  return vterm ? g.vimg + ((size_t)(b0 + wi) * 8 + kc) * (kTcChunk / 2) : g.eimg + (size_t)kc * (kTcChunk / 2);
+}
+
+template <int NB>
 __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, TrotTcArgs g) {
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bars[4 + 2 * WPC];
+  using X = TcShape<NB>;
+  constexpr int WPC = kTcWPC, S = X::Stages, NH = NB / 8;  // complex output columns per epilogue thread
+  constexpr uint32_t kBBytes = X::BBytes;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bars[2 * kTcMaxStages + 2 * WPC + 1];
   __shared__ uint32_t tslot;
-  constexpr int NB = NBT, NH = NBT / 4;          // complex output columns per epilogue half
-  constexpr uint32_t kBBytes = 8u * 3u * NB * kTcKC * 2u;
-  unsigned char* base = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
-  unsigned char* Abuf = base;                                  // kTcStages x 24 KB
-  unsigned char* Bbuf = base + kTcStages * kTcChunk;           // WPC x kBBytes
-  uint64_t* full = bars;             // [2]
-  uint64_t* empty = bars + 2;        // [2]
-  uint64_t* acc_full = bars + 4;     // [WPC]
-  uint64_t* b_ready = bars + 4 + WPC;  // [WPC]
+  __shared__ volatile int abort_flag;
+  __shared__ float coefs[18];  // sqrt(dt) / k rounded once from FP64 (the FP64 pipe is narrow: one division per k)
+  // no swizzling: 128-byte alignment serves the bulk copies and the descriptors
+  unsigned char* base = smem_raw + ((128 - (tc::smem_u32(smem_raw) & 127)) & 127);
+  unsigned char* Abuf = base;                          // S x 24 KB
+  unsigned char* Bbuf = base + (size_t)S * kTcChunk;   // WPC x kBBytes
+  uint64_t* full = bars;                 // [S] an A chunk has landed
+  uint64_t* empty = bars + S;            // [S] the MMAs reading the slot are done
+  uint64_t* acc_full = bars + 2 * S;     // [WPC]
+  uint64_t* b_ready = acc_full + WPC;    // [WPC]
+  uint64_t* drain = b_ready + WPC;       // the abort path's commit
   const TrotterArgs& a = g.t;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int N = a.N, nc = sp.ntot, nterms = a.nterms;
   const int nsteps = nterms + 2;  // E, V x nterms, E
   const int b0 = blockIdx.x * WPC;
   const int nw = min(WPC, a.W - b0);
-  if (warp == 8) tc::tmem_alloc(&tslot, WPC * 64);
-  if (tid == 256) {
-    for (int k = 0; k < 2; ++k) {
+  if (warp == 16) tc::tmem_alloc(&tslot, X::TmemCols);
+  if (tid < 18) coefs[tid] = tid == 0 ? 1.f : (float)(a.sqrt_dt / (double)tid);
+  if (tid == kTcEpi) {
+    for (int k = 0; k < S; ++k) {
       tc::mbar_init(&full[k], 1);
       tc::mbar_init(&empty[k], 1);
     }
     for (int wi = 0; wi < WPC; ++wi) {
       tc::mbar_init(&acc_full[wi], 1);
-      tc::mbar_init(&b_ready[wi], 256);
+      tc::mbar_init(&b_ready[wi], kTcEpi);
     }
+    tc::mbar_init(drain, 1);
+    abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   {  // zero the B images: padding rows (j >= 2 nc) and K rows (p >= N) stay zero
@@ -1185,46 +1228,45 @@ __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, Tro
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = tslot;
-  if (warp == 8) {
+  if (warp == 16) {
+    // ------------------------------------------------ MMA issuer
     if (lane == 0) {
       bool ok = true;
-      const uint32_t idesc = tc::idesc_bf16_f32(128, NB);
+      const uint32_t idesc2 = tc::idesc_bf16_f32(128, 2 * NB), idesc1 = tc::idesc_bf16_f32(128, NB);
       const uint32_t sa = tc::smem_u32(Abuf), sb = tc::smem_u32(Bbuf);
-      constexpr uint32_t bsl = (uint32_t)NB * kTcKC * 2;
-      int chunk = 0;
+      constexpr uint32_t bsl = X::BSlice;
+      const uint32_t bhi = (uint32_t)(tc::smem_desc(sb, kTcBLbo, kTcBSbo) >> 32);
+      int c = 0;
       for (int step = 0; step < nsteps && ok; ++step) {
         const bool vterm = step > 0 && step <= nterms;
         const int nk = vterm ? 8 : 4;
         for (int wi = 0; wi < nw && ok; ++wi) {
-          const uint16_t* vimg = g.vimg + (size_t)(b0 + wi) * 8 * (kTcChunk / 2);
           const uint32_t bw = sb + (uint32_t)wi * kBBytes;
-          for (int kc = 0; kc < nk && ok; ++kc, ++chunk) {
-            const int st = chunk & 1;
-            if (chunk >= 2) ok = tc::mbar_wait(&empty[st], (uint32_t)(((chunk - 2) >> 1) & 1));
-            if (!ok) break;
-            const uint16_t* src = (vterm ? vimg : g.eimg) + (size_t)kc * (kTcChunk / 2);
-            tc::mbar_expect_tx(&full[st], kTcChunk);
-            tc::bulk_g2s(Abuf + (size_t)st * kTcChunk, src, kTcChunk, &full[st]);
-            if (kc == 0) {  // this walker's B operand for the step is written by the epilogue
-              ok = tc::mbar_wait(&b_ready[wi], (uint32_t)(step & 1));
-              if (!ok) break;
-            }
-            ok = tc::mbar_wait(&full[st], (uint32_t)((chunk >> 1) & 1));
+          // this walker's B operand for the step is written by the epilogue
+          ok = tc::mbar_wait(&b_ready[wi], (uint32_t)(step & 1));
+          for (int kc = 0; kc < nk && ok; ++kc, ++c) {
+            const int st = c % S;
+            ok = tc::mbar_wait(&full[st], (uint32_t)((c / S) & 1));
             if (!ok) break;
             tc::fence_after_sync();
             const uint64_t a0 = tc::smem_desc(sa + (uint32_t)st * kTcChunk, 128, 512);
-            const uint32_t alo = (uint32_t)a0, dhi = (uint32_t)(a0 >> 32);  // A and B share the high word
-            const uint32_t blo = (uint32_t)tc::smem_desc(bw + (uint32_t)kc * 3 * bsl, 128, 512);
-            const uint32_t dcol = taddr + (uint32_t)(wi * 64);
+            const uint32_t alo = (uint32_t)a0, ahi = (uint32_t)(a0 >> 32);
+            const int kb = kc & 3;
+            const uint32_t blo = (uint32_t)tc::smem_desc(bw + (uint32_t)kb * 3 * bsl, kTcBLbo, kTcBSbo);
+            const uint32_t dcol = taddr + (uint32_t)(wi * X::WalkerCols + (kc >= 4 ? 2 * NB : 0));
+            // B slices 0 and 1 are adjacent rows of the B image, so one MMA of N = 2 NB takes both
+            // (TMEM blocks X, Y of the accumulator): A_t [B_0; B_1] for t = 0, 1, 2, then A_0 B_2 into
+            // block X.  Products t + u <= 2 plus A_2 B_1; four MMAs per 16-wide K step, each reading
+            // its A slice once (the per-MMA A read from shared memory is what bounds these MMAs).
 #pragma unroll
-            for (int t = 0; t < 3; ++t)
+            for (int ks = 0; ks < kTcKC / 16; ++ks) {
+              const uint32_t ak = alo + (uint32_t)((ks * 256) >> 4), bk = blo + (uint32_t)((ks * 2 * kTcBLbo) >> 4);
 #pragma unroll
-              for (int u = 0; t + u <= 2; ++u)
-#pragma unroll
-                for (int ks = 0; ks < kTcKC / 16; ++ks)
-                  tc::mma_bf16_lo(dcol, alo + (uint32_t)((t * kTcSlice + ks * 256) >> 4),
-                                  blo + (uint32_t)((u * bsl + ks * 256) >> 4), dhi, idesc,
-                                  (kc | t | u | ks) ? 1u : 0u);
+              for (int t = 0; t < 3; ++t)
+                tc::mma_bf16_lo2(dcol, ak + (uint32_t)((t * kTcSlice) >> 4), ahi, bk, bhi, idesc2,
+                                 (kb | ks | t) ? 1u : 0u);
+              tc::mma_bf16_lo2(dcol, ak, ahi, bk + (uint32_t)((2 * bsl) >> 4), bhi, idesc1, 1u);
+            }
             tc::mma_commit(&empty[st]);
           }
           if (ok) tc::mma_commit(&acc_full[wi]);
@@ -1232,9 +1274,49 @@ __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, Tro
       }
       if (!ok) {
         report_timeout(g.status);
-        // let copies / MMAs already issued land before the tensor memory is released
-        for (int k = 0; k < 2; ++k) tc::mbar_wait(&empty[k], 0u, 1000000u);
-        for (int k = 0; k < 2; ++k) tc::mbar_wait(&full[k], 0u, 1000000u);
+        abort_flag = 1;
+        // the MMAs already issued complete before the epilogue is released and TMEM is freed
+        tc::mma_commit(drain);
+        tc::mbar_wait(drain, 0u, 1000000u);
+        for (int wi = 0; wi < WPC; ++wi) tc::mbar_arrive(&acc_full[wi]);
+      }
+    }
+    __syncwarp();
+  } else if (warp > 16) {
+    // ------------------------------------------------ loaders: chunk c by loader c % kTcLoaders
+    if (lane == 0) {
+      const int w = warp - 17;
+      bool ok = true;
+      int last = -1;  // this loader's last issued chunk
+      int c = 0;
+      for (int step = 0; step < nsteps && ok; ++step) {
+        const int nk = (step > 0 && step <= nterms) ? 8 : 4;
+        for (int wi = 0; wi < nw && ok; ++wi)
+          for (int kc = 0; kc < nk; ++kc, ++c) {
+            if (c % kTcLoaders != w) continue;
+            const int st = c % S;
+            if (c >= S) {  // the MMAs of chunk c - S have read the slot
+              const uint32_t par = (uint32_t)(((c / S) - 1) & 1);
+              uint32_t polls = 0;
+              while (!tc::mbar_try_wait(&empty[st], par))  // suspends between polls
+                if (abort_flag || ++polls > 20000000u) {
+                  ok = false;
+                  break;
+                }
+              if (!ok) break;
+            }
+            tc::mbar_expect_tx(&full[st], kTcChunk);
+            tc::bulk_g2s(Abuf + (size_t)st * kTcChunk, tc_chunk_src(g, b0, step, wi, kc, nterms), kTcChunk,
+                         &full[st]);
+            last = c;
+          }
+      }
+      if (!ok) {
+        if (!abort_flag) report_timeout(g.status);
+        // bounded drain of this loader's copies in flight (its slots are its own: S is a
+        // multiple of the loader count) before the CTA releases its shared memory
+        for (int u = last; u >= 0 && u > last - S; u -= kTcLoaders)
+          tc::mbar_wait(&full[u % S], (uint32_t)((u / S) & 1), 1000000u);
       }
     }
     __syncwarp();
@@ -1260,8 +1342,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, Tro
           const int s = j < sp.n[0] ? 0 : 1, n = s ? sp.n[1] : sp.n[0], col = s ? j - sp.off[1] : j;
           const double2* w = (s == 0 ? a.in_a : a.in_b) + (size_t)b * N * n;
           const double2 x = prow ? w[(size_t)p * n + col] : make_double2(0.0, 0.0);
-          put_b<NB>(B, 2 * j, p, (float)x.x);
-          put_b<NB>(B, 2 * j + 1, p, (float)x.y);
+          put_b<NB>(B, 2 * j, p, d2f_bits(x.x));
+          put_b<NB>(B, 2 * j + 1, p, d2f_bits(x.y));
         }
       }
       tc::fence_proxy_async();
@@ -1270,29 +1352,51 @@ __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, Tro
     }
     bool ok = true;
     for (int step = 0; step < nsteps && ok; ++step) {
+      const bool vterm = step > 0 && step <= nterms;
       const bool next_is_v = step < nterms;  // the operand built now feeds a V step
-      const float coef = step == 0 ? 1.f : (float)(a.sqrt_dt / (double)step);
+      const float coef = coefs[step < 18 ? step : 0];
 #pragma unroll
       for (int wi = 0; wi < WPC; ++wi) {
         if (wi >= nw) break;
-        if (!tc::mbar_wait(&acc_full[wi], (uint32_t)(step & 1))) {
-          report_timeout(g.status);
+        if (!tc::mbar_wait(&acc_full[wi], (uint32_t)(step & 1)) || abort_flag) {
+          if (!abort_flag) report_timeout(g.status);
           ok = false;
           break;
         }
         tc::fence_after_sync();
         float d[2 * NH];
-        const uint32_t tl = taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(wi * 64 + h * 2 * NH);
-        {  // all column groups in flight, one wait
-          uint32_t raw[2 * NH];
+        const uint32_t tl = taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(wi * X::WalkerCols + h * 2 * NH);
+        {  // accumulator = block X + block Y
+          uint32_t rx[2 * NH], ry[2 * NH];
 #pragma unroll
-          for (int c = 0; c < 2 * NH; c += 8) tc::tmem_ld8_raw(tl + c, raw + c);
+          for (int c = 0; c < 2 * NH; c += 4) {
+            tc::tmem_ld4_raw(tl + c, rx + c);
+            tc::tmem_ld4_raw(tl + NB + c, ry + c);
+          }
           tc::tmem_wait_ld();
 #pragma unroll
           for (int c = 0; c < 2 * NH; ++c) {
-            uint32_t v = raw[c];
-            asm volatile("" : "+r"(v));  // consume after tcgen05.wait::ld
-            d[c] = __uint_as_float(v);
+            uint32_t x = rx[c], y = ry[c];
+            asm volatile("" : "+r"(x), "+r"(y));  // consume after tcgen05.wait::ld
+            d[c] = __uint_as_float(x) + __uint_as_float(y);
+          }
+          if (vterm) {  // the Vi accumulator
+#pragma unroll
+            for (int c = 0; c < 2 * NH; c += 4) {
+              tc::tmem_ld4_raw(tl + 2 * NB + c, rx + c);
+              tc::tmem_ld4_raw(tl + 3 * NB + c, ry + c);
+            }
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int jj = 0; jj < NH; ++jj) {
+              uint32_t xr = rx[2 * jj], xi = rx[2 * jj + 1], yr = ry[2 * jj], yi = ry[2 * jj + 1];
+              asm volatile("" : "+r"(xr), "+r"(xi), "+r"(yr), "+r"(yi));
+              const float vr = __uint_as_float(xr) + __uint_as_float(yr), vi = __uint_as_float(xi) + __uint_as_float(yi);
+              // V T = (Vr Tr - Vi Ti) + i (Vr Ti + Vi Tr)
+              const float re = d[2 * jj] - vi, im = d[2 * jj + 1] + vr;
+              d[2 * jj] = re;
+              d[2 * jj + 1] = im;
+            }
           }
         }
         const int b = b0 + wi;
@@ -1318,15 +1422,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, Tro
             else { tr = -coef * d[2 * jj + 1]; ti = coef * d[2 * jj]; }
             orr[wi][jj] += tr;
             oi[wi][jj] += ti;
-            if (next_is_v) {
-              put_b<NB>(B, 2 * j, p, tr);
-              put_b<NB>(B, 2 * j, 128 + p, -ti);
-              put_b<NB>(B, 2 * j + 1, p, ti);
-              put_b<NB>(B, 2 * j + 1, 128 + p, tr);
-            } else {
-              put_b<NB>(B, 2 * j, p, orr[wi][jj]);
-              put_b<NB>(B, 2 * j + 1, p, oi[wi][jj]);
-            }
+            put_b<NB>(B, 2 * j, p, next_is_v ? tr : orr[wi][jj]);
+            put_b<NB>(B, 2 * j + 1, p, next_is_v ? ti : oi[wi][jj]);
           }
         }
         tc::fence_proxy_async();
@@ -1338,7 +1435,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) trotter_tc_kernel(Spins sp, Tro
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 8) tc::tmem_dealloc(taddr, WPC * 64);
+  if (warp == 16) tc::tmem_dealloc(taddr, X::TmemCols);
 }
 
 // [Vr | Vi] of every walker as the A image of trotter_tc_kernel: (W, 8 chunks, 3 slices, 128 rows, 32)
@@ -1601,12 +1698,11 @@ static int run_trotter32(const trot_system* s, const Spins& sp, const TrotterArg
   return TROT_OK;
 }
 
-template <int NBT, int WPC>
+template <int NB>
 static void trotter_tc_launch(const Spins& sp, const TrotTcArgs& g, int W, cudaStream_t st) {
-  constexpr size_t smem = 1024 + kTcStages * (size_t)kTcChunk + WPC * (8u * 3u * NBT * kTcKC * 2u);
-  static_assert(smem <= 227 * 1024, "tensor-core Trotter shared memory");
-  cudaFuncSetAttribute(trotter_tc_kernel<NBT, WPC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  trotter_tc_kernel<NBT, WPC><<<(W + WPC - 1) / WPC, kTcThreads, smem, st>>>(sp, g);
+  constexpr size_t smem = TcShape<NB>::smem;
+  cudaFuncSetAttribute(trotter_tc_kernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  trotter_tc_kernel<NB><<<(W + kTcWPC - 1) / kTcWPC, kTcThreads, smem, st>>>(sp, g);
 }
 
 static int run_trotter_tc(const trot_system* s, const Spins& sp, const TrotterArgs& t, const MixedBuffers& m,
@@ -1632,10 +1728,10 @@ static int run_trotter_tc(const trot_system* s, const Spins& sp, const TrotterAr
   g.status = m.status;
   TROT_TIMED("trotter_tc", st, ([&]() -> int {
     switch (NB) {
-      case 16: trotter_tc_launch<16, 2>(sp, g, W, st); break;
-      case 32: trotter_tc_launch<32, 2>(sp, g, W, st); break;
-      case 48: trotter_tc_launch<48, 2>(sp, g, W, st); break;
-      default: trotter_tc_launch<64, 1>(sp, g, W, st); break;
+      case 16: trotter_tc_launch<16>(sp, g, W, st); break;
+      case 32: trotter_tc_launch<32>(sp, g, W, st); break;
+      case 48: trotter_tc_launch<48>(sp, g, W, st); break;
+      default: trotter_tc_launch<64>(sp, g, W, st); break;
     }
     TROT_CHECK_LAUNCH("trotter_tc_kernel");
     return TROT_OK;

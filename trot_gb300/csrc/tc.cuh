@@ -218,6 +218,13 @@ __device__ __forceinline__ void tmem_ld8_raw(uint32_t taddr, uint32_t* r) {
                : "r"(taddr));
 }
 
+// 4 consecutive columns without the wait (same rules as tmem_ld8_raw).
+__device__ __forceinline__ void tmem_ld4_raw(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+}
+
 // Byte offset of element (row r, k) inside a [rows x 32] K-major tile (8-row
 // groups 512 B apart, k groups 128 B apart): descriptor LBO 128, SBO 512.
 __host__ __device__ __forceinline__ uint32_t tile_off32(int r, int k) {
