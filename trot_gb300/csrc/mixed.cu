@@ -137,8 +137,10 @@ static constexpr int kGroups = 5;     // accumulators for t + u = 0..4
 static constexpr int kSlices = 5;
 static constexpr int kMaxOcc = 16;    // largest n the exchange epilogue handles
 // FP16 digit format of the exact product (trot_mixed.digit_format 2): Cholesky rows
-// 2^eA sum_t qA_t 2^-(9 + 9t), Green's-function rows 2^eB sum_u qB_u 2^-(8 + 9u);
-// digit products of order d = t + u carry 2^(eA + eB - 17 - 9d).  Both operands are
+// 2^eA sum_t qA_t 2^-(9 + 9t), Green's-function rows 2^eB sum_u qB_u 2^-(8 + 9u), five
+// planes each; digit products of order d = t + u carry 2^(eA + eB - 17 - 9d).  Four planes
+// (products d <= 3) are not enough: the exchange sum cancels strongly, and the error of
+// the individual terms (2^-35 of their size) reached 3e-5 Ha on walkers near the trial.  Both operands are
 // stored per K16 step: [plane][rows][16] blocks in core-matrix order (see tile16_idx).
 static constexpr int kDigitFormat = 2;
 static constexpr int kRotTopBits = 9, kGreenTopBits = 8, kLowBits = 9;
@@ -369,8 +371,11 @@ static constexpr int kExLoaders = 2;     // loader warps: bulk copies issued by 
 static constexpr int kExThreads = 32 * (18 + kExLoaders);  // 16 epilogue warps, the MMA warp, the reducer, the loaders
 static constexpr int kExEpi = 512;      // epilogue threads
 static constexpr int kExSync = 544;     // epilogue + reducer: the per-tile and per-walker barriers
-static constexpr int kExKU = 2;         // K16 steps per ring unit (one bulk copy; larger copies stream faster)
-static constexpr int kExSlots = 2;      // ring of Green's-function units
+static constexpr int kExKU = 1;         // K16 steps per ring unit (one 7.5 KB bulk copy at P = 48)
+static constexpr int kExSlots = 4;      // ring of Green's-function units (two per loader warp)
+// unit g goes to slot g % kExSlots and loader g % kExLoaders: every slot is refilled by one loader only,
+// which the loaders' bounded drain on the timeout path relies on
+static_assert(kExSlots % kExLoaders == 0, "exchange kernel: ring slots per loader");
 
 // One epilogue warp's exchange sum of a walker: fixed-point values V[c] with scale 2^-s[c]
 // (s[c] = kExNonFinite: a lane's value was not finite).
@@ -637,6 +642,18 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
       const float sa = pow2f(a.rot_e[(size_t)blk * 128 + r] - kRotTopBits);
       for (int it = 0; it < ntl; ++it, ++tgl) {
         const int tile = t0 + it, buf = tgl & 1;
+        // this thread's Green's-function exponents of the tile, loaded before the accumulator wait
+        // (green_e holds P entries for every tile, so the loads stay in bounds for partial tiles)
+        int ebr[WBT][JH][2];
+        if (!reducer) {
+          const int32_t* eB = a.green_e + (size_t)tile * P;
+#pragma unroll
+          for (int bl = 0; bl < WBT; ++bl)
+#pragma unroll
+            for (int jj = 0; jj < JH; ++jj)
+#pragma unroll
+              for (int c = 0; c < 2; ++c) ebr[bl][jj][c] = __ldg(eB + bl * 2 * NP + 2 * (j0 + jj) + c);
+        }
         if (tid == 0) *flag = (tc::mbar_wait(&acc_full[buf], (uint32_t)((tgl >> 1) & 1)) && *abort_flag == 0) ? 1 : 0;
         tc::named_bar(1, kExSync);
         if (!*flag) {
@@ -646,8 +663,7 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
         }
         tc::fence_after_sync();
         const int nw = min(WBT, a.W - tile * WBT);
-        const int32_t* eB = a.green_e + (size_t)tile * P;
-#pragma unroll 1
+#pragma unroll
         for (int bl = 0; bl < WBT; ++bl) {
           if (bl >= nw) break;  // uniform across the CTA
           const int b = tile * WBT + bl;
@@ -678,12 +694,12 @@ __global__ void __launch_bounds__(kExThreads, 1) exchange_exact_kernel(ExArgs a)
                 }
                 // sum_d 2^(-9 d) A_d: the 2^-9d scalings are exact, the leading pair error-free
                 ff x = ff_two_sum(g[0], g[1] * 1.953125e-03f);
-                float lo = x.lo + g[2] * 3.814697265625e-06f;
-                lo += g[3] * 7.450580596923828125e-09f;
-                lo += g[4] * 1.4551915228366852e-11f;
+                float lo = x.lo;
+#pragma unroll
+                for (int d = 2; d < kGroups; ++d) lo += g[d] * pow2f(-9 * d);
                 x = ff_fast(x.hi, lo);
                 // times 2^(eA - 9) 2^(eB - 8), as two exact power-of-two factors
-                const float sb = pow2f(eB[cb + 2 * jj + c] - kGreenTopBits);
+                const float sb = pow2f(ebr[bl][jj][c] - kGreenTopBits);
                 (c == 0 ? sFr : sFi)[r * FS + j0 + jj] = ff{x.hi * sa * sb, x.lo * sa * sb};
               }
           }
