@@ -99,6 +99,90 @@ struct Spins {
 // memory (row-major, leading dimension ld), executed by the whole block.
 // Returns det(A) to all threads; A is overwritten by its LU factors.
 // If `inv` is non-null it receives A^{-1} (Gauss-Jordan on [A | I]).
+// One warp, an n x n matrix A (row stride n) in shared memory, partial pivoting (the first
+// largest |A[i][k]| wins, as in block_gauss_jordan).  Returns det(A).  With `inverse`, A is
+// overwritten by its inverse (in-place Gauss-Jordan: each pivot step updates the n x n working
+// array once, half the work of eliminating [A | I]; the row interchanges are undone as column
+// interchanges in reverse order at the end, `perm` holds n ints of scratch); without it, A
+// holds its LU factors.  Phases are separated by __syncwarp, so no CTA barrier is involved.
+// The determinant is returned in lane 0.
+TROT_D double2 warp_gauss_jordan(double2* A, int n, bool inverse, int* perm) {
+  const int lane = threadIdx.x & 31;
+  double2 det = cmk(1.0, 0.0);
+  for (int k = 0; k < n; ++k) {
+    double best = -1.0;
+    int bi = k;
+    for (int i = k + lane; i < n; i += 32) {
+      const double a = cabs2(A[i * n + k]);
+      if (a > best) { best = a; bi = i; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (bi != k) {
+      for (int j = lane; j < n; j += 32) {
+        const double2 t = A[k * n + j];
+        A[k * n + j] = A[bi * n + j];
+        A[bi * n + j] = t;
+      }
+      det = cmk(-det.x, -det.y);
+    }
+    if (inverse && lane == 0) perm[k] = bi;
+    __syncwarp();
+    // the pivot's reciprocal and the running determinant by lane 0 only (the FP64 pipe is
+    // narrow: an FP64 division issued by the whole warp costs as much as an elimination step)
+    double2 rp = cmk(0.0, 0.0);
+    if (lane == 0) {
+      const double2 piv = A[k * n + k];
+      det = cmul(det, piv);
+      rp = cdiv(cmk(1.0, 0.0), piv);
+    }
+    rp.x = __shfl_sync(0xffffffffu, rp.x, 0);
+    rp.y = __shfl_sync(0xffffffffu, rp.y, 0);
+    if (inverse) {
+      __syncwarp();
+      for (int j = lane; j < n; j += 32) A[k * n + j] = j == k ? rp : cmul(A[k * n + j], rp);
+      __syncwarp();
+      // A[i][j] -= A[i][k] A[k][j] for i != k, j != k (the (n-1)^2 elements, row / column k
+      // skipped by the index map); then column k: A[i][k] = -A[i][k] rp
+      const int m = n - 1;
+      for (int e = lane; e < m * m; e += 32) {
+        int i = e / m, j = e - (e / m) * m;
+        i += i >= k;
+        j += j >= k;
+        A[i * n + j] = csub(A[i * n + j], cmul(A[i * n + k], A[k * n + j]));
+      }
+      __syncwarp();
+      for (int i = lane; i < n; i += 32)
+        if (i != k) A[i * n + k] = cmul(cmk(-A[i * n + k].x, -A[i * n + k].y), rp);
+    } else {
+      for (int i = k + 1 + lane; i < n; i += 32) A[i * n + k] = cmul(A[i * n + k], rp);
+      __syncwarp();
+      const int m = n - k - 1;
+      for (int e = lane; e < m * m; e += 32) {
+        const int i = k + 1 + e / m, j = k + 1 + (e - (e / m) * m);
+        A[i * n + j] = csub(A[i * n + j], cmul(A[i * n + k], A[k * n + j]));
+      }
+    }
+    __syncwarp();
+  }
+  if (inverse) {
+    for (int k = n - 1; k >= 0; --k) {
+      const int p = perm[k];
+      if (p != k)
+        for (int i = lane; i < n; i += 32) {
+          const double2 t = A[i * n + k];
+          A[i * n + k] = A[i * n + p];
+          A[i * n + p] = t;
+        }
+      __syncwarp();
+    }
+  }
+  return det;
+}
+
 TROT_D double2 block_gauss_jordan(double2* A, int n, int ld, double2* inv, int* piv_s, double2* red) {
   const int tid = threadIdx.x, nt = blockDim.x;
   if (inv) {

@@ -19,6 +19,8 @@
 
 namespace trot {
 
+static constexpr int kMaxOccGJ = 16;  // largest n of the warp Gauss-Jordan kernels (perm scratch)
+
 // ------------------------------------------------------------------ Green's functions in float-float
 // Same quantities as green_kernel (green.cu): M_s = C_s^T w_s, M_s^{-1} by FP64
 // Gauss-Jordan, G_s = (w_s M_s^{-1})^T and e1 = sum_s mult_s sum G_s o rot_h1_s, with
@@ -30,14 +32,13 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
                 double2* __restrict__ green, double2* __restrict__ e1_out) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ double2 red[32];
-  __shared__ int piv;
+  __shared__ int perm[kMaxOccGJ];
   const int b = blockIdx.x, s = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
   const int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
   ffc* Wf = reinterpret_cast<ffc*>(smem_raw);                    // N x n
   ff* Cf = reinterpret_cast<ff*>(Wf + (size_t)N * nmax);          // N x n
-  double2* Md = reinterpret_cast<double2*>(Cf + (size_t)N * nmax + ((N * nmax) & 1));  // n x n
-  double2* Mi = Md + nmax * nmax;                                 // n x n
-  ffc* Mif = reinterpret_cast<ffc*>(Mi + nmax * nmax);            // n x n
+  double2* Md = reinterpret_cast<double2*>(Cf + (size_t)N * nmax + ((N * nmax) & 1));  // n x n, then M^{-1}
+  ffc* Mif = reinterpret_cast<ffc*>(Md + nmax * nmax);            // n x n
   ff e1r{0.f, 0.f}, e1i{0.f, 0.f};
   {
     const int n = s ? sp.n[1] : sp.n[0];
@@ -82,8 +83,10 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
       Md[e] = make_double2(ff_d(sr), ff_d(si));
     }
     __syncthreads();
-    block_gauss_jordan(Md, n, n, Mi, &piv, red);
-    for (int e = tid; e < n * n; e += nt) Mif[e] = ffc{ff_from_d(Mi[e].x), ff_from_d(Mi[e].y)};
+    // M^{-1} in place, FP64, by one warp (warp-synchronous phases; the other warps wait here)
+    if (tid < 32) warp_gauss_jordan(Md, n, true, perm);
+    __syncthreads();
+    for (int e = tid; e < n * n; e += nt) Mif[e] = ffc{ff_from_d(Md[e].x), ff_from_d(Md[e].y)};
     __syncthreads();
     const double* H = s ? sp.rot_h1[1] : sp.rot_h1[0];
     double2* gout = green + (size_t)b * sp.ntot * N + (size_t)(s ? sp.off[1] : 0) * N;
@@ -118,7 +121,11 @@ green_ff_kernel(Spins sp, int N, const double2* __restrict__ wa, const double2* 
 static int launch_green_ff(const Spins& sp, int W, int N, const double2* wa, const double2* wb, double2* green,
                            double2* e1_out, cudaStream_t st) {
   const int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
-  const size_t smem = (size_t)N * nmax * (sizeof(ffc) + sizeof(ff)) + 16 + (size_t)nmax * nmax * 3 * 16;
+  const size_t smem = (size_t)N * nmax * (sizeof(ffc) + sizeof(ff)) + 16 + (size_t)nmax * nmax * 2 * 16;
+  if (nmax > kMaxOccGJ) {
+    set_error("green_ff: nocc %d > %d", nmax, kMaxOccGJ);
+    return TROT_ERR_UNSUPPORTED;
+  }
   if (smem > 200 * 1024) {
     set_error("green_ff: %zu bytes of shared memory needed", smem);
     return TROT_ERR_UNSUPPORTED;
@@ -1499,8 +1506,6 @@ __global__ void tc_weight_kernel(TrotterArgs a, const double2* __restrict__ ov_n
 // overlap_weight_finish_kernel multiplies the spins and applies phaseless_update.
 __global__ void __launch_bounds__(256) overlap_weight_ff_kernel(Spins sp, TrotterArgs a, double2* __restrict__ ovp) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  __shared__ double2 red[32];
-  __shared__ int piv;
   const int b = blockIdx.x, s = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
   const int N = a.N;
   const int nmax = sp.n[0] > sp.n[1] ? sp.n[0] : sp.n[1];
@@ -1546,8 +1551,10 @@ __global__ void __launch_bounds__(256) overlap_weight_ff_kernel(Spins sp, Trotte
     Md[e] = make_double2(ff_d(sr), ff_d(si));
   }
   __syncthreads();
-  const double2 det = block_gauss_jordan(Md, n, n, nullptr, &piv, red);
-  if (tid == 0) ovp[(size_t)s * a.W + b] = (s ? sp.mult[1] : sp.mult[0]) == 2 ? cmul(det, det) : det;
+  if (tid < 32) {  // LU determinant in FP64 by one warp
+    const double2 det = warp_gauss_jordan(Md, n, false, nullptr);
+    if (tid == 0) ovp[(size_t)s * a.W + b] = (s ? sp.mult[1] : sp.mult[0]) == 2 ? cmul(det, det) : det;
+  }
 }
 
 // overlap = prod_s det(M_s)^mult_s, then the phaseless weight update
