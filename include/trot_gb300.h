@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define TROT_ABI_VERSION 3
+#define TROT_ABI_VERSION 4
 
 typedef enum {
   TROT_OK = 0,
@@ -143,6 +143,12 @@ typedef struct {
   const double* chol_flat;     /* (G, N*N) */
   const double* mf_shifts_im;  /* (G) imaginary parts of mf_shifts (real parts are 0) */
   const trot_mixed* mixed;     /* host struct of mixed-precision operands, or NULL */
+  /* (G, N(N+1)/2): the upper triangle of every chol[g], row-major packed (k(p, q) = p N -
+   * p (p - 1) / 2 + q - p, q >= p), when every chol[g] is exactly symmetric; else NULL.  The
+   * FP64 VHS (and its transpose contraction in the step VJP) then runs over the packed
+   * columns and is mirrored: half the FP64 products, the same values.  The FP64 step's and
+   * apply-Trotter's workspace grows by W N(N+1)/2 complex values. */
+  const double* chol_packed;
 } trot_system;
 
 /* Walker population.  Walkers are updated in place by the step. */

@@ -28,7 +28,7 @@ def test_header_symbols_exported():
 
 
 def test_abi_version():
-    assert _lib.load().trot_abi_version() == 3
+    assert _lib.load().trot_abi_version() == 4
 
 
 def _sys(**kw):

@@ -52,7 +52,7 @@ class TrotSystem(ctypes.Structure):
         ("weight_floor", _d), ("weight_cap", _d), ("pop_control_damping", _d),
         ("mo_a", _p), ("mo_b", _p), ("rot_h1_a", _p), ("rot_h1_b", _p),
         ("rot_chol_a", _p), ("rot_chol_b", _p), ("exp_h1_half", _p), ("chol_flat", _p),
-        ("mf_shifts_im", _p), ("mixed", _p),
+        ("mf_shifts_im", _p), ("mixed", _p), ("chol_packed", _p),
     ]
 
 
@@ -158,7 +158,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
-        if lib.trot_abi_version() != 3:
+        if lib.trot_abi_version() != 4:
             raise RuntimeError("trot_gb300 ABI version mismatch")
         _lib = lib
         return lib

@@ -37,6 +37,7 @@ from torch.utils.checkpoint import checkpoint
 
 from . import _lib, native
 from . import ctx as ctx_dev
+from .prop import pack_symmetric
 from .core import QmcParams
 from .trial import RhfTrial, UhfTrial
 
@@ -102,6 +103,7 @@ class AdjointProblem:
         mf_im, h0p, _, _ = ctx_dev.prop_ctx(self.h0, zero, self.chol, self.rdm1, self.params.dt)
         self.mf_im, self.h0_prop = mf_im, h0p
         self.chol_flat = self.chol.reshape(G, N * N)
+        self.chol_packed = pack_symmetric(self.chol)
 
     def system(self, exp_h1_half=None, rot_h1=(None, None)) -> _lib.TrotSystem:
         s = _lib.TrotSystem()
@@ -122,6 +124,7 @@ class AdjointProblem:
         s.rot_h1_b = native.ptr(rot_h1[1]) if self.kind == _lib.UHF_U else 0
         s.exp_h1_half = native.ptr(exp_h1_half)
         s.chol_flat = self.chol_flat.data_ptr()
+        s.chol_packed = native.ptr(self.chol_packed)
         s.mf_shifts_im = self.mf_im.data_ptr()
         return s
 

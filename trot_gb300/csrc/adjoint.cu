@@ -544,6 +544,7 @@ struct AdjCommon {
   const double* mo[2];
   const double* rot_h1[2];
   const double* rot_chol[2];
+  const double* chol_packed;  // packed upper triangle of the Cholesky vectors, or null
 };
 
 static int check_adj(const trot_system* s) {
@@ -579,6 +580,7 @@ static AdjCommon common_of(const trot_system* s) {
     a.rot_h1[q] = (q == 1 && uhf) ? s->rot_h1_b : s->rot_h1_a;
     a.rot_chol[q] = (q == 1 && uhf) ? s->rot_chol_b : s->rot_chol_a;
   }
+  a.chol_packed = s->chol_packed;
   return a;
 }
 
@@ -588,6 +590,7 @@ struct SpinWs {  // per-spin buffers of the step adjoint
 struct StepWs {
   SpinWs sp[2];
   double2 *fb, *xs, *st, *ft, *V, *Bc, *gV, *gxsv, *gfb, *kappa, *ov_new;
+  double2* vp;  // packed VHS, then the packed cotangent g_V + g_V^T (W, N(N+1)/2), with chol_packed
   double *wt_new, *wsum, *g_req, *g_c, *g_es, *opart;
   double2* kpart;  // split-K partials of the long-K products
   int* act;
@@ -629,6 +632,7 @@ static void carve_step(const AdjCommon& a, Carver& c, StepWs& b) {
   b.V = c.take<double2>(W * NN);
   b.Bc = c.take<double2>(NN);
   b.gV = c.take<double2>(W * NN);
+  if (a.chol_packed) b.vp = c.take<double2>(W * ((size_t)a.N * (a.N + 1) / 2));
   b.gxsv = c.take<double2>(W * G);
   b.gfb = c.take<double2>(W * G);
   b.kappa = c.take<double2>(W);
@@ -768,7 +772,7 @@ int trot_prop_step_vjp(const trot_system* s, const trot_state* in, const double*
                                     splitk_slices(W, G), st));
   }
   TROT_TRY(launch_fields(W, G, s->sqrt_dt, b.fb, s->mf_shifts_im, fields, b.xs, b.st, b.ft, st));
-  TROT_TRY(launch_zgemm_cr(W, (int)NN, G, 1.0, b.xs, G, s->chol_flat, (int)NN, false, b.V, (int)NN, false, st));
+  TROT_TRY(launch_vhs64(W, N, G, b.xs, s->chol_flat, a.chol_packed, b.vp, b.V, st));
   adj_to_complex_kernel<<<grid_of(NN), 256, 0, st>>>(NN, s->exp_h1_half, b.Bc);
   TROT_CHECK_LAUNCH("adj_to_complex_kernel");
   double2 ck[8];
@@ -866,9 +870,17 @@ int trot_prop_step_vjp(const trot_system* s, const trot_state* in, const double*
     TROT_TRY(outer_sum(W, N, n, x.gw1, x.wz, b.opart, g_exp_h1_half, st));
     TROT_TRY(zgemm_batched(W, N, n, N, one, b.Bc, 0, N, 1, x.gw1, sw, n, 0, zero, gin[q], sw, n, st));
   }
-  // V = sum_g xs_g L_g: g_xs^V[b][g] = sum_pq L_g[pq] g_V[b][pq]
-  TROT_TRY(launch_zgemm_cr_splitk(W, G, (int)NN, 1.0, b.gV, (int)NN, s->chol_flat, (int)NN, true, b.gxsv, G, false,
-                                  b.kpart, splitk_slices(W, G), st));
+  // V = sum_g xs_g L_g: g_xs^V[b][g] = sum_pq L_g[pq] g_V[b][pq] (with symmetric L_g: over the packed
+  // upper triangle of g_V + g_V^T, half the FP64 products)
+  if (a.chol_packed) {
+    const int P = N * (N + 1) / 2;
+    TROT_TRY(launch_pack_sym(N, W, b.gV, b.vp, st));
+    TROT_TRY(launch_zgemm_cr_splitk(W, G, P, 1.0, b.vp, P, a.chol_packed, P, true, b.gxsv, G, false, b.kpart,
+                                    splitk_slices(W, G), st));
+  } else {
+    TROT_TRY(launch_zgemm_cr_splitk(W, G, (int)NN, 1.0, b.gV, (int)NN, s->chol_flat, (int)NN, true, b.gxsv, G,
+                                    false, b.kpart, splitk_slices(W, G), st));
+  }
   adj_fields_kernel<<<grid_of((size_t)W * G), 256, 0, st>>>(W, G, s->sqrt_dt, s->mf_shifts_im, b.xs, b.gxsv, b.g_req,
                                                              b.g_c, b.gfb);
   TROT_CHECK_LAUNCH("adj_fields_kernel");

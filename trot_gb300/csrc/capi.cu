@@ -59,6 +59,7 @@ static size_t carve_step(const trot_system* s, const Spins& sp, Carver& c, StepB
   if (op == TROT_OP_LOCAL_ENERGY || op == TROT_OP_PROP_STEP) b.exc = c.take<double2>(W * exchange_chunks((int)G));
   if (op == TROT_OP_APPLY_TROTTER || op == TROT_OP_PROP_STEP) {
     b.vhs = c.take<double2>(W * N * N);
+    if (s->chol_packed) b.vp = c.take<double2>(W * (N * (N + 1) / 2));
   }
   if (op == TROT_OP_PROP_STEP) {
     b.xs = c.take<double2>(W * G);
@@ -292,8 +293,7 @@ int trot_apply_trotter(const trot_system* s, const double* wa, const double* wb,
   StepBuffers b;
   carve_step(s, sp, c, b, TROT_OP_APPLY_TROTTER);
   if (!c.ok) { set_error("workspace too small: %zu < %zu", ws_bytes, c.used); return TROT_ERR_WORKSPACE_TOO_SMALL; }
-  TROT_TRY(launch_zgemm_cr(W, N * N, G, 1.0, (const double2*)xs, G, s->chol_flat, N * N, false, b.vhs, N * N,
-                           false, st));
+  TROT_TRY(launch_vhs64(W, N, G, (const double2*)xs, s->chol_flat, s->chol_packed, b.vp, b.vhs, st));
   a.vhs = b.vhs;
   return launch_trotter(sp, a, st);
 }
@@ -333,7 +333,7 @@ int trot_prop_step(const trot_system* s, const trot_state* state, const double* 
   // 4. shifted fields
   TROT_TIMED("fields", st, launch_fields(W, G, s->sqrt_dt, b.fb, s->mf_shifts_im, fields, b.xs, b.shift_term, b.fb_term, st));
   // 5. VHS
-  TROT_TIMED("vhs_fp64", st, launch_zgemm_cr(W, N * N, G, 1.0, b.xs, G, s->chol_flat, N * N, false, b.vhs, N * N, false, st));
+  TROT_TIMED("vhs_fp64", st, launch_vhs64(W, N, G, b.xs, s->chol_flat, s->chol_packed, b.vp, b.vhs, st));
   // 6. propagation + overlaps + weights
   TrotterArgs a{};
   a.W = W; a.N = N; a.G = G; a.nterms = s->n_exp_terms; a.sqrt_dt = s->sqrt_dt; a.expH = s->exp_h1_half;

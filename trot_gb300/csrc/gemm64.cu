@@ -134,4 +134,57 @@ int launch_zgemm_cr_splitk(int M, int Nn, int K, double alpha, const double2* A,
   return TROT_OK;
 }
 
+
+// ------------------------------------------------------------------ packed symmetric VHS
+// With every L_g symmetric, V_b = sum_g xs[b][g] L_g is symmetric: its upper triangle
+// (row-major packed columns k(p, q) = p N - p (p - 1) / 2 + q - p, q >= p) is one product over
+// the N (N + 1) / 2 packed columns of the Cholesky vectors, mirrored into the full matrix:
+// half the FP64 products, and every element is the same dot product over g as in the full
+// product, so the values are identical.
+__global__ void vhs_unpack_kernel(int W, int N, const double2* __restrict__ vp, double2* __restrict__ vhs) {
+  const size_t P = (size_t)N * (N + 1) / 2, total = (size_t)W * N * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t b = e / ((size_t)N * N);
+    const int r = (int)(e % ((size_t)N * N)), i = r / N, j = r % N;
+    const int p = i < j ? i : j, q = i < j ? j : i;
+    vhs[e] = vp[b * P + (size_t)p * N - (size_t)p * (p - 1) / 2 + (q - p)];
+  }
+}
+
+// Mp[b][k(i, j)] = M[b][i][j] + M[b][j][i] off the diagonal, M[b][i][i] on it: with a
+// symmetric L, sum_ij L[i][j] M[i][j] = sum_{i <= j} L[i][j] Mp[k(i, j)].
+__global__ void pack_sym_kernel(int N, int W, const double2* __restrict__ m, double2* __restrict__ mp) {
+  const size_t P = (size_t)N * (N + 1) / 2, total = (size_t)W * N * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t b = e / ((size_t)N * N);
+    const int r = (int)(e % ((size_t)N * N)), i = r / N, j = r % N;
+    if (j < i) continue;
+    double2 v = m[e];
+    if (j > i) v = cadd(v, m[b * N * N + (size_t)j * N + i]);
+    mp[b * P + (size_t)i * N - (size_t)i * (i - 1) / 2 + (j - i)] = v;
+  }
+}
+
+static int grid_1d(size_t total) {
+  const size_t b = (total + 255) / 256;
+  return (int)(b < 152 * 32 ? (b > 0 ? b : 1) : 152 * 32);
+}
+
+int launch_vhs64(int W, int N, int G, const double2* xs, const double* chol_flat, const double* chol_packed,
+                 double2* vp, double2* vhs, cudaStream_t st) {
+  if (!chol_packed || !vp)
+    return launch_zgemm_cr(W, N * N, G, 1.0, xs, G, chol_flat, N * N, false, vhs, N * N, false, st);
+  const int P = N * (N + 1) / 2;
+  TROT_TRY(launch_zgemm_cr(W, P, G, 1.0, xs, G, chol_packed, P, false, vp, P, false, st));
+  vhs_unpack_kernel<<<grid_1d((size_t)W * N * N), 256, 0, st>>>(W, N, vp, vhs);
+  TROT_CHECK_LAUNCH("vhs_unpack_kernel");
+  return TROT_OK;
+}
+
+int launch_pack_sym(int N, int W, const double2* m, double2* mp, cudaStream_t st) {
+  pack_sym_kernel<<<grid_1d((size_t)W * N * N), 256, 0, st>>>(N, W, m, mp);
+  TROT_CHECK_LAUNCH("pack_sym_kernel");
+  return TROT_OK;
+}
+
 }  // namespace trot

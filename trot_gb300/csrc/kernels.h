@@ -31,6 +31,7 @@ struct Carver {
 
 struct StepBuffers {
   double2 *green, *e1, *fb, *xs, *shift_term, *fb_term, *vhs, *exc;
+  double2* vp;  // packed upper triangle of the VHS (W, N(N+1)/2) when chol_packed is set
   int* node_flag;
 };
 
@@ -54,6 +55,12 @@ int launch_zgemm_cr(int M, int Nn, int K, double alpha, const double2* A, int ld
 int launch_zgemm_cr_splitk(int M, int Nn, int K, double alpha, const double2* A, int lda, const double* B, int ldb,
                            bool b_is_nk, double2* C, int ldc, bool accumulate, double2* part, int S,
                            cudaStream_t st);
+// FP64 VHS = xs . chol (W x N^2): over the packed upper triangle (then mirrored) when
+// chol_packed and vp (W x N(N+1)/2 complex scratch) are given, else the full product.
+int launch_vhs64(int W, int N, int G, const double2* xs, const double* chol_flat, const double* chol_packed,
+                 double2* vp, double2* vhs, cudaStream_t st);
+// Mp = the packed upper triangle of M + M^T (diagonal once), W matrices of N x N.
+int launch_pack_sym(int N, int W, const double2* m, double2* mp, cudaStream_t st);
 
 // step64.cu
 int launch_fields(int W, int G, double sqrt_dt, const double2* fb, const double* mf_im,

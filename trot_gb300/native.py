@@ -123,6 +123,7 @@ def system(kind, n_walkers, trial, meas_ctx=None, prop_ctx=None, h0=0.0, params=
         s.nchol = int(prop_ctx.chol_flat.shape[0])
         s.exp_h1_half = ptr(prop_ctx.exp_h1_half)
         s.chol_flat = ptr(prop_ctx.chol_flat)
+        s.chol_packed = ptr(getattr(prop_ctx, "chol_packed", None))
         s.mf_shifts_im = ptr(prop_ctx.mf_shifts_im)
         s.h0_prop = float(prop_ctx.h0_prop)
         s.dt = float(prop_ctx.dt)

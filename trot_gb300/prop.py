@@ -34,6 +34,9 @@ class CholAfqmcCtx:
     h0_prop: float
     chol_flat: torch.Tensor  # (G, N*N) float64
     norb: int
+    # (G, N(N+1)/2) upper triangles when every chol[g] is exactly symmetric (the FP64 VHS is then
+    # built over the packed columns: half the products, identical values), else None
+    chol_packed: torch.Tensor | None = None
 
     @property
     def mf_shifts(self) -> torch.Tensor:
@@ -49,7 +52,17 @@ def _build_prop_ctx(ham_data: HamChol, rdm1, dt: float, mixed_precision: bool = 
     mf_im, h0_prop, eh, chol = ctx_dev.prop_ctx(h0, ham_data.h1, ham_data.chol, rdm1, dt)
     G, N = int(chol.shape[0]), int(chol.shape[1])
     return CholAfqmcCtx(dt=float(dt), sqrt_dt=float(np.sqrt(dt)), exp_h1_half=eh, mf_shifts_im=mf_im,
-                        h0_prop=h0_prop, chol_flat=chol.reshape(G, N * N), norb=N)
+                        h0_prop=h0_prop, chol_flat=chol.reshape(G, N * N), norb=N, chol_packed=pack_symmetric(chol))
+
+
+def pack_symmetric(chol: torch.Tensor) -> torch.Tensor | None:
+    """Row-major packed upper triangles (G, N(N+1)/2) of the Cholesky vectors when every
+    chol[g] is exactly symmetric, else None."""
+    N = int(chol.shape[1])
+    if N == 0 or not bool(torch.equal(chol, chol.transpose(1, 2))):
+        return None
+    iu = torch.triu_indices(N, N, device=chol.device)
+    return chol[:, iu[0], iu[1]].contiguous()
 
 
 class TrotterOps(NamedTuple):
@@ -85,6 +98,7 @@ def make_trotter_ops(ham_basis: str, walker_kind: str, mixed_precision: bool = F
         s.n_exp_terms = int(n_terms)
         s.sqrt_dt, s.dt = ctx.sqrt_dt, ctx.dt
         s.exp_h1_half, s.chol_flat = native.ptr(ctx.exp_h1_half), native.ptr(ctx.chol_flat)
+        s.chol_packed = native.ptr(ctx.chol_packed)
         s.mf_shifts_im = native.ptr(ctx.mf_shifts_im)
         if prec == _lib.MIXED:
             from . import mixed

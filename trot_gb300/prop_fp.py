@@ -21,7 +21,8 @@ def build_prop_ctx_fp(ham_data, rdm1, dt: float, ene0: float, mixed_precision: b
     context with h0_prop shifted by ene0."""
     ctx = _build_prop_ctx(ham_data, rdm1, dt, mixed_precision=mixed_precision)
     return CholAfqmcCtx(dt=ctx.dt, sqrt_dt=ctx.sqrt_dt, exp_h1_half=ctx.exp_h1_half, mf_shifts_im=ctx.mf_shifts_im,
-                        h0_prop=ctx.h0_prop + float(ene0), chol_flat=ctx.chol_flat, norb=ctx.norb)
+                        h0_prop=ctx.h0_prop + float(ene0), chol_flat=ctx.chol_flat, norb=ctx.norb,
+                        chol_packed=ctx.chol_packed)
 
 
 def afqmc_step_fp(state: PropState, sys: System, *, params, ham_data, trial_data, prop_ctx: CholAfqmcCtx,
