@@ -217,3 +217,75 @@ def test_chunked_reader(tmp_path, filters):
     with h5file.File(p) as f:
         assert f["x"].extent() is None
         assert _eq(np.asarray(f["x"]), arr)
+
+
+def _v2_file(path, arr, sub):
+    """A file in the newer format (as libver="latest" writers lay it out): superblock
+    version 2, version-2 object headers (OHDR, one continuation chunk OCHK), groups held
+    as link messages, a version-3 attribute, a version-2 dataspace and a version-3
+    fill-value message. Checksums are left zero (the reader does not verify them)."""
+    buf = bytearray(b"\0" * 48)  # superblock, written last
+
+    def put(b):
+        while len(buf) % 8:
+            buf.append(0)
+        at = len(buf)
+        buf.extend(b)
+        return at
+
+    def msg(t, data, flags=0):
+        return struct.pack("<BHB", t, len(data), flags) + data
+
+    def ohdr(msgs):
+        body = b"".join(msgs)
+        return b"OHDR" + bytes([2, 0x02]) + struct.pack("<I", len(body)) + body + b"\0" * 4  # 4-byte chunk size
+
+    def dataset(a):
+        data_at = put(a.tobytes())
+        space = bytes([2, a.ndim, 0, 1]) + struct.pack(f"<{a.ndim}Q", *a.shape)
+        layout = struct.pack("<BBQQ", 3, 1, data_at, a.nbytes)
+        fill = bytes([3, 0x09])  # version 3: early allocation, never write fill values
+        return put(ohdr([msg(0x01, space), msg(0x03, h5file._encode_dtype(a.dtype), 1), msg(0x05, fill),
+                         msg(0x08, layout)]))
+
+    def link(name, addr):
+        nb = name.encode()
+        return bytes([1, 0x00]) + bytes([len(nb)]) + nb + struct.pack("<Q", addr)  # 1-byte name length, hard link
+
+    x_at, y_at = dataset(arr), dataset(sub)
+    linfo = bytes([0, 0]) + struct.pack("<QQ", h5file.UNDEF, h5file.UNDEF)  # compact storage
+    g_at = put(ohdr([msg(0x02, linfo), msg(0x06, link("y", y_at))]))
+    # continuation chunk with one more link
+    cont_body = msg(0x06, link("g", g_at))
+    cont_at = put(b"OCHK" + cont_body + b"\0" * 4)
+    attr_name = b"units\0"
+    attr_dt = h5file._encode_dtype(np.dtype("<i8"))
+    attr_space = bytes([2, 0, 0, 0])  # scalar
+    attr = (bytes([3, 0]) + struct.pack("<HHH", len(attr_name), len(attr_dt), len(attr_space)) + bytes([0])
+            + attr_name + attr_dt + attr_space + struct.pack("<q", 42))
+    root_at = put(ohdr([msg(0x02, linfo), msg(0x06, link("x", x_at)), msg(0x0C, attr),
+                        msg(0x10, struct.pack("<QQ", cont_at, len(cont_body) + 8))]))
+    eof = len(buf)
+    sb = h5file.SIGNATURE + bytes([2, 8, 8, 0]) + struct.pack("<QQQQ", 0, h5file.UNDEF, eof, root_at) + b"\0" * 4
+    buf[:48] = sb
+    with open(path, "wb") as f:
+        f.write(bytes(buf))
+
+
+def test_reader_newer_format(tmp_path):
+    rng = np.random.default_rng(9)
+    arr, sub = rng.normal(size=(4, 3)), np.arange(7, dtype=np.int64)
+    p = tmp_path / "v2.h5"
+    _v2_file(p, arr, sub)
+    with h5file.File(p) as f:
+        assert sorted(f.keys()) == ["g", "x"]
+        assert f.attrs["units"] == 42
+        assert _eq(np.asarray(f["x"]), arr) and f["x"].extent() is not None
+        assert isinstance(f["g"], h5file.Group) and f["g"].keys() == ["y"]
+        assert _eq(f["g/y"][...], sub)
+
+
+def test_loaded_arrays_are_writable():
+    got = staging.load(os.path.join(GOLDEN, "staged_rhf.h5"))
+    got.ham.h1[0, 0] += 1.0  # h5py hands out writable arrays too
+    assert got.ham.chol.flags.writeable and got.trial.data["mo"].flags.writeable

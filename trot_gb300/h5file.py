@@ -471,7 +471,14 @@ class Dataset:
             addr = struct.unpack_from("<Q", lay, 2 if ver >= 3 else 8)[0]
             if addr == UNDEF or n == 0:
                 return rd.decode_values(b"\0" * (n * isz), dt, self.shape)
-            return rd.decode_values(rd.ra(addr, n * isz), dt, self.shape)
+            if dt is _VlenStr:
+                return rd.decode_values(rd.ra(addr, n * isz), dt, self.shape)
+            out = np.empty(self.shape, dtype=dt)  # writable, filled by one positioned read
+            view = memoryview(out.reshape(-1).view(np.uint8))
+            got = os.preadv(rd.fh.fileno(), [view], rd.base + addr)
+            if got != n * isz:
+                raise OSError(f"{self.name}: short read ({got} of {n * isz} bytes)")
+            return out
         if cls == 2:
             if ver >= 4:
                 raise NotImplementedError("version-4 chunk indexes")
