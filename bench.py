@@ -679,6 +679,52 @@ def staged_load_leg(norb=256, nchol=2000, reps=3):
             "device_copy_matches_file": ok}
 
 
+def cisd_leg(steps=10, warmup=3, fp64_steps=2):
+    """Config 4 (CISD trial, N=60, 8+8 electrons, G=300, W=256) beside the headline: mixed
+    (the reference's default CISD dtypes, tensor-core propagation) and FP64 walker-steps/s
+    with E_L each step, timed with CUDA events like the headline, and the mixed-vs-FP64
+    E_L difference on walkers near the trial. Errors are recorded, not raised."""
+    import torch
+
+    from trot_gb300.synthetic import CONFIGS
+
+    cfg = CONFIGS["cfg4_cisd_n60"]
+    W = cfg["n_walkers"]
+    out = {"workload": f"cisd N={cfg['norb']} nocc={cfg['nelec'][0]} G={cfg['nchol']} W={W} dt={cfg['dt']} "
+                       f"qr/sr every {cfg['qr_every']}, prop + E_L each step"}
+    try:
+        for prec, n in (("mixed", steps), ("fp64", fp64_steps)):
+            wl = build_workload(cfg, prec)
+            run_steps(wl, warmup)
+            torch.cuda.synchronize()
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a0.record()
+            run_steps(wl, n, k0=warmup)
+            a1.record()
+            torch.cuda.synchronize()
+            ms = a0.elapsed_time(a1)
+            out[prec] = {"value": W * n / (ms / 1e3), "unit": UNIT, "steps": n, "ms_per_step": ms / n}
+            if prec == "mixed":
+                import trot_gb300 as tg
+
+                m64 = tg.make_cisd_meas_ops(wl["sys"], mixed_precision=False, testing=True)
+                mc64 = m64.build_meas_ctx(wl["ham"], wl["trial"])
+                near = {}
+                for noise in (0.05, 0.3):
+                    wn = perturbed_trial_walkers(wl, noise)
+                    a64 = m64.kernels["energy"](wn, wl["ham"], mc64, wl["trial"])
+                    amx = wl["meas_ops"].kernels["energy"](wn, wl["ham"], wl["meas_ctx"], wl["trial"])
+                    dd = (amx - a64).abs()
+                    near[f"noise_{noise}"] = {"max_abs_dE_L_Ha": float(dd.max()),
+                                              "max_abs_E_L_Ha": float(a64.abs().max())}
+                out["precision_near_trial"] = near
+            del wl
+        out["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    except Exception as exc:  # the headline line must still print
+        out["error"] = f"{type(exc).__name__}: {exc}"
+    return out
+
+
 def cpu_cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -708,6 +754,7 @@ def main():
                     help="run only the mixed-vs-FP64 trajectory comparison and print its JSON")
     ap.add_argument("--no-fragments", action="store_true", help="skip the 24-fragment batch leg")
     ap.add_argument("--no-staged", action="store_true", help="skip the staged-input cache -> HBM leg")
+    ap.add_argument("--no-cisd", action="store_true", help="skip the CISD (config 4) leg")
     ap.add_argument("--staged-only", action="store_true", help="run only the staged-input cache -> HBM leg")
     ap.add_argument("--fragments-only", action="store_true",
                     help="run only the 24-fragment batch leg and print its JSON")
@@ -959,6 +1006,8 @@ def main():
         line["fragments"] = fragments_leg()
     if not args.no_staged and rank == 0 and world == 1 and args.config == "cfg2_uhf_n120":
         line["staged_load"] = staged_load_leg()
+    if not args.no_cisd and rank == 0 and world == 1 and args.config == "cfg2_uhf_n120":
+        line["cisd"] = cisd_leg()
     if not args.no_cpu_baseline:
         sample = args.cpu_sample or 64
         r, secs, ks = cpu_port_rate(cfg, sample, 2, min_seconds=10.0)
