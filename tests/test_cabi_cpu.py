@@ -198,3 +198,18 @@ def test_cisd_packed_contraction_workspace():
     assert lib.trot_cisd_workspace_size(ctypes.byref(_cisd(gl_precision=_lib.MIXED, **big)), 8,
                                         _lib.OP_LOCAL_ENERGY) == 0
     assert b"exceeds shared memory" in lib.trot_last_error()
+
+
+def test_packed_vhs_workspace():
+    """With chol_packed set, the FP64 step and apply-Trotter workspaces carry the packed VHS
+    (W N(N+1)/2 complex values, up to the carver's alignment); the other ops are unchanged."""
+    lib = _lib.load()
+    W, N = 40, 30
+    full, packed = _sys(n_walkers=W, norb=N), _sys(n_walkers=W, norb=N, chol_packed=0x2000)
+    extra = W * N * (N + 1) // 2 * 16
+    for op in (_lib.OP_PROP_STEP, _lib.OP_APPLY_TROTTER):
+        a = lib.trot_workspace_size(ctypes.byref(full), op)
+        b = lib.trot_workspace_size(ctypes.byref(packed), op)
+        assert extra <= b - a <= extra + 512, (op, a, b)
+    for op in (_lib.OP_FORCE_BIAS, _lib.OP_LOCAL_ENERGY):
+        assert lib.trot_workspace_size(ctypes.byref(full), op) == lib.trot_workspace_size(ctypes.byref(packed), op)
