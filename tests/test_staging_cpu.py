@@ -289,3 +289,20 @@ def test_loaded_arrays_are_writable():
     got = staging.load(os.path.join(GOLDEN, "staged_rhf.h5"))
     got.ham.h1[0, 0] += 1.0  # h5py hands out writable arrays too
     assert got.ham.chol.flags.writeable and got.trial.data["mo"].flags.writeable
+
+
+def test_large_string_attributes_and_unicode_names(tmp_path):
+    big = "ψ" * 6000 + "end"  # > 4 KB of UTF-8: the global heap collection grows past its minimum
+    meta = json.dumps({"basis": "cc-pVTZ", "notes": "x" * 9000})
+    p = tmp_path / "u.h5"
+    with h5file.File(p, "w") as f:
+        f.attrs["meta_json"] = meta
+        g = f.create_group("données")
+        g.attrs["big"] = big
+        g.attrs["small"] = "ok"
+        g.create_dataset("énergie", data=np.arange(3.0))
+    with h5file.File(p) as f:
+        assert f.attrs["meta_json"] == meta
+        g = f["données"]
+        assert g.attrs["big"] == big and g.attrs["small"] == "ok"
+        assert _eq(g["énergie"][...], np.arange(3.0))
